@@ -1,0 +1,151 @@
+/*
+ * m3sph.h - C ABI of the GB300 library for M3TET_SPH's time-step hot path.
+ *
+ * Plain pointers and sizes only. Array layouts are the reference's MATLAB column-major ones:
+ * EL2NOD is 10 x nel uint32 (1-based, element-major: the 10 nodes of element e are contiguous),
+ * GCOORD / GCOORD_SPH are 3 x nnod double, velocity vectors are dof-interleaved
+ * (dof 3*(node-1)+{1,2,3}, nod2dof.m). Every entry point returns an int status (M3SPH_OK = 0)
+ * and never throws; m3sph_last_error() describes the last failure of the calling thread.
+ * Host arrays are borrowed for the duration of a call; results go into caller-provided buffers.
+ * Handles own their device memory and one CUDA stream; calls on one handle are not reentrant.
+ */
+#ifndef M3SPH_H
+#define M3SPH_H
+#include <stdint.h>
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define M3SPH_API __attribute__((visibility("default")))
+#else
+#define M3SPH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  M3SPH_OK = 0,
+  M3SPH_ERR_BAD_INPUT = 1,
+  M3SPH_ERR_CUDA = 2,
+  M3SPH_ERR_NAN = 3,            /* NaN in a right-hand side or solution */
+  M3SPH_ERR_NOT_CONVERGED = 4,  /* iteration limit reached above tolerance */
+  M3SPH_ERR_NEGATIVE_JACOBIAN = 5,
+  M3SPH_ERR_POINT_NOT_FOUND = 6,
+  M3SPH_ERR_NO_DEVICE = 7
+};
+
+/* element classes (tetmesh_p1_to_p2_sph.m:183-189) */
+enum { M3SPH_OUT_CONE_NO_CROSS_2PI = 0, M3SPH_OUT_CONE_CROSS_2PI = 1,
+       M3SPH_IN_CONE_NO_ISO = 2, M3SPH_IN_CONE_ISO = 3 };
+
+/* One multigrid level of the reference MESH struct (init_mesh_curved_p.m:182-217).
+ * Level 0 is the finest (MESH.EL2NOD{1}); level nmg-1 the coarsest. The nodes of a coarse
+ * level are the first nnod nodes of the next finer level, and the children of coarse element
+ * e (1-based) are fine elements 8(e-1)+1 .. 8e (tetmesh_p2_to_p1.m). */
+typedef struct m3sph_level {
+  int32_t nel;                  /* number of P2 tetrahedra */
+  int32_t nnod;                 /* number of P2 nodes */
+  int32_t nvnod;                /* number of vertex (pressure) nodes */
+  const uint32_t *EL2NOD;       /* 10 x nel, 1-based */
+  const uint8_t *isplit;        /* nel, split (1..3) that made the next finer level; NULL on level 0 */
+  /* geometry: required on level 0 only (NULL elsewhere) */
+  const double *GCOORD;         /* 3 x nnod Cartesian */
+  const double *GCOORD_SPH;     /* 3 x nnod (theta, phi, r) */
+  const uint8_t *elclass;       /* nel, M3SPH_* element class */
+  int32_t niso;                 /* number of in-cone isoparametric elements */
+  const uint32_t *els_iso;      /* niso, 1-based element ids */
+  const double *cubic_sph_rot;  /* niso x 3 x 20 (theta,phi,r) of the 20 cubic nodes, X-90 frame */
+} m3sph_level;
+
+typedef struct m3sph_mesh m3sph_mesh;   /* opaque: device-resident MESH + MG hierarchy */
+
+/* Physical parameters used by the element operator (PHYSICS, NUMSCALE fields). */
+typedef struct m3sph_physics {
+  double g;          /* PHYSICS.g (e.g. -9.81) */
+  double Bscale;     /* NUMSCALE.Bscale */
+  double Dens0;      /* NUMSCALE.Dens0 */
+  double minVisc;    /* PHYSICS.minVisc (<=0: no clamp) */
+  double maxVisc;    /* PHYSICS.maxVisc (<=0: no clamp) */
+} m3sph_physics;
+
+/* Solver options (flow3d_patera_mg_sph_p.m:70-129, mgpcg_solver_p.m:620-724). */
+typedef struct m3sph_opts {
+  double rtol_Pat;      /* 1e-4 in the reference */
+  double rtol_U;        /* 5e-3 */
+  int32_t itmax_Pat;    /* 120 */
+  int32_t itmin_Pat;    /* 3 */
+  int32_t itmax_U;      /* 20 */
+  int32_t precision;    /* 0: plain FP64 everywhere; 1: FP32 V-cycle inside FP64 outer CG */
+  int32_t smoother;     /* 0: weighted Jacobi; 1: learned element smoother on the 2 finest levels */
+  double target_rel_residual; /* >0: keep iterating Patera until the coupled FP64 residual is below */
+} m3sph_opts;
+
+typedef struct m3sph_info {
+  int32_t itPat;            /* Patera iterations */
+  int32_t nitU;             /* velocity MG-PCG iterations (initial + restarts + final) */
+  int32_t nitZ;             /* MG-PCG iterations inside Patera */
+  int32_t nvcycle;          /* V-cycles applied */
+  double norm_rP;           /* final pressure residual (normdf) */
+  double rel_residual;      /* coupled FP64 relative residual on free dofs, pressure mean removed */
+  double t_setup_ms;        /* element matrices, Galerkin, coarse factorisation */
+  double t_iter_ms;         /* Patera + MG-PCG iterations */
+  int32_t smoother_fallbacks; /* times the learned smoother was replaced by Jacobi */
+  int32_t status;
+} m3sph_info;
+
+M3SPH_API const char *m3sph_last_error(void);
+M3SPH_API int m3sph_device_count(int *count);
+
+/* Build the device-resident mesh + MG hierarchy (init_mesh_curved_p / create_multigrid_meshes_3d_sph
+ * outputs). Computes per-node rotations (make_rotation_matrix.m), element colours, and the
+ * intermesh transfer operators (intermesh_transfer_matrix.m:1-62). */
+M3SPH_API int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t device, m3sph_mesh **out);
+M3SPH_API int m3sph_mesh_destroy(m3sph_mesh *mesh);
+/* number of element colours of level `img` (0-based) */
+M3SPH_API int m3sph_mesh_ncolors(const m3sph_mesh *mesh, int32_t img, int32_t *ncolors);
+
+/* Set the velocity boundary conditions in the rotated (theta,phi,r) frame (UBC.ifix/vfix,
+ * 1-based dof ids as in bc_sph.m) and the nodal viscosity / density (VAR.Visc, VAR.Dens,
+ * nnod each; only vertex values are used, calc_element_visc.m:5-7). Recomputes the element
+ * operator (assembly_stokes_sph_3d_double_jacobian.m), the Galerkin coarse operators
+ * (restrict_stiffmat.m) and the coarse factorisation (cholesky_factorization.m). */
+M3SPH_API int m3sph_stokes_setup(m3sph_mesh *mesh, const double *Visc, const double *Dens, const int32_t *ifix,
+                       const double *vfix, int32_t nfix, const m3sph_physics *phys, int32_t precision);
+
+/* Replaces flow3d_patera_mg_sph_p (flow3d_patera_mg_sph_p.m:1-780): Patera pressure CG around
+ * MG-PCG. P (nvnod) is the initial pressure on input and the solution on output; U_xyz (3*nnod,
+ * dof-interleaved Cartesian) receives the velocity. */
+M3SPH_API int m3sph_stokes_solve(m3sph_mesh *mesh, double *U_xyz, double *P, const m3sph_opts *opts,
+                       m3sph_info *info);
+
+/* Replaces one mgpcg_solver_p call (mgpcg_solver_p.m:1-743) on the current operator: solves
+ * K1 x = b on the free dofs of the rotated frame (b, x: 3*nnod, fixed dofs ignored / zero).
+ * tol is absolute on normdf(r) if is_abs_tol, else relative to the initial residual. */
+M3SPH_API int m3sph_mgpcg(m3sph_mesh *mesh, const double *b, double *x, double tol, int32_t is_abs_tol,
+                int32_t itmax, int32_t *itCG, double *rrms_final);
+
+/* Operator-level entry points (replace MUTILS spmv on the assembled matrices):
+ * y = K1 x with K1 = RR' K RR on free dofs (fixed dofs give 0), x,y 3*nnod rotated frame. */
+M3SPH_API int m3sph_stokes_apply(m3sph_mesh *mesh, const double *x, double *y);
+/* y = GG q (3*nnod <- nvnod, rotated frame) and s = GG' z (nvnod <- 3*nnod) */
+M3SPH_API int m3sph_grad_apply(m3sph_mesh *mesh, const double *q, double *y);
+M3SPH_API int m3sph_div_apply(m3sph_mesh *mesh, const double *z, double *s);
+/* Buoyancy force vector Fb = RR' Fb_xyz (3*nnod) */
+M3SPH_API int m3sph_force_vector(m3sph_mesh *mesh, double *Fb);
+/* Copy out the element matrices of level 0 in the rotated, BC-masked frame:
+ * K: nel x 900 (full 30x30, row-major), G: nel x 120 (30x4 row-major), M: nel x 16. */
+M3SPH_API int m3sph_element_matrices(m3sph_mesh *mesh, double *K, double *G, double *M);
+/* y = KK{img} x on level img (0-based, img>=1: Galerkin coarse operator), vectors 3*nnod(img) */
+M3SPH_API int m3sph_level_apply(m3sph_mesh *mesh, int32_t img, const double *x, double *y);
+/* Ic2f{img} (intermesh_transfer_matrix): prolong x_c (3*nnod(img+1)) -> x_f (3*nnod(img)) and
+ * restrict r_f -> r_c with Ic2f' (free-dof masked as in restrict_stiffmat.m:94-96). */
+M3SPH_API int m3sph_prolong(m3sph_mesh *mesh, int32_t img, const double *xc, double *xf);
+M3SPH_API int m3sph_restrict(m3sph_mesh *mesh, int32_t img, const double *rf, double *rc);
+/* One V-cycle (MG_V_cycle_v2, mgpcg_solver_p.m:388-596) in the setup precision: d = B r. */
+M3SPH_API int m3sph_vcycle(m3sph_mesh *mesh, const double *r, double *d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* M3SPH_H */

@@ -1,0 +1,128 @@
+// Shared device/host declarations of the m3sph CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/m3sph.h"
+
+namespace m3sph {
+
+constexpr int NNODEL = 10;        // P2 velocity nodes per element
+constexpr int NUDOF = 30;         // velocity dofs per element
+constexpr int NPACK = 465;        // packed lower triangle of a 30x30 symmetric matrix
+constexpr int NIP = 14;           // quadrature points (ip_tetrahedron.m:100-123)
+constexpr int MAX_COLORS = 128;
+
+// packed lower-triangle index of (r, c), r >= c, column-major (MUTILS sparse_create layout)
+__host__ __device__ constexpr int pack_idx(int r, int c) { return c * (2 * NUDOF - c + 1) / 2 + (r - c); }
+
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define M3_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t _e = (call);                           \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+// quadrature / shape-function tables (computed on the host, copied to constant memory)
+struct ShapeTables {
+  double ipw[NIP];
+  double NP[NIP][4];
+  double NU[NIP][10];
+  double dNU[NIP][10][3];
+  double N20[NIP][20];
+  double dN20[NIP][20][3];
+};
+void build_shape_tables(ShapeTables &t);
+int upload_shape_tables();
+
+// device buffers of one multigrid level
+struct Level {
+  int nel = 0, nnod = 0, nvnod = 0, ndof = 0;
+  int nfree = 0;
+  std::vector<int> cstart;            // colour ranges in stored element order (host)
+  int *el2nod = nullptr;              // [10][nel], 0-based, stored (colour) order
+  int *perm = nullptr;                // stored -> original element id
+  int *invperm = nullptr;             // original -> stored
+  uint8_t *freemask = nullptr;        // [ndof], 1 = free dof
+  double *K64 = nullptr;              // [465][nel] rotated, masked element matrices
+  float *K32 = nullptr;
+  double *Dinv64 = nullptr;           // [ndof] inverse diagonal (0 on fixed dofs)
+  float *Dinv32 = nullptr;
+  // children (coarse levels): fine stored index of child k, and parent-local vertex indices
+  int *child = nullptr;               // [8][nel]
+  uint32_t *child_vloc = nullptr;     // [8][nel], 4 x 4-bit parent-local node index (0..9)
+  // transfer to the next coarser level (levels 0..nmg-2)
+  int *P_ptr = nullptr, *P_col = nullptr;   // fine node rows
+  float *P_w = nullptr;
+  int *R_ptr = nullptr, *R_col = nullptr;   // coarse node rows (transpose)
+  float *R_w = nullptr;
+  // host copies needed at set-up
+  std::vector<int> h_el2nod_orig;     // [nel][10] original order, 0-based
+};
+
+struct Finest {
+  double *gcoord = nullptr;           // [3][nnod]
+  double *gcoord_sph = nullptr;       // [3][nnod]
+  double *RR = nullptr;               // [9][nnod] (theta,phi,r)->(x,y,z), row-major 3x3
+  uint8_t *cls = nullptr;             // [nel] stored order
+  int *iso_slot = nullptr;            // [nel] stored order, -1 if not iso
+  double *cubic = nullptr;            // [60][niso] (theta,phi,r) x 20 nodes, X-90 frame
+  int niso = 0;
+  double *visc = nullptr, *dens = nullptr;  // [nvnod]
+  double *G64 = nullptr;              // [120][nel]: G[p][3n+c]
+  double *M64 = nullptr;              // [10][nel] packed lower 4x4
+  double *Fbe = nullptr;              // [30][nel]
+  double *Fb = nullptr;               // [ndof] assembled, rotated
+  double *LiMM = nullptr;             // [nvnod] inverse lumped M
+  int *err = nullptr;                 // device error flags
+};
+
+struct Coarse {
+  int n = 0;                          // dofs of the coarsest level
+  double *A64 = nullptr;              // dense inverse (n x n)
+  float *A32 = nullptr;
+};
+
+struct SetupArgs {
+  int nel, nnod;
+  const int *el2nod;        // [10][nel] stored order
+  const uint8_t *cls;
+  const int *iso_slot;
+  const double *cubic;      // [60][niso]
+  int niso;
+  const double *gcoord, *gcoord_sph, *RR;
+  const double *visc, *dens;
+  const uint8_t *freemask;
+  double g, Bscale, Dens0, minVisc, maxVisc;
+  double *K64; float *K32; double *G64; double *M64; double *Fbe;
+  int *err;
+};
+
+}  // namespace m3sph
+
+struct m3sph_mesh {
+  int device = 0;
+  int nmg = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<m3sph::Level> lev;
+  m3sph::Finest fin;
+  m3sph::Coarse coarse;
+  int precision = 0;                  // 0 fp64, 1 fp32 V-cycle
+  bool have_operator = false;
+  std::vector<int> h_ifix;            // 0-based fixed dofs (rotated frame)
+  std::vector<double> h_vfix;
+  double *Ufix = nullptr;             // [ndof0] prescribed values (rotated frame)
+  double *bc_rhs = nullptr;           // K1_full * Ufix
+  // scratch
+  std::vector<void *> work;           // device buffers owned by the workspace
+  void *wk = nullptr;                 // host-side workspace descriptor
+  void (*wk_free)(void *) = nullptr;
+  double *red = nullptr;              // reduction partials
+  double *scal = nullptr;             // device scalars
+  double *h_scal = nullptr;           // pinned host mirror
+};

@@ -1,0 +1,1251 @@
+// Host orchestration and C ABI of the Stokes hot path: device-resident MESH and multigrid
+// hierarchy, operator set-up, V-cycle, flexible MG-PCG and the Patera pressure CG.
+//
+// Reference behaviour restated (paths inside the reference project):
+//   mfiles_M3TET/flow3d_patera_mg_sph_p.m:70-129 (constants), :225-298 (rotation, BCs),
+//       :374-384,709-727 (pressure preconditioner), :386-632 (Patera loop), :767-778 (rm0space)
+//   mfiles_M3TET/mgpcg_solver_p.m:70-199 (flexible PCG), :388-596 (MG_V_cycle_v2),
+//       :676-687 (Jacobi weights), :728-743 (mat_x_vec)
+//   mfiles_M3TET/restrict_stiffmat.m:79-142, intermesh_transfer_matrix.m:1-62
+//   mfiles_SPH/make_rotation_matrix.m:69-112, mfiles_M3TET/ip_tetrahedron.m:100-123
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace m3sph {
+
+// ---- declarations of kernels in the other translation units ----
+
+int launch_element_setup(const SetupArgs &a, cudaStream_t s);
+template <typename T> int ebe_apply(const Level &L, const T *K, const T *x, T *y, cudaStream_t s);
+int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
+template <typename T> int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s);
+int grad_apply(const Level &L, const double *G, const double *q, double *y, cudaStream_t s);
+int div_apply(const Level &L, const double *G, const double *z, double *out, cudaStream_t s);
+int mass_apply(const Level &L, const double *M, const double *d, double *out, cudaStream_t s);
+template <typename T> int galerkin(const Level &F, const T *Kf, Level &C, T *Kc, cudaStream_t s);
+int dot(const double *a, const double *b, size_t n, double *partials, double *out, cudaStream_t s);
+int dot2(const double *a, const double *c, const double *b, size_t n, double *partials, double *out, cudaStream_t s);
+int vsum(const double *a, size_t n, double *partials, double *out, cudaStream_t s);
+int cg_dir(const double *d, double *q, size_t n, const double *scal, int first, cudaStream_t s);
+int cg_update(double *x, double *r, const double *q, const double *Kq, size_t n, double *scal, double *partials,
+              cudaStream_t s);
+int axpby(double a, const double *x, double b, double *y, size_t n, cudaStream_t s);
+int sub_mask(const double *b, double *y, const uint8_t *mask, size_t n, cudaStream_t s);
+int apply_mask(double *y, const uint8_t *mask, size_t n, cudaStream_t s);
+int d2f(const double *a, float *b, size_t n, cudaStream_t s);
+int f2d(const float *a, double *b, size_t n, cudaStream_t s);
+template <typename T> int jac_first(T w, const T *r0, const T *Di, T *d, size_t n, cudaStream_t s);
+template <typename T> int jac(T w, const T *r0, const T *Kd, const T *Di, T *d, size_t n, cudaStream_t s);
+template <typename T> int restrict_(const Level &F, const Level &C, const T *a, const T *b, T *out, cudaStream_t s);
+template <typename T> int prolong(const Level &F, const Level &C, const T *xc, const T *add, T *out, cudaStream_t s);
+template <typename T> int dense_inverse(const Level &L, const T *K, T *A, T *work, cudaStream_t s);
+template <typename T> int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s);
+size_t element_setup_smem();
+
+// ---- errors ----
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+int cuda_fail(cudaError_t e, const char *what) {
+  g_err = std::string("CUDA error ") + cudaGetErrorString(e) + " in " + what;
+  return M3SPH_ERR_CUDA;
+}
+#define M3_TRY(call)                 \
+  do {                               \
+    int _s = (call);                 \
+    if (_s != M3SPH_OK) return _s;   \
+  } while (0)
+
+// ---- quadrature and shape functions (host) ----
+void build_shape_tables(ShapeTables &t) {
+  // 14-point Gellert-Harbord rule, ip_tetrahedron.m:100-123; weights / 6 (:193)
+  const double g = 1.0 / (46.0 * std::sqrt(46.0));
+  const double h = std::acos(g) + (2.0 / 3.0) * std::asin(g);
+  const double k = (104.0 + 8.0 * std::sqrt(46.0) * std::cos(h)) / 3.0;
+  const double s = std::sqrt(49.0 - k);
+  const double b = (7.0 + s) / k, a = 1.0 - 3.0 * b;
+  const double d = (7.0 - s) / k, c = 1.0 - 3.0 * d;
+  const double p = (98.0 - k - 14.0 * s) / (1680.0 * s * std::pow(b - a, 3));
+  const double q = (98.0 - k + 14.0 * s) / (1680.0 * s * std::pow(c - d, 3));
+  const double r = (1.0 - 4.0 * (p + q)) / 6.0;
+  const double e = (1.0 + std::pow(2.0 / (105.0 * r), 0.25)) / 4.0;
+  const double f = (1.0 - 2.0 * e) / 2.0;
+  const double X[3][NIP] = {{a, b, b, b, c, d, d, d, e, e, e, f, f, f},
+                            {b, a, b, b, d, c, d, d, e, f, f, e, e, f},
+                            {b, b, a, b, d, d, c, d, f, e, f, e, f, e}};
+  const double W[NIP] = {p, p, p, p, q, q, q, q, r, r, r, r, r, r};
+  for (int ip = 0; ip < NIP; ++ip) {
+    const double R = X[0][ip], S = X[1][ip], T = X[2][ip], U = 1.0 - R - S - T;
+    t.ipw[ip] = W[ip] / 6.0;
+    const double L[4] = {R, S, T, U};
+    const double gL[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, -1, -1}};
+    for (int v = 0; v < 4; ++v) t.NP[ip][v] = L[v];
+    // P2 (sf_dsf_tet10): vertices L(2L-1), edges 4 La Lb on edges 1-2,2-3,3-4,4-1,1-3,2-4
+    const int E10[6][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {0, 2}, {1, 3}};
+    for (int v = 0; v < 4; ++v) {
+      t.NU[ip][v] = L[v] * (2 * L[v] - 1);
+      for (int j = 0; j < 3; ++j) t.dNU[ip][v][j] = (4 * L[v] - 1) * gL[v][j];
+    }
+    for (int m = 0; m < 6; ++m) {
+      const int ia = E10[m][0], ib = E10[m][1];
+      t.NU[ip][4 + m] = 4 * L[ia] * L[ib];
+      for (int j = 0; j < 3; ++j) t.dNU[ip][4 + m][j] = 4 * (L[ib] * gL[ia][j] + L[ia] * gL[ib][j]);
+    }
+    // cubic 20-node tetrahedron (sf_dsf_tet20 node order)
+    for (int v = 0; v < 4; ++v) {
+      t.N20[ip][v] = 0.5 * L[v] * (3 * L[v] - 1) * (3 * L[v] - 2);
+      for (int j = 0; j < 3; ++j) t.dN20[ip][v][j] = 0.5 * (27 * L[v] * L[v] - 18 * L[v] + 2) * gL[v][j];
+    }
+    const int EP[12][2] = {{0, 1}, {1, 0}, {1, 2}, {2, 1}, {2, 3}, {3, 2}, {3, 0}, {0, 3}, {0, 2}, {2, 0}, {3, 1}, {1, 3}};
+    for (int m = 0; m < 12; ++m) {
+      const int ia = EP[m][0], ib = EP[m][1];
+      t.N20[ip][4 + m] = 4.5 * L[ia] * L[ib] * (3 * L[ia] - 1);
+      for (int j = 0; j < 3; ++j)
+        t.dN20[ip][4 + m][j] = 4.5 * (L[ib] * (6 * L[ia] - 1) * gL[ia][j] + L[ia] * (3 * L[ia] - 1) * gL[ib][j]);
+    }
+    const int FC[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+    for (int m = 0; m < 4; ++m) {
+      const int i0 = FC[m][0], i1 = FC[m][1], i2 = FC[m][2];
+      t.N20[ip][16 + m] = 27 * L[i0] * L[i1] * L[i2];
+      for (int j = 0; j < 3; ++j)
+        t.dN20[ip][16 + m][j] =
+            27 * (L[i1] * L[i2] * gL[i0][j] + L[i0] * L[i2] * gL[i1][j] + L[i0] * L[i1] * gL[i2][j]);
+    }
+  }
+}
+
+// ---- device allocation helpers ----
+template <typename T>
+static int dalloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  M3_CUDA(cudaMalloc((void **)p, sizeof(T) * n));
+  return M3SPH_OK;
+}
+template <typename T>
+static int upload(T **p, const T *h, size_t n, cudaStream_t s) {
+  M3_TRY(dalloc(p, n));
+  M3_CUDA(cudaMemcpyAsync(*p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+  return M3SPH_OK;
+}
+static void dfree(void *p) {
+  if (p) cudaFree(p);
+}
+
+// ---- greedy element colouring: elements sharing a vertex get different colours ----
+static int color_elements(const std::vector<int> &el, int nel, int nvert_ids, std::vector<int> &color, int &ncolor) {
+  std::vector<uint64_t> used(2 * (size_t)nvert_ids, 0);
+  color.assign(nel, -1);
+  ncolor = 0;
+  for (int e = 0; e < nel; ++e) {
+    uint64_t m0 = 0, m1 = 0;
+    for (int v = 0; v < 4; ++v) {
+      const int n = el[(size_t)e * 10 + v];
+      m0 |= used[2 * (size_t)n];
+      m1 |= used[2 * (size_t)n + 1];
+    }
+    int c = -1;
+    if (~m0) c = __builtin_ctzll(~m0);
+    else if (~m1) c = 64 + __builtin_ctzll(~m1);
+    if (c < 0) {
+      set_error("element colouring needs more than 128 colours");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    color[e] = c;
+    ncolor = std::max(ncolor, c + 1);
+    for (int v = 0; v < 4; ++v) {
+      const int n = el[(size_t)e * 10 + v];
+      used[2 * (size_t)n + (c >> 6)] |= 1ull << (c & 63);
+    }
+  }
+  return M3SPH_OK;
+}
+
+static const double P2LC[10][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0},   {.5, .5, 0},
+                                   {0, .5, .5}, {0, 0, .5}, {.5, 0, 0}, {.5, 0, .5}, {0, .5, 0}};
+static const int EDG[6][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {0, 2}, {3, 1}};
+
+static void sf10h(const double *lc, double *N) {
+  const double r = lc[0], s = lc[1], t = lc[2], u = 1 - r - s - t;
+  N[0] = r * (2 * r - 1); N[1] = s * (2 * s - 1); N[2] = t * (2 * t - 1); N[3] = u * (2 * u - 1);
+  N[4] = 4 * r * s; N[5] = 4 * s * t; N[6] = 4 * t * u; N[7] = 4 * r * u; N[8] = 4 * r * t; N[9] = 4 * s * u;
+}
+
+}  // namespace m3sph
+
+using namespace m3sph;
+
+// ======================================================================================
+// C ABI
+// ======================================================================================
+extern "C" const char *m3sph_last_error(void) { return g_err.c_str(); }
+
+extern "C" int m3sph_device_count(int *count) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    *count = 0;
+    return cuda_fail(e, "cudaGetDeviceCount");
+  }
+  *count = n;
+  return M3SPH_OK;
+}
+
+static int build_level(m3sph_mesh *M, int img, const m3sph_level &in, Level &L) {
+  cudaStream_t s = M->stream;
+  L.nel = in.nel;
+  L.nnod = in.nnod;
+  L.nvnod = in.nvnod;
+  L.ndof = 3 * in.nnod;
+  if (in.nel <= 0 || in.nnod <= 0 || !in.EL2NOD) {
+    set_error("level " + std::to_string(img) + ": empty or missing EL2NOD");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  L.h_el2nod_orig.resize((size_t)in.nel * 10);
+  for (size_t i = 0; i < (size_t)in.nel * 10; ++i) {
+    const uint32_t v = in.EL2NOD[i];
+    if (v < 1 || v > (uint32_t)in.nnod) {
+      set_error("level " + std::to_string(img) + ": EL2NOD entry out of range");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    L.h_el2nod_orig[i] = (int)v - 1;
+  }
+  std::vector<int> color;
+  int ncolor = 0;
+  M3_TRY(color_elements(L.h_el2nod_orig, in.nel, in.nnod, color, ncolor));
+  std::vector<int> cnt(ncolor + 1, 0);
+  for (int e = 0; e < in.nel; ++e) cnt[color[e] + 1]++;
+  for (int c = 0; c < ncolor; ++c) cnt[c + 1] += cnt[c];
+  L.cstart = cnt;
+  std::vector<int> perm(in.nel), invperm(in.nel), fill(cnt.begin(), cnt.end() - 1);
+  for (int e = 0; e < in.nel; ++e) {
+    const int pos = fill[color[e]]++;
+    perm[pos] = e;
+    invperm[e] = pos;
+  }
+  std::vector<int> el_soa((size_t)in.nel * 10);
+  for (int p = 0; p < in.nel; ++p)
+    for (int n = 0; n < 10; ++n) el_soa[(size_t)n * in.nel + p] = L.h_el2nod_orig[(size_t)perm[p] * 10 + n];
+  M3_TRY(upload(&L.el2nod, el_soa.data(), el_soa.size(), s));
+  M3_TRY(upload(&L.perm, perm.data(), perm.size(), s));
+  M3_TRY(upload(&L.invperm, invperm.data(), invperm.size(), s));
+  M3_TRY(dalloc(&L.freemask, L.ndof));
+  M3_CUDA(cudaMemsetAsync(L.freemask, 1, L.ndof, s));
+  M3_TRY(dalloc(&L.Dinv64, L.ndof));
+  M3_TRY(dalloc(&L.Dinv32, L.ndof));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+// children of coarse level C (level img+1) in fine level F (level img), and the transfer rows
+static int build_transfer(m3sph_mesh *M, Level &F, Level &C, const uint8_t *isplit_c) {
+  cudaStream_t s = M->stream;
+  (void)isplit_c;
+  if ((size_t)F.nel != 8 * (size_t)C.nel) {
+    set_error("fine level must have 8 children per coarse element");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  std::vector<int> hperm_c(C.nel), hinv_f(F.nel);
+  M3_CUDA(cudaMemcpy(hperm_c.data(), C.perm, sizeof(int) * C.nel, cudaMemcpyDeviceToHost));
+  M3_CUDA(cudaMemcpy(hinv_f.data(), F.invperm, sizeof(int) * F.nel, cudaMemcpyDeviceToHost));
+  std::vector<int> child((size_t)8 * C.nel);
+  std::vector<uint32_t> vloc((size_t)8 * C.nel);
+  // parent-local index of each child vertex
+  std::vector<uint32_t> vloc_orig((size_t)F.nel);
+  for (int p = 0; p < C.nel; ++p) {
+    const int *pn = &C.h_el2nod_orig[(size_t)p * 10];
+    for (int k = 0; k < 8; ++k) {
+      const int fe = 8 * p + k;
+      uint32_t code = 0;
+      for (int v = 0; v < 4; ++v) {
+        const int node = F.h_el2nod_orig[(size_t)fe * 10 + v];
+        int loc = -1;
+        for (int j = 0; j < 10; ++j)
+          if (pn[j] == node) loc = j;
+        if (loc < 0) {
+          set_error("child vertex is not a node of its parent");
+          return M3SPH_ERR_BAD_INPUT;
+        }
+        code |= (uint32_t)loc << (4 * v);
+      }
+      vloc_orig[fe] = code;
+    }
+  }
+  for (int pc = 0; pc < C.nel; ++pc) {
+    const int p = hperm_c[pc];
+    for (int k = 0; k < 8; ++k) {
+      child[(size_t)k * C.nel + pc] = hinv_f[8 * p + k];
+      vloc[(size_t)k * C.nel + pc] = vloc_orig[8 * p + k];
+    }
+  }
+  M3_TRY(upload(&C.child, child.data(), child.size(), s));
+  M3_TRY(upload(&C.child_vloc, vloc.data(), vloc.size(), s));
+  // transfer rows: parent of the first element listing the node (intermesh_transfer_matrix.m:19-23)
+  std::vector<int> first(F.nnod, -1);
+  for (size_t i = 0; i < (size_t)F.nel * 10; ++i) {
+    const int n = F.h_el2nod_orig[i];
+    if (first[n] < 0) first[n] = (int)i;
+  }
+  std::vector<int> ptr(F.nnod + 1, 0), col;
+  std::vector<float> w;
+  col.reserve((size_t)F.nnod * 4);
+  w.reserve((size_t)F.nnod * 4);
+  for (int n = 0; n < F.nnod; ++n) {
+    if (first[n] < 0) {
+      set_error("fine node not referenced by any element");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    const int fe = first[n] / 10, ln = first[n] % 10, p = fe / 8;
+    const uint32_t code = vloc_orig[fe];
+    double lc[3];
+    if (ln < 4) {
+      const int pl = (code >> (4 * ln)) & 15;
+      for (int d = 0; d < 3; ++d) lc[d] = P2LC[pl][d];
+    } else {
+      const int a0 = (code >> (4 * EDG[ln - 4][0])) & 15, a1 = (code >> (4 * EDG[ln - 4][1])) & 15;
+      for (int d = 0; d < 3; ++d) lc[d] = 0.5 * (P2LC[a0][d] + P2LC[a1][d]);
+    }
+    double N[10];
+    sf10h(lc, N);
+    for (int j = 0; j < 10; ++j)
+      if (std::fabs(N[j]) > 1e-14) {
+        col.push_back(C.h_el2nod_orig[(size_t)p * 10 + j]);
+        w.push_back((float)N[j]);
+      }
+    ptr[n + 1] = (int)col.size();
+  }
+  // transpose (coarse rows)
+  std::vector<int> rptr(C.nnod + 1, 0), rcol(col.size());
+  std::vector<float> rw(col.size());
+  for (int c : col) rptr[c + 1]++;
+  for (int i = 0; i < C.nnod; ++i) rptr[i + 1] += rptr[i];
+  std::vector<int> fill(rptr.begin(), rptr.end() - 1);
+  for (int n = 0; n < F.nnod; ++n)
+    for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
+      const int pos = fill[col[k]]++;
+      rcol[pos] = n;
+      rw[pos] = w[k];
+    }
+  M3_TRY(upload(&F.P_ptr, ptr.data(), ptr.size(), s));
+  M3_TRY(upload(&F.P_col, col.data(), col.size(), s));
+  M3_TRY(upload(&F.P_w, w.data(), w.size(), s));
+  M3_TRY(upload(&F.R_ptr, rptr.data(), rptr.size(), s));
+  M3_TRY(upload(&F.R_col, rcol.data(), rcol.size(), s));
+  M3_TRY(upload(&F.R_w, rw.data(), rw.size(), s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+static void free_level(Level &L) {
+  for (void *p : {(void *)L.el2nod, (void *)L.perm, (void *)L.invperm, (void *)L.freemask, (void *)L.K64,
+                  (void *)L.K32, (void *)L.Dinv64, (void *)L.Dinv32, (void *)L.child, (void *)L.child_vloc,
+                  (void *)L.P_ptr, (void *)L.P_col, (void *)L.P_w, (void *)L.R_ptr, (void *)L.R_col, (void *)L.R_w})
+    dfree(p);
+  L = Level();
+}
+
+extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
+  if (!M) return M3SPH_OK;
+  cudaSetDevice(M->device);
+  if (M->stream) cudaStreamSynchronize(M->stream);
+  for (auto &L : M->lev) free_level(L);
+  Finest &f = M->fin;
+  for (void *p : {(void *)f.gcoord, (void *)f.gcoord_sph, (void *)f.RR, (void *)f.cls, (void *)f.iso_slot,
+                  (void *)f.cubic, (void *)f.visc, (void *)f.dens, (void *)f.G64, (void *)f.M64, (void *)f.Fbe,
+                  (void *)f.Fb, (void *)f.LiMM, (void *)f.err})
+    dfree(p);
+  dfree(M->coarse.A64);
+  dfree(M->coarse.A32);
+  dfree(M->Ufix);
+  dfree(M->bc_rhs);
+  dfree(M->red);
+  dfree(M->scal);
+  for (void *p : M->work) dfree(p);
+  if (M->h_scal) cudaFreeHost(M->h_scal);
+  if (M->wk && M->wk_free) M->wk_free(M->wk);
+  if (M->stream) cudaStreamDestroy(M->stream);
+  delete M;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t device, m3sph_mesh **out) {
+  if (!out || !levels || nmg < 1) {
+    set_error("m3sph_mesh_create: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    set_error("no CUDA device available: the m3sph library has no CPU path");
+    return M3SPH_ERR_NO_DEVICE;
+  }
+  M3_CUDA(cudaSetDevice(device));
+  m3sph_mesh *M = new m3sph_mesh();
+  M->device = device;
+  M->nmg = nmg;
+  int st = M3SPH_OK;
+  auto fail = [&](int code) {
+    m3sph_mesh_destroy(M);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(M3SPH_ERR_CUDA);
+  st = upload_shape_tables();
+  if (st) return fail(st);
+  M->lev.resize(nmg);
+  for (int i = 0; i < nmg; ++i) {
+    st = build_level(M, i, levels[i], M->lev[i]);
+    if (st) return fail(st);
+    if (i > 0 && levels[i].nnod > levels[i - 1].nnod) {
+      set_error("coarse level has more nodes than the finer level");
+      return fail(M3SPH_ERR_BAD_INPUT);
+    }
+  }
+  for (int i = 0; i + 1 < nmg; ++i) {
+    st = build_transfer(M, M->lev[i], M->lev[i + 1], levels[i + 1].isplit);
+    if (st) return fail(st);
+  }
+  // finest-level geometry
+  const m3sph_level &f0 = levels[0];
+  Level &L0 = M->lev[0];
+  if (!f0.GCOORD || !f0.GCOORD_SPH || !f0.elclass) {
+    set_error("level 0 needs GCOORD, GCOORD_SPH and elclass");
+    return fail(M3SPH_ERR_BAD_INPUT);
+  }
+  Finest &F = M->fin;
+  cudaStream_t s = M->stream;
+  const int nnod = f0.nnod, nel = f0.nel;
+  std::vector<double> gc(3 * (size_t)nnod), gs(3 * (size_t)nnod), RR(9 * (size_t)nnod);
+  for (int n = 0; n < nnod; ++n)
+    for (int k = 0; k < 3; ++k) {
+      gc[(size_t)k * nnod + n] = f0.GCOORD[3 * (size_t)n + k];
+      gs[(size_t)k * nnod + n] = f0.GCOORD_SPH[3 * (size_t)n + k];
+    }
+  for (int n = 0; n < nnod; ++n) {   // make_rotation_matrix.m:69-112 from cartesian2spherical(GCOORD)
+    const double x = f0.GCOORD[3 * (size_t)n], y = f0.GCOORD[3 * (size_t)n + 1], z = f0.GCOORD[3 * (size_t)n + 2];
+    const double th = std::atan2(std::sqrt(x * x + y * y), z);
+    double ph = std::atan2(y, x);
+    if (ph < 0) ph += 2 * M_PI;
+    const double st_ = std::sin(th), ct = std::cos(th), sp = std::sin(ph), cp = std::cos(ph);
+    const double Rm[9] = {cp * ct, -sp, cp * st_, sp * ct, cp, sp * st_, -st_, 0.0, ct};
+    for (int q = 0; q < 9; ++q) RR[(size_t)q * nnod + n] = Rm[q];
+  }
+  std::vector<int> hperm(nel);
+  M3_CUDA(cudaMemcpy(hperm.data(), L0.perm, sizeof(int) * nel, cudaMemcpyDeviceToHost));
+  std::vector<uint8_t> cls(nel);
+  std::vector<int> iso_slot(nel, -1), iso_of_orig(nel, -1);
+  for (int i = 0; i < f0.niso; ++i) {
+    const uint32_t e = f0.els_iso[i];
+    if (e < 1 || e > (uint32_t)nel) {
+      set_error("els_iso entry out of range");
+      return fail(M3SPH_ERR_BAD_INPUT);
+    }
+    iso_of_orig[e - 1] = i;
+  }
+  for (int p = 0; p < nel; ++p) {
+    const int e = hperm[p];
+    cls[p] = f0.elclass[e];
+    if (cls[p] > 3) {
+      set_error("element class out of range");
+      return fail(M3SPH_ERR_BAD_INPUT);
+    }
+    if (cls[p] == M3SPH_IN_CONE_ISO) {
+      if (iso_of_orig[e] < 0) {
+        set_error("in-cone isoparametric element without cubic geometry");
+        return fail(M3SPH_ERR_BAD_INPUT);
+      }
+      iso_slot[p] = iso_of_orig[e];
+    }
+  }
+  F.niso = f0.niso;
+  std::vector<double> cub(60 * (size_t)std::max(1, f0.niso), 0.0);
+  for (int i = 0; i < f0.niso; ++i)
+    for (int q = 0; q < 60; ++q) cub[(size_t)q * f0.niso + i] = f0.cubic_sph_rot[(size_t)i * 60 + q];
+  if ((st = upload(&F.gcoord, gc.data(), gc.size(), s)) || (st = upload(&F.gcoord_sph, gs.data(), gs.size(), s)) ||
+      (st = upload(&F.RR, RR.data(), RR.size(), s)) || (st = upload(&F.cls, cls.data(), cls.size(), s)) ||
+      (st = upload(&F.iso_slot, iso_slot.data(), iso_slot.size(), s)) ||
+      (st = upload(&F.cubic, cub.data(), cub.size(), s)) || (st = dalloc(&F.visc, nnod)) ||
+      (st = dalloc(&F.dens, nnod)) || (st = dalloc(&F.G64, 120 * (size_t)nel)) ||
+      (st = dalloc(&F.M64, 10 * (size_t)nel)) || (st = dalloc(&F.Fbe, 30 * (size_t)nel)) ||
+      (st = dalloc(&F.Fb, L0.ndof)) || (st = dalloc(&F.LiMM, L0.nvnod)) || (st = dalloc(&F.err, 4)) ||
+      (st = dalloc(&L0.K64, (size_t)NPACK * nel)) || (st = dalloc(&L0.K32, (size_t)NPACK * nel)) ||
+      (st = dalloc(&M->Ufix, L0.ndof)) || (st = dalloc(&M->bc_rhs, L0.ndof)) || (st = dalloc(&M->red, 4096)) ||
+      (st = dalloc(&M->scal, 64)))
+    return fail(st);
+  if (cudaMallocHost((void **)&M->h_scal, 64 * sizeof(double)) != cudaSuccess) return fail(M3SPH_ERR_CUDA);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "mesh upload"));
+  *out = M;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_mesh_ncolors(const m3sph_mesh *M, int32_t img, int32_t *nc) {
+  if (!M || img < 0 || img >= M->nmg || !nc) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  *nc = (int)M->lev[img].cstart.size() - 1;
+  return M3SPH_OK;
+}
+
+// ---- work vectors ----
+namespace {
+struct Work {
+  // per level T vectors for the V-cycle
+  std::vector<double *> r64, d64, kd64;
+  std::vector<float *> r32, d32, kd32;
+  double *cwork64 = nullptr;
+  float *cwork32 = nullptr;
+  // outer vectors (level 0, fp64)
+  double *r = nullptr, *d = nullptr, *q = nullptr, *Kq = nullptr, *tmp = nullptr;
+  double *U = nullptr, *z = nullptr, *y = nullptr, *Rhs = nullptr;
+  double *pr = nullptr, *pd = nullptr, *pq = nullptr, *pSq = nullptr, *pt = nullptr, *pP = nullptr, *prl = nullptr;
+};
+}  // namespace
+
+static std::mutex g_work_mu;
+
+static Work *get_work(m3sph_mesh *M) { return reinterpret_cast<Work *>(M->wk); }
+
+static int alloc_work(m3sph_mesh *M) {
+  if (M->wk) return M3SPH_OK;
+  Work *W = new Work();
+  M->wk = W;
+  M->wk_free = [](void *p) { delete reinterpret_cast<Work *>(p); };
+  const int nmg = M->nmg;
+  W->r64.resize(nmg); W->d64.resize(nmg); W->kd64.resize(nmg);
+  W->r32.resize(nmg); W->d32.resize(nmg); W->kd32.resize(nmg);
+  for (int i = 0; i < nmg; ++i) {
+    const size_t n = M->lev[i].ndof;
+    M3_TRY(dalloc(&W->r64[i], n)); M3_TRY(dalloc(&W->d64[i], n)); M3_TRY(dalloc(&W->kd64[i], n));
+    M3_TRY(dalloc(&W->r32[i], n)); M3_TRY(dalloc(&W->d32[i], n)); M3_TRY(dalloc(&W->kd32[i], n));
+  }
+  const size_t nc = M->lev[nmg - 1].ndof;
+  M3_TRY(dalloc(&W->cwork64, 2 * nc));
+  M3_TRY(dalloc(&W->cwork32, 2 * nc));
+  const size_t n0 = M->lev[0].ndof, np = M->lev[0].nvnod;
+  M3_TRY(dalloc(&W->r, n0)); M3_TRY(dalloc(&W->d, n0)); M3_TRY(dalloc(&W->q, n0));
+  M3_TRY(dalloc(&W->Kq, n0)); M3_TRY(dalloc(&W->tmp, n0));
+  M3_TRY(dalloc(&W->U, n0)); M3_TRY(dalloc(&W->z, n0)); M3_TRY(dalloc(&W->y, n0)); M3_TRY(dalloc(&W->Rhs, n0));
+  M3_TRY(dalloc(&W->pr, np)); M3_TRY(dalloc(&W->pd, np)); M3_TRY(dalloc(&W->pq, np));
+  M3_TRY(dalloc(&W->pSq, np)); M3_TRY(dalloc(&W->pt, np)); M3_TRY(dalloc(&W->pP, np)); M3_TRY(dalloc(&W->prl, np));
+  // register device buffers for freeing
+  auto reg = [&](void *p) { M->work.push_back(p); };
+  for (int i = 0; i < nmg; ++i) {
+    reg(W->r64[i]); reg(W->d64[i]); reg(W->kd64[i]); reg(W->r32[i]); reg(W->d32[i]); reg(W->kd32[i]);
+  }
+  for (void *p : {(void *)W->cwork64, (void *)W->cwork32, (void *)W->r, (void *)W->d, (void *)W->q, (void *)W->Kq,
+                  (void *)W->tmp, (void *)W->U, (void *)W->z, (void *)W->y, (void *)W->Rhs, (void *)W->pr,
+                  (void *)W->pd, (void *)W->pq, (void *)W->pSq, (void *)W->pt, (void *)W->pP, (void *)W->prl})
+    reg(p);
+  return M3SPH_OK;
+}
+
+// ======================================================================================
+// operator set-up
+// ======================================================================================
+__global__ void k_set_masks(uint8_t *mask, const int *ifix, int nfix, int ndof) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nfix && ifix[i] >= 0 && ifix[i] < ndof) mask[ifix[i]] = 0;
+}
+__global__ void k_scatter_vals(double *v, const int *ifix, const double *vals, int nfix) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nfix) v[ifix[i]] = vals[i];
+}
+__global__ void k_recip(const double *a, double *b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = 1.0 / a[i];
+}
+
+// bc_rhs = K_full Ufix where K_full is the rotated (unmasked) operator: only columns of fixed
+// dofs matter, so apply the element operator with masks lifted on a vector that is zero on free
+// dofs. The stored K has fixed rows/cols zeroed, hence a dedicated pass on unmasked matrices.
+static int compute_bc_rhs(m3sph_mesh *M, const SetupArgs &base, Work *W) {
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  // temporary unmasked element matrices
+  double *Ku = nullptr;
+  float *Ku32 = nullptr;
+  double *Gt = nullptr, *Mt = nullptr, *Ft = nullptr;
+  uint8_t *ones = nullptr;
+  M3_TRY(dalloc(&Ku, (size_t)NPACK * L0.nel));
+  M3_TRY(dalloc(&Ku32, (size_t)NPACK * L0.nel));
+  M3_TRY(dalloc(&Gt, 120 * (size_t)L0.nel));
+  M3_TRY(dalloc(&Mt, 10 * (size_t)L0.nel));
+  M3_TRY(dalloc(&Ft, 30 * (size_t)L0.nel));
+  M3_TRY(dalloc(&ones, L0.ndof));
+  M3_CUDA(cudaMemsetAsync(ones, 1, L0.ndof, s));
+  SetupArgs a = base;
+  a.freemask = ones;
+  a.K64 = Ku; a.K32 = Ku32; a.G64 = Gt; a.M64 = Mt; a.Fbe = Ft;
+  M3_TRY(launch_element_setup(a, s));
+  M3_TRY(ebe_apply<double>(L0, Ku, M->Ufix, M->bc_rhs, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  for (void *p : {(void *)Ku, (void *)Ku32, (void *)Gt, (void *)Mt, (void *)Ft, (void *)ones}) dfree(p);
+  (void)W;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const double *Dens, const int32_t *ifix,
+                                  const double *vfix, int32_t nfix, const m3sph_physics *phys, int32_t precision) {
+  if (!M || !Visc || !Dens || (nfix > 0 && (!ifix || !vfix)) || !phys) {
+    set_error("m3sph_stokes_setup: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  cudaStream_t s = M->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  Level &L0 = M->lev[0];
+  M->precision = precision ? 1 : 0;
+  M3_TRY(alloc_work(M));
+  Work *W = get_work(M);
+  // masks
+  std::vector<int> fx(nfix);
+  for (int i = 0; i < nfix; ++i) {
+    if (ifix[i] < 1 || ifix[i] > L0.ndof) {
+      set_error("ifix entry out of range");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    fx[i] = ifix[i] - 1;
+  }
+  M->h_ifix = fx;
+  M->h_vfix.assign(vfix, vfix + nfix);
+  int *d_fix = nullptr;
+  double *d_vals = nullptr;
+  M3_TRY(upload(&d_fix, fx.data(), std::max<size_t>(1, fx.size()), s));
+  M3_TRY(upload(&d_vals, M->h_vfix.data(), std::max<size_t>(1, fx.size()), s));
+  for (int i = 0; i < M->nmg; ++i) {
+    Level &L = M->lev[i];
+    M3_CUDA(cudaMemsetAsync(L.freemask, 1, L.ndof, s));
+    if (nfix) k_set_masks<<<(nfix + 255) / 256, 256, 0, s>>>(L.freemask, d_fix, nfix, L.ndof);
+  }
+  M3_CUDA(cudaMemsetAsync(M->Ufix, 0, sizeof(double) * L0.ndof, s));
+  if (nfix) k_scatter_vals<<<(nfix + 255) / 256, 256, 0, s>>>(M->Ufix, d_fix, d_vals, nfix);
+  M3_CUDA(cudaMemcpyAsync(M->fin.visc, Visc, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(M->fin.dens, Dens, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemsetAsync(M->fin.err, 0, sizeof(int) * 4, s));
+  int nfree = 0;
+  {
+    std::vector<uint8_t> fm(L0.ndof, 1);
+    for (int i : fx) fm[i] = 0;
+    for (int i = 0; i < M->nmg; ++i) {
+      int c = 0;
+      for (int d = 0; d < M->lev[i].ndof; ++d) c += fm[d];
+      M->lev[i].nfree = c;
+    }
+    nfree = M->lev[0].nfree;
+  }
+  (void)nfree;
+  SetupArgs a{};
+  a.nel = L0.nel; a.nnod = L0.nnod; a.el2nod = L0.el2nod; a.cls = M->fin.cls; a.iso_slot = M->fin.iso_slot;
+  a.cubic = M->fin.cubic; a.niso = M->fin.niso; a.gcoord = M->fin.gcoord; a.gcoord_sph = M->fin.gcoord_sph;
+  a.RR = M->fin.RR; a.visc = M->fin.visc; a.dens = M->fin.dens; a.freemask = L0.freemask;
+  a.g = phys->g; a.Bscale = phys->Bscale; a.Dens0 = phys->Dens0; a.minVisc = phys->minVisc; a.maxVisc = phys->maxVisc;
+  a.K64 = L0.K64; a.K32 = L0.K32; a.G64 = M->fin.G64; a.M64 = M->fin.M64; a.Fbe = M->fin.Fbe; a.err = M->fin.err;
+  M3_TRY(launch_element_setup(a, s));
+  int herr[4];
+  M3_CUDA(cudaMemcpyAsync(herr, M->fin.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  if (herr[0] & 1) {
+    set_error("negative Jacobi");
+    return M3SPH_ERR_NEGATIVE_JACOBIAN;
+  }
+  if (herr[0] & 2) {
+    set_error("integration point with theta = 0 (det(J_CS) = Inf)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (herr[0] & 4) {
+    set_error(" Calculated a zero or negative viscosity. STOPPING.");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  // assembled force vector, lumped pressure mass, boundary-condition rhs
+  M3_TRY(scatter_elvec(L0, M->fin.Fbe, 30, 3, M->fin.Fb, L0.ndof, s));
+  M3_TRY(mass_apply(L0, M->fin.M64, nullptr, W->pt, s));
+  k_recip<<<(L0.nvnod + 255) / 256, 256, 0, s>>>(W->pt, M->fin.LiMM, L0.nvnod);
+  if (nfix) {
+    M3_TRY(compute_bc_rhs(M, a, W));
+  } else {
+    M3_CUDA(cudaMemsetAsync(M->bc_rhs, 0, sizeof(double) * L0.ndof, s));
+  }
+  // level diagonals and Galerkin coarse operators
+  M3_TRY(level_inverse_diag<double>(L0, L0.K64, W->tmp, s));
+  for (int i = 1; i < M->nmg; ++i) {
+    Level &F = M->lev[i - 1], &C = M->lev[i];
+    if (M->precision == 0) {
+      if (!C.K64) M3_TRY(dalloc(&C.K64, (size_t)NPACK * C.nel));
+      M3_TRY(galerkin<double>(F, F.K64, C, C.K64, s));
+      M3_TRY(level_inverse_diag<double>(C, C.K64, W->tmp, s));
+    } else {
+      if (!C.K32) M3_TRY(dalloc(&C.K32, (size_t)NPACK * C.nel));
+      M3_TRY(galerkin<float>(F, F.K32, C, C.K32, s));
+      M3_TRY(level_inverse_diag<float>(C, C.K32, W->tmp, s));
+    }
+  }
+  // coarsest dense inverse (stands in for cholesky_factorization)
+  Level &Lc = M->lev[M->nmg - 1];
+  const int nc = Lc.ndof;
+  if (nc > 12000) {
+    set_error("coarsest level too large for the dense coarse solve; add a multigrid level");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M->coarse.n = nc;
+  if (M->nmg > 1) {
+    if (M->precision == 0) {
+      if (!M->coarse.A64) M3_TRY(dalloc(&M->coarse.A64, (size_t)nc * nc));
+      M3_TRY(dense_inverse<double>(Lc, Lc.K64, M->coarse.A64, W->cwork64, s));
+    } else {
+      if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
+      M3_TRY(dense_inverse<float>(Lc, Lc.K32, M->coarse.A32, W->cwork32, s));
+    }
+  }
+  M3_CUDA(cudaStreamSynchronize(s));
+  dfree(d_fix);
+  dfree(d_vals);
+  M->have_operator = true;
+  (void)t0;
+  return M3SPH_OK;
+}
+
+// ======================================================================================
+// V-cycle (MG_V_cycle_v2) in precision T; level-0 residual r0 given in T, d0 out in T
+// ======================================================================================
+static const double WD0[3] = {0.9, 0.4, 0.25}, WU0[3] = {0.25, 0.4, 0.9};
+static const double WDc[3] = {0.25, 0.4, 0.9}, WUc[3] = {0.9, 0.4, 0.25};
+
+template <typename T> static const T *levK(const Level &L);
+template <> const double *levK<double>(const Level &L) { return L.K64; }
+template <> const float *levK<float>(const Level &L) { return L.K32; }
+template <typename T> static const T *levDi(const Level &L);
+template <> const double *levDi<double>(const Level &L) { return L.Dinv64; }
+template <> const float *levDi<float>(const Level &L) { return L.Dinv32; }
+
+template <typename T>
+static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std::vector<T *> &kd, const T *Ainv) {
+  cudaStream_t s = M->stream;
+  const int nm = M->nmg;
+  if (nm == 1) {
+    M3_TRY(dense_gemv<T>(Ainv, M->coarse.n, r[0], M->lev[0].freemask, d[0], s));
+    return M3SPH_OK;
+  }
+  for (int j = 0; j < nm - 1; ++j) {
+    const Level &L = M->lev[j];
+    const double *w = j == 0 ? WD0 : WDc;
+    const size_t n = L.ndof;
+    M3_TRY(jac_first<T>((T)w[0], r[j], levDi<T>(L), d[j], n, s));
+    M3_TRY(ebe_apply<T>(L, levK<T>(L), d[j], kd[j], s));
+    for (int k = 1; k < 3; ++k) {
+      M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
+      M3_TRY(ebe_apply<T>(L, levK<T>(L), d[j], kd[j], s));
+    }
+    M3_TRY(restrict_<T>(L, M->lev[j + 1], r[j], kd[j], r[j + 1], s));
+  }
+  M3_TRY(dense_gemv<T>(Ainv, M->coarse.n, r[nm - 1], M->lev[nm - 1].freemask, d[nm - 1], s));
+  for (int j = nm - 2; j >= 0; --j) {
+    const Level &L = M->lev[j];
+    const double *w = j == 0 ? WU0 : WUc;
+    const size_t n = L.ndof;
+    M3_TRY(prolong<T>(L, M->lev[j + 1], d[j + 1], d[j], d[j], s));
+    for (int k = 0; k < 3; ++k) {
+      M3_TRY(ebe_apply<T>(L, levK<T>(L), d[j], kd[j], s));
+      M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
+    }
+  }
+  return M3SPH_OK;
+}
+
+// d (fp64) = B r (fp64) in the set-up precision
+static int vcycle(m3sph_mesh *M, const double *r, double *dout) {
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  const size_t n0 = M->lev[0].ndof;
+  if (M->precision == 0) {
+    std::vector<double *> rr = W->r64, dd = W->d64;
+    rr[0] = const_cast<double *>(r);
+    dd[0] = dout;
+    return vcycle_T<double>(M, rr, dd, W->kd64, M->coarse.A64);
+  }
+  M3_TRY(d2f(r, W->r32[0], n0, s));
+  M3_TRY(vcycle_T<float>(M, W->r32, W->d32, W->kd32, M->coarse.A32));
+  M3_TRY(f2d(W->d32[0], dout, n0, s));
+  return M3SPH_OK;
+}
+
+// ======================================================================================
+// flexible MG-PCG (mgpcg_solver_p.m:117-199), FP64 outer iteration
+// ======================================================================================
+struct CGStats {
+  int it = 0;
+  double rrms = 0.0;
+  int nvc = 0;
+};
+
+static int read_scal(m3sph_mesh *M, int idx, double &v) {
+  M3_CUDA(cudaMemcpyAsync(M->h_scal + idx, M->scal + idx, sizeof(double), cudaMemcpyDeviceToHost, M->stream));
+  M3_CUDA(cudaStreamSynchronize(M->stream));
+  v = M->h_scal[idx];
+  return M3SPH_OK;
+}
+
+// b masked to free dofs on entry; x holds the initial guess (fixed entries are left unchanged)
+static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs_tol, int itmax, CGStats &st) {
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  const size_t n = L0.ndof;
+  const double sq = std::sqrt((double)std::max(1, L0.nfree));
+  M3_TRY(ebe_apply<double>(L0, L0.K64, x, W->r, s));
+  M3_TRY(sub_mask(b, W->r, L0.freemask, n, s));
+  M3_TRY(dot(W->r, W->r, n, M->red, M->scal + 3, s));
+  double rr;
+  M3_TRY(read_scal(M, 3, rr));
+  if (std::isnan(rr)) {
+    set_error("RHS vector contains NaNs");
+    return M3SPH_ERR_NAN;
+  }
+  double rrms = std::sqrt(rr) / sq;
+  if (!abs_tol) tol = tol * rrms;
+  st.it = 0;
+  int it = 0;
+  for (it = 1; it <= itmax; ++it) {
+    M3_TRY(vcycle(M, W->r, W->d));
+    st.nvc++;
+    M3_TRY(dot2(W->r, W->Kq, W->d, n, M->red, M->scal + 0, s));   // scal[0]=r.d, scal[1]=Kq_prev.d
+    M3_TRY(cg_dir(W->d, W->q, n, M->scal, it == 1, s));
+    M3_TRY(ebe_apply<double>(L0, L0.K64, W->q, W->Kq, s));
+    M3_TRY(dot(W->q, W->Kq, n, M->red, M->scal + 2, s));
+    M3_TRY(cg_update(x, W->r, W->q, W->Kq, n, M->scal, M->red, s));
+    M3_TRY(read_scal(M, 3, rr));
+    rrms = std::sqrt(rr) / sq;
+    if (std::isnan(rrms)) {
+      set_error("NaN in MG-PCG residual");
+      return M3SPH_ERR_NAN;
+    }
+    if (rrms < tol) break;
+  }
+  st.it = std::min(it, itmax);
+  st.rrms = rrms;
+  return M3SPH_OK;
+}
+
+// ======================================================================================
+// Patera pressure CG (flow3d_patera_mg_sph_p.m:386-632)
+// ======================================================================================
+static int pdot(m3sph_mesh *M, const double *a, const double *b, double &v) {
+  M3_TRY(dot(a, b, M->lev[0].nvnod, M->red, M->scal + 8, M->stream));
+  return read_scal(M, 8, v);
+}
+__global__ void k_shift(double *a, double c, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] += c;
+}
+__global__ void k_precond_p1(const double *r, const double *LiMM, double *d, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = r[i] * LiMM[i];
+}
+__global__ void k_precond_p2(const double *r, const double *Md, const double *LiMM, double *d, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] += LiMM[i] * (r[i] - Md[i]);
+}
+__global__ void k_rhs(const double *Fb, const double *GP, const double *bc, const uint8_t *mask, double *out, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = mask[i] ? Fb[i] + GP[i] - bc[i] : 0.0;
+}
+__global__ void k_scale(double *a, double c, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) a[i] *= c;
+}
+__global__ void k_rotate_back(const double *U, const double *RR, int nnod, double *Uxyz) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnod) return;
+  for (int r = 0; r < 3; ++r) {
+    double v = 0.0;
+    for (int c = 0; c < 3; ++c) v += RR[(size_t)(r * 3 + c) * nnod + n] * U[3 * n + c];
+    Uxyz[3 * n + r] = v;
+  }
+}
+
+static int remove_mean(m3sph_mesh *M, double *a) {
+  const int np = M->lev[0].nvnod;
+  M3_TRY(vsum(a, np, M->red, M->scal + 9, M->stream));
+  double sm;
+  M3_TRY(read_scal(M, 9, sm));
+  k_shift<<<(np + 255) / 256, 256, 0, M->stream>>>(a, -sm / np, np);
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+static int build_rhs(m3sph_mesh *M, const double *P, double *Rhs) {
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  M3_TRY(grad_apply(L0, M->fin.G64, P, W->y, M->stream));
+  k_rhs<<<(unsigned)((L0.ndof + 255) / 256), 256, 0, M->stream>>>(M->fin.Fb, W->y, M->bc_rhs, L0.freemask, Rhs,
+                                                                  L0.ndof);
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+// coupled FP64 relative residual
+static int coupled_residual(m3sph_mesh *M, const double *U, const double *P, double &rel) {
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  const size_t n = L0.ndof;
+  const int np = L0.nvnod;
+  // f = mask(Fb - bc_rhs)
+  M3_CUDA(cudaMemsetAsync(W->tmp, 0, sizeof(double) * n, s));
+  k_rhs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M->fin.Fb, W->tmp, M->bc_rhs, L0.freemask, W->Rhs, n);
+  double ff;
+  M3_TRY(dot(W->Rhs, W->Rhs, n, M->red, M->scal + 10, s));
+  M3_TRY(read_scal(M, 10, ff));
+  // ru = mask(Fb + G P - bc - K U)
+  M3_TRY(build_rhs(M, P, W->Rhs));
+  M3_TRY(ebe_apply<double>(L0, L0.K64, U, W->tmp, s));
+  M3_TRY(sub_mask(W->Rhs, W->tmp, L0.freemask, n, s));
+  double ru;
+  M3_TRY(dot(W->tmp, W->tmp, n, M->red, M->scal + 10, s));
+  M3_TRY(read_scal(M, 10, ru));
+  // rp = -G' U, mean removed
+  M3_TRY(div_apply(L0, M->fin.G64, U, W->pt, s));
+  M3_TRY(remove_mean(M, W->pt));
+  double rp;
+  M3_TRY(dot(W->pt, W->pt, np, M->red, M->scal + 10, s));
+  M3_TRY(read_scal(M, 10, rp));
+  rel = std::sqrt(ru + rp) / std::sqrt(std::max(ff, 1e-300));
+  return M3SPH_OK;
+}
+
+static int precondition_P(m3sph_mesh *M, const double *r, double *d) {
+  Work *W = get_work(M);
+  const int np = M->lev[0].nvnod;
+  k_precond_p1<<<(np + 255) / 256, 256, 0, M->stream>>>(r, M->fin.LiMM, d, np);
+  M3_TRY(mass_apply(M->lev[0], M->fin.M64, d, W->pSq, M->stream));   // pSq used as temp (Md)
+  k_precond_p2<<<(np + 255) / 256, 256, 0, M->stream>>>(r, W->pSq, M->fin.LiMM, d, np);
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const m3sph_opts *opts,
+                                  m3sph_info *info) {
+  if (!M || !U_xyz || !P || !opts) {
+    set_error("m3sph_stokes_solve: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (!M->have_operator) {
+    set_error("m3sph_stokes_solve: call m3sph_stokes_setup first");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  const size_t n = L0.ndof;
+  const int np = L0.nvnod;
+  m3sph_info inf{};
+  auto t0 = std::chrono::steady_clock::now();
+  double rtol_Pat = opts->rtol_Pat > 0 ? opts->rtol_Pat : 1e-4;
+  double rtol_U = opts->rtol_U > 0 ? opts->rtol_U : 5e-3;
+  const int itmax_Pat = opts->itmax_Pat > 0 ? opts->itmax_Pat : 120;
+  const int itmin_Pat = opts->itmin_Pat > 0 ? opts->itmin_Pat : 3;
+  const int itmax_U = opts->itmax_U > 0 ? opts->itmax_U : 20;
+  const double rtol_restart = 0.8 * rtol_Pat;
+  const double sqp = std::sqrt((double)np);
+  double *U = W->U, *Pd = W->pP, *r = W->pr, *d = W->pd, *q = W->pq, *Sq = W->pSq, *z = W->z, *y = W->y;
+  M3_CUDA(cudaMemcpyAsync(Pd, P, sizeof(double) * np, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(U, M->Ufix, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  CGStats cs;
+  // initial velocity
+  M3_TRY(build_rhs(M, Pd, W->Rhs));
+  M3_TRY(mgpcg(M, W->Rhs, U, rtol_U * rtol_restart, false, itmax_U, cs));
+  inf.nitU += cs.it;
+  // initial pressure residual r = -G'U
+  M3_TRY(div_apply(L0, M->fin.G64, U, r, s));
+  k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np);
+  M3_TRY(remove_mean(M, r));
+  double rr;
+  M3_TRY(pdot(M, r, r, rr));
+  double norm_rP = std::sqrt(rr) / sqp;
+  double tol_Pat = rtol_Pat * norm_rP;
+  M3_TRY(mgpcg(M, W->Rhs, U, rtol_U * rtol_restart * norm_rP, true, itmax_U, cs));
+  inf.nitU += cs.it;
+  double tol_U_restart = rtol_U * tol_Pat;
+  bool restart = true, conv_problem = false;
+  double norm_rP0 = norm_rP, rd = 0.0, rdlast = 0.0, tol_Z = 0.0;
+  int itPat = 0;
+  const double target = opts->target_rel_residual;
+  for (itPat = 1; itPat <= itmax_Pat; ++itPat) {
+    M3_TRY(precondition_P(M, r, d));
+    if (restart) {
+      M3_CUDA(cudaMemcpyAsync(q, d, sizeof(double) * np, cudaMemcpyDeviceToDevice, s));
+      restart = false;
+      norm_rP0 = norm_rP;
+      tol_Z = rtol_U * std::max(rtol_restart * norm_rP0, tol_Pat);
+    } else {
+      // beta = (r - rlast).d / rdlast
+      double rd_new, rld;
+      M3_TRY(pdot(M, r, d, rd_new));
+      M3_TRY(pdot(M, W->prl, d, rld));
+      const double beta = (rd_new - rld) / rdlast;
+      M3_TRY(axpby(1.0, d, beta, q, np, s));
+    }
+    M3_TRY(remove_mean(M, q));
+    M3_TRY(pdot(M, r, d, rd));
+    rdlast = rd;
+    M3_TRY(grad_apply(L0, M->fin.G64, q, y, s));
+    M3_TRY(apply_mask(y, L0.freemask, n, s));
+    M3_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * n, s));
+    M3_TRY(mgpcg(M, y, z, tol_Z, true, itmax_U, cs));
+    inf.nitZ += cs.it;
+    M3_TRY(div_apply(L0, M->fin.G64, z, Sq, s));
+    double qSq;
+    M3_TRY(pdot(M, q, Sq, qSq));
+    M3_CUDA(cudaMemcpyAsync(W->prl, r, sizeof(double) * np, cudaMemcpyDeviceToDevice, s));
+    const double alpha = rd / qSq;
+    M3_TRY(axpby(alpha, q, 1.0, Pd, np, s));
+    M3_TRY(axpby(alpha, z, 1.0, U, n, s));
+    M3_TRY(axpby(-alpha, Sq, 1.0, r, np, s));
+    M3_TRY(remove_mean(M, r));
+    const double norm_rP_last = norm_rP;
+    M3_TRY(pdot(M, r, r, rr));
+    norm_rP = std::sqrt(rr) / sqp;
+    if (std::isnan(norm_rP)) {
+      set_error("Solution containes NaNs !!!!");
+      return M3SPH_ERR_NAN;
+    }
+    const double norm_rP_min = std::min(norm_rP_last, norm_rP);
+    bool done = norm_rP < tol_Pat && itPat >= itmin_Pat;
+    if (done && target > 0) {
+      double rel;
+      M3_TRY(coupled_residual(M, U, Pd, rel));
+      if (rel > target) {
+        // the coupled residual is not yet at the target: tighten both tolerances and go on
+        tol_Pat *= 0.1;
+        rtol_U *= 0.1;
+        tol_U_restart = rtol_U * tol_Pat;
+        done = false;
+        restart = true;
+      }
+    }
+    if (done) break;
+    if (norm_rP < rtol_restart * norm_rP0 || norm_rP > 10 * norm_rP0) {
+      M3_TRY(build_rhs(M, Pd, W->Rhs));
+      M3_TRY(mgpcg(M, W->Rhs, U, tol_U_restart, true, itmax_U, cs));
+      inf.nitU += cs.it;
+      M3_TRY(div_apply(L0, M->fin.G64, U, r, s));
+      k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np);
+      double rt;
+      M3_TRY(pdot(M, r, r, rt));
+      const double norm_rP_true = std::sqrt(rt) / sqp;
+      if (norm_rP_true > 1.1 * norm_rP) {
+        rtol_U = rtol_U * 0.75 * (norm_rP / norm_rP_true);
+        tol_U_restart = rtol_U * tol_Pat;
+      }
+      if (norm_rP > 10 * norm_rP0 || norm_rP > 1.2 * norm_rP_min) {
+        if (conv_problem) break;
+        rtol_U = 0.1 * rtol_U;
+        tol_U_restart = rtol_U * tol_Pat;
+        conv_problem = true;
+      }
+      restart = true;
+    }
+  }
+  M3_TRY(build_rhs(M, Pd, W->Rhs));
+  M3_TRY(mgpcg(M, W->Rhs, U, tol_U_restart, true, itmax_U, cs));
+  inf.nitU += cs.it;
+  inf.itPat = std::min(itPat, itmax_Pat);
+  inf.norm_rP = norm_rP;
+  inf.nvcycle = cs.nvc;
+  double rel = 0.0;
+  M3_TRY(coupled_residual(M, U, Pd, rel));
+  inf.rel_residual = rel;
+  // back-rotation U_xyz = RR U
+  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(U, M->fin.RR, L0.nnod, W->tmp);
+  M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaMemcpyAsync(P, Pd, sizeof(double) * np, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  auto t1 = std::chrono::steady_clock::now();
+  inf.t_iter_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  inf.status = M3SPH_OK;
+  if (info) *info = inf;
+  return M3SPH_OK;
+}
+
+// ======================================================================================
+// operator-level entry points (tests, benchmarks)
+// ======================================================================================
+static int need_op(m3sph_mesh *M) {
+  if (!M || !M->have_operator) {
+    set_error("operator not set up (call m3sph_stokes_setup)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_stokes_apply(m3sph_mesh *M, const double *x, double *y) {
+  M3_TRY(need_op(M));
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(W->tmp, x, sizeof(double) * L0.ndof, cudaMemcpyHostToDevice, s));
+  M3_TRY(ebe_apply<double>(L0, L0.K64, W->tmp, W->y, s));
+  M3_CUDA(cudaMemcpyAsync(y, W->y, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_grad_apply(m3sph_mesh *M, const double *q, double *y) {
+  M3_TRY(need_op(M));
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(W->pt, q, sizeof(double) * L0.nvnod, cudaMemcpyHostToDevice, s));
+  M3_TRY(grad_apply(L0, M->fin.G64, W->pt, W->y, s));
+  M3_CUDA(cudaMemcpyAsync(y, W->y, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_div_apply(m3sph_mesh *M, const double *z, double *out) {
+  M3_TRY(need_op(M));
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(W->tmp, z, sizeof(double) * L0.ndof, cudaMemcpyHostToDevice, s));
+  M3_TRY(div_apply(L0, M->fin.G64, W->tmp, W->pt, s));
+  M3_CUDA(cudaMemcpyAsync(out, W->pt, sizeof(double) * L0.nvnod, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_force_vector(m3sph_mesh *M, double *Fb) {
+  M3_TRY(need_op(M));
+  M3_CUDA(cudaMemcpyAsync(Fb, M->fin.Fb, sizeof(double) * M->lev[0].ndof, cudaMemcpyDeviceToHost, M->stream));
+  M3_CUDA(cudaStreamSynchronize(M->stream));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_element_matrices(m3sph_mesh *M, double *K, double *G, double *Mm) {
+  M3_TRY(need_op(M));
+  Level &L0 = M->lev[0];
+  const int nel = L0.nel;
+  std::vector<double> hk((size_t)NPACK * nel), hg(120 * (size_t)nel), hm(10 * (size_t)nel);
+  std::vector<int> perm(nel);
+  M3_CUDA(cudaMemcpy(hk.data(), L0.K64, sizeof(double) * hk.size(), cudaMemcpyDeviceToHost));
+  M3_CUDA(cudaMemcpy(hg.data(), M->fin.G64, sizeof(double) * hg.size(), cudaMemcpyDeviceToHost));
+  M3_CUDA(cudaMemcpy(hm.data(), M->fin.M64, sizeof(double) * hm.size(), cudaMemcpyDeviceToHost));
+  M3_CUDA(cudaMemcpy(perm.data(), L0.perm, sizeof(int) * nel, cudaMemcpyDeviceToHost));
+  for (int p = 0; p < nel; ++p) {
+    const int e = perm[p];
+    if (K)
+      for (int c = 0; c < 30; ++c)
+        for (int r = c; r < 30; ++r) {
+          const double v = hk[(size_t)pack_idx(r, c) * nel + p];
+          K[(size_t)e * 900 + r * 30 + c] = v;
+          K[(size_t)e * 900 + c * 30 + r] = v;
+        }
+    if (G)
+      for (int pp = 0; pp < 4; ++pp)
+        for (int q = 0; q < 30; ++q) G[(size_t)e * 120 + q * 4 + pp] = hg[(size_t)(pp * 30 + q) * nel + p];
+    if (Mm) {
+      int k = 0;
+      for (int c = 0; c < 4; ++c)
+        for (int r = c; r < 4; ++r) {
+          const double v = hm[(size_t)k * nel + p];
+          ++k;
+          Mm[(size_t)e * 16 + r * 4 + c] = v;
+          Mm[(size_t)e * 16 + c * 4 + r] = v;
+        }
+    }
+  }
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_level_apply(m3sph_mesh *M, int32_t img, const double *x, double *y) {
+  M3_TRY(need_op(M));
+  if (img < 0 || img >= M->nmg) {
+    set_error("level out of range");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  Level &L = M->lev[img];
+  cudaStream_t s = M->stream;
+  const size_t n = L.ndof;
+  if (img == 0 || M->precision == 0) {
+    M3_CUDA(cudaMemcpyAsync(W->r64[img], x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    M3_TRY(ebe_apply<double>(L, L.K64, W->r64[img], W->kd64[img], s));
+    M3_CUDA(cudaMemcpyAsync(y, W->kd64[img], sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  } else {
+    M3_CUDA(cudaMemcpyAsync(W->r64[img], x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    M3_TRY(d2f(W->r64[img], W->r32[img], n, s));
+    M3_TRY(ebe_apply<float>(L, L.K32, W->r32[img], W->kd32[img], s));
+    M3_TRY(f2d(W->kd32[img], W->kd64[img], n, s));
+    M3_CUDA(cudaMemcpyAsync(y, W->kd64[img], sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  }
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_prolong(m3sph_mesh *M, int32_t img, const double *xc, double *xf) {
+  M3_TRY(need_op(M));
+  if (img < 0 || img + 1 >= M->nmg) {
+    set_error("level out of range");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  Level &F = M->lev[img], &C = M->lev[img + 1];
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(W->r64[img + 1], xc, sizeof(double) * C.ndof, cudaMemcpyHostToDevice, s));
+  M3_TRY(prolong<double>(F, C, W->r64[img + 1], nullptr, W->d64[img], s));
+  M3_CUDA(cudaMemcpyAsync(xf, W->d64[img], sizeof(double) * F.ndof, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_restrict(m3sph_mesh *M, int32_t img, const double *rf, double *rc) {
+  M3_TRY(need_op(M));
+  if (img < 0 || img + 1 >= M->nmg) {
+    set_error("level out of range");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  Level &F = M->lev[img], &C = M->lev[img + 1];
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(W->r64[img], rf, sizeof(double) * F.ndof, cudaMemcpyHostToDevice, s));
+  M3_TRY(restrict_<double>(F, C, W->r64[img], nullptr, W->d64[img + 1], s));
+  M3_CUDA(cudaMemcpyAsync(rc, W->d64[img + 1], sizeof(double) * C.ndof, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_vcycle(m3sph_mesh *M, const double *r, double *d) {
+  M3_TRY(need_op(M));
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  const size_t n = M->lev[0].ndof;
+  M3_CUDA(cudaMemcpyAsync(W->tmp, r, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_TRY(vcycle(M, W->tmp, W->d));
+  M3_CUDA(cudaMemcpyAsync(d, W->d, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, int32_t is_abs_tol, int32_t itmax,
+                           int32_t *itCG, double *rrms_final) {
+  M3_TRY(need_op(M));
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  const size_t n = L0.ndof;
+  M3_CUDA(cudaMemcpyAsync(W->Rhs, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_TRY(apply_mask(W->Rhs, L0.freemask, n, s));
+  M3_CUDA(cudaMemcpyAsync(W->U, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CGStats cs;
+  M3_TRY(mgpcg(M, W->Rhs, W->U, tol, is_abs_tol != 0, itmax, cs));
+  M3_CUDA(cudaMemcpyAsync(x, W->U, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  if (itCG) *itCG = cs.it;
+  if (rrms_final) *rrms_final = cs.rrms;
+  return M3SPH_OK;
+}

@@ -1,0 +1,186 @@
+"""Host-side mirror of the reference Stokes interface over the C ABI.
+
+``flow3d_patera_sph(VAR, MESH, COMM, UBC, SETTINGS, PHYSICS, NUMSCALE, dt)`` keeps the reference's
+signature (mfiles_M3TET/flow3d_patera_sph.m:1-8) and returns ``(VAR, Uinfo)``; the work is done
+by ``m3sph_stokes_setup`` + ``m3sph_stokes_solve`` in libm3sph.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib as L
+from . import mesh as meshmod
+
+
+class DeviceMesh:
+    """Device-resident MESH + multigrid hierarchy (owns an m3sph_mesh handle)."""
+
+    def __init__(self, levels, device=0):
+        self.levels = levels
+        self.nmg = len(levels)
+        self._keep = []
+        arr = (L.Level * self.nmg)()
+        for i, lv in enumerate(levels):
+            el = np.ascontiguousarray(lv['EL2NOD'].astype(np.uint32) + 1)       # 1-based, 10 x nel col-major
+            self._keep.append(el)
+            a = arr[i]
+            a.nel = len(el)
+            a.nnod = lv['GCOORD'].shape[1]
+            a.nvnod = int(lv['EL2NOD'][:, :4].max()) + 1
+            a.EL2NOD = L.u32ptr(el)
+            if 'isplit' in lv and i > 0:
+                isp = np.ascontiguousarray(lv['isplit'].astype(np.uint8) + 1)
+                self._keep.append(isp)
+                a.isplit = L.u8ptr(isp)
+            if i == 0:
+                gc = np.ascontiguousarray(lv['GCOORD'].T)                         # 3 x nnod col-major
+                gs = np.ascontiguousarray(lv['GCOORD_SPH'].T)
+                cl = np.ascontiguousarray(lv['cls'].astype(np.uint8))
+                iso = np.ascontiguousarray(lv['els_iso'].astype(np.uint32) + 1)
+                cub = np.ascontiguousarray(lv['cubic_sph_rot'].astype(np.float64))
+                self._keep += [gc, gs, cl, iso, cub]
+                a.GCOORD = L.dptr(gc)
+                a.GCOORD_SPH = L.dptr(gs)
+                a.elclass = L.u8ptr(cl)
+                a.niso = len(iso)
+                a.els_iso = L.u32ptr(iso) if len(iso) else None
+                a.cubic_sph_rot = L.dptr(cub) if len(iso) else None
+        self._arr = arr
+        h = C.c_void_p()
+        L.check(L.lib().m3sph_mesh_create(self.nmg, arr, device, C.byref(h)))
+        self.h = h
+        f = levels[0]
+        self.nnod = f['GCOORD'].shape[1]
+        self.ndof = 3 * self.nnod
+        self.nvnod = int(f['EL2NOD'][:, :4].max()) + 1
+        self.precision = None
+
+    def close(self):
+        if getattr(self, 'h', None):
+            L.lib().m3sph_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ncolors(self, img=0):
+        n = C.c_int32()
+        L.check(L.lib().m3sph_mesh_ncolors(self.h, img, C.byref(n)))
+        return n.value
+
+    # ---- operator set-up ----
+    def setup(self, visc, dens, ifix, vfix, phys=None, precision=0):
+        """ifix: 0-based dof ids in the rotated frame; vfix: prescribed values."""
+        phys = phys or {}
+        ph = L.Physics(g=phys.get('g', -9.81), Bscale=phys.get('Bscale', 1.0), Dens0=phys.get('Dens0', 0.0),
+                       minVisc=phys.get('minVisc', 0.0) or 0.0, maxVisc=phys.get('maxVisc', 0.0) or 0.0)
+        visc = np.ascontiguousarray(visc, dtype=np.float64)
+        dens = np.ascontiguousarray(dens, dtype=np.float64)
+        fx = np.ascontiguousarray(np.asarray(ifix, dtype=np.int32) + 1)
+        vf = np.ascontiguousarray(vfix, dtype=np.float64)
+        L.check(L.lib().m3sph_stokes_setup(self.h, L.dptr(visc), L.dptr(dens), L.iptr(fx), L.dptr(vf),
+                                           len(fx), C.byref(ph), int(precision)))
+        self.precision = precision
+
+    # ---- operators ----
+    def apply(self, x):
+        y = np.empty(self.ndof)
+        L.check(L.lib().m3sph_stokes_apply(self.h, L.dptr(np.ascontiguousarray(x, dtype=np.float64)), L.dptr(y)))
+        return y
+
+    def grad(self, q):
+        y = np.empty(self.ndof)
+        L.check(L.lib().m3sph_grad_apply(self.h, L.dptr(np.ascontiguousarray(q, dtype=np.float64)), L.dptr(y)))
+        return y
+
+    def div(self, z):
+        s = np.empty(self.nvnod)
+        L.check(L.lib().m3sph_div_apply(self.h, L.dptr(np.ascontiguousarray(z, dtype=np.float64)), L.dptr(s)))
+        return s
+
+    def force(self):
+        f = np.empty(self.ndof)
+        L.check(L.lib().m3sph_force_vector(self.h, L.dptr(f)))
+        return f
+
+    def element_matrices(self):
+        nel = len(self.levels[0]['EL2NOD'])
+        K = np.empty((nel, 30, 30))
+        G = np.empty((nel, 30, 4))
+        M = np.empty((nel, 4, 4))
+        L.check(L.lib().m3sph_element_matrices(self.h, L.dptr(K), L.dptr(G), L.dptr(M)))
+        return K, G, M
+
+    def level_apply(self, img, x):
+        n = 3 * self.levels[img]['GCOORD'].shape[1]
+        y = np.empty(n)
+        L.check(L.lib().m3sph_level_apply(self.h, img, L.dptr(np.ascontiguousarray(x, dtype=np.float64)), L.dptr(y)))
+        return y
+
+    def prolong(self, img, xc):
+        y = np.empty(3 * self.levels[img]['GCOORD'].shape[1])
+        L.check(L.lib().m3sph_prolong(self.h, img, L.dptr(np.ascontiguousarray(xc, dtype=np.float64)), L.dptr(y)))
+        return y
+
+    def restrict(self, img, rf):
+        y = np.empty(3 * self.levels[img + 1]['GCOORD'].shape[1])
+        L.check(L.lib().m3sph_restrict(self.h, img, L.dptr(np.ascontiguousarray(rf, dtype=np.float64)), L.dptr(y)))
+        return y
+
+    def vcycle(self, r):
+        d = np.empty(self.ndof)
+        L.check(L.lib().m3sph_vcycle(self.h, L.dptr(np.ascontiguousarray(r, dtype=np.float64)), L.dptr(d)))
+        return d
+
+    def mgpcg(self, b, x0, tol, is_abs_tol=True, itmax=20):
+        x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+        it = C.c_int32()
+        rr = C.c_double()
+        L.check(L.lib().m3sph_mgpcg(self.h, L.dptr(np.ascontiguousarray(b, dtype=np.float64)), L.dptr(x), tol,
+                                    int(is_abs_tol), itmax, C.byref(it), C.byref(rr)))
+        return x, it.value, rr.value
+
+    def solve(self, P0=None, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20,
+              target_rel_residual=0.0, smoother=0):
+        U = np.empty(self.ndof)
+        P = np.zeros(self.nvnod) if P0 is None else np.ascontiguousarray(P0, dtype=np.float64).copy()
+        o = L.Opts(rtol_Pat=rtol_Pat, rtol_U=rtol_U, itmax_Pat=itmax_Pat, itmin_Pat=itmin_Pat, itmax_U=itmax_U,
+                   precision=int(self.precision or 0), smoother=smoother, target_rel_residual=target_rel_residual)
+        info = L.Info()
+        L.check(L.lib().m3sph_stokes_solve(self.h, L.dptr(U), L.dptr(P), C.byref(o), C.byref(info)))
+        return U, P, info.as_dict()
+
+
+def flow3d_patera_sph(VAR, MESH, COMM, UBC, SETTINGS, PHYSICS, NUMSCALE, dt):
+    """Mirror of flow3d_patera_sph.m:1-8 -> flow3d_patera_mg_sph_p on the GPU.
+
+    VAR: dict with 'Visc', 'Dens' (nnod) and 'P' (nvnod); MESH: dict with 'levels' (finest first)
+    and optionally a cached 'device_mesh'; UBC: dict with 'ifix' (1-based rotated-frame dofs) and
+    'vfix'. Returns (VAR, Uinfo) with VAR['Ux','Uy','Uz','Uth','Uph','Ur','P'] filled.
+    """
+    dm = MESH.get('device_mesh')
+    if dm is None:
+        dm = DeviceMesh(MESH['levels'])
+        MESH['device_mesh'] = dm
+    prec = 1 if SETTINGS.get('mixed_precision', True) else 0
+    phys = dict(g=PHYSICS.get('g', -9.81), Bscale=NUMSCALE.get('Bscale', 1.0), Dens0=NUMSCALE.get('Dens0', 0.0),
+                minVisc=PHYSICS.get('minVisc'), maxVisc=PHYSICS.get('maxVisc'))
+    t0 = time.perf_counter()
+    dm.setup(VAR['Visc'], VAR['Dens'], np.asarray(UBC['ifix']) - 1, UBC['vfix'], phys, precision=prec)
+    t1 = time.perf_counter()
+    U, P, info = dm.solve(VAR.get('P'), rtol_Pat=SETTINGS.get('rtol_Pat', 1e-4), rtol_U=SETTINGS.get('rtol_U', 5e-3),
+                          target_rel_residual=SETTINGS.get('target_rel_residual', 0.0))
+    info['t_setup_ms'] = (t1 - t0) * 1e3
+    VAR = dict(VAR)
+    VAR['Ux'], VAR['Uy'], VAR['Uz'] = U[0::3].copy(), U[1::3].copy(), U[2::3].copy()
+    R = meshmod.rotation_blocks(MESH['levels'][0]['GCOORD'])
+    Ul = np.einsum('nji,nj->ni', R, U.reshape(-1, 3))
+    VAR['Uth'], VAR['Uph'], VAR['Ur'] = Ul[:, 0].copy(), Ul[:, 1].copy(), Ul[:, 2].copy()
+    VAR['P'] = P
+    return VAR, info

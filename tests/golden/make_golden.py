@@ -1,0 +1,39 @@
+"""Regenerate the golden fixtures from the reference project (needs the reference checkout).
+
+* earthshell_n37k.npz: the reference's shipped curved P2 mesh
+  (SETUP_TEST/MESHES/EarthShell_n37k.mat, produced by tetmesh_p1_to_p2_sph): vertex
+  coordinates, 10-node connectivity (0-based), all node coordinates and PointIDs.
+* quadrature_14.json: the numeric values of the 14-point rule documented in
+  mfiles_M3TET/ip_tetrahedron.m:109-117 (read from the comments as text).
+
+Usage: python tests/golden/make_golden.py /path/to/reference
+"""
+import json
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+import scipy.io as sio
+
+HERE = Path(__file__).resolve().parent
+
+
+def main(ref):
+    ref = Path(ref)
+    m = sio.loadmat(ref / 'SETUP_TEST/MESHES/EarthShell_n37k.mat', squeeze_me=True, struct_as_record=False)['MESH']
+    el = m.EL2NOD.astype(np.int64).T - 1
+    np.savez_compressed(HERE / 'earthshell_n37k.npz', EL2NOD=el.astype(np.int32), GCOORD=m.GCOORD.T.copy(),
+                        PointID=m.PointID.astype(np.int32), r_cmb=float(m.r_cmb), r_surf=float(m.r_surf))
+    txt = (ref / 'mfiles_M3TET/ip_tetrahedron.m').read_text(errors='replace').splitlines()
+    vals = {}
+    for ln in txt[108:118]:
+        mm = re.match(r'\s*([a-z])\s*=.*%\s*=\s*([0-9.]+)', ln)
+        if mm:
+            vals[mm.group(1)] = float(mm.group(2))
+    (HERE / 'quadrature_14.json').write_text(json.dumps(vals, indent=1, sort_keys=True) + '\n')
+    print(sorted(vals.items()))
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

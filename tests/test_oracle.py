@@ -1,0 +1,65 @@
+"""The oracle itself: documented quadrature constants, shape functions, operator identities."""
+import json
+from pathlib import Path
+
+import numpy as np
+
+from oracle import stokes_oracle as O
+
+GOLD = Path(__file__).resolve().parent / 'golden'
+
+
+def test_quadrature_matches_documented_values():
+    vals = json.loads((GOLD / 'quadrature_14.json').read_text())
+    ipx, ipw = O.ip_tetrahedron14()
+    a, b, c, d, e, f = ipx[0, 0], ipx[0, 1], ipx[0, 4], ipx[0, 5], ipx[0, 8], ipx[0, 11]
+    got = dict(a=a, b=b, c=c, d=d, e=e, f=f, p=ipw[0] * 6, q=ipw[4] * 6, r=ipw[8] * 6)
+    for k, v in vals.items():
+        assert abs(got[k] - v) < 5e-16 * 10, (k, got[k], v)
+    assert abs(ipw.sum() - 1.0 / 6.0) < 1e-15
+    # degree-5 exactness on a monomial: int r^2 s t over the unit tet = 2!1!1!/(2+1+1+3)! = 2/5040
+    r, s, t = ipx
+    assert abs((ipw * r ** 2 * s * t).sum() - 2.0 / 5040.0) < 1e-17
+
+
+def test_shape_function_derivatives_fd():
+    rng = np.random.default_rng(0)
+    for fn, n in ((O.sf10, 10), (O.sf20, 20)):
+        for _ in range(5):
+            x = rng.uniform(0.05, 0.3, 3)
+            N, dN = fn(*x)
+            assert abs(N.sum() - 1.0) < 1e-13
+            h = 1e-6
+            for j in range(3):
+                xp, xm = x.copy(), x.copy()
+                xp[j] += h
+                xm[j] -= h
+                fd = (fn(*xp)[0] - fn(*xm)[0]) / (2 * h)
+                assert np.abs(fd - dN[:, j]).max() < 1e-7
+
+
+def test_element_operator_identities(tiny):
+    f = tiny['levels'][0]
+    K, G, Mm, Fb = O.element_matrices(f, tiny['visc'], tiny['dens'], **tiny['phys'])
+    scale = np.abs(K).max()
+    assert np.abs(K - K.transpose(0, 2, 1)).max() <= 1e-14 * scale
+    for comp in range(3):
+        tr = np.zeros(30)
+        tr[comp::3] = 1.0
+        assert np.abs(K @ tr).max() < 1e-13 * scale
+        assert np.abs(np.einsum('eqp,q->ep', G, tr)).max() < 1e-13 * np.abs(G).max()
+    ev = np.linalg.eigvalsh(K[:200])
+    assert ev.min() > -1e-13 * ev.max()
+
+
+def test_transfer_matches_host_setup(tiny):
+    """Oracle intermesh_transfer_matrix (barycentric solve + rounding) equals the library's
+    combinatorial set-up rows built in m3tet_sph_gb300.mesh."""
+    lv = tiny['levels']
+    Xs_c = O.p2_straight(lv[1]['GCOORD'], lv[1]['EL2NOD'])
+    Xs_f = O.straight_coords(Xs_c, lv[0]['EL2NOD'])
+    Ic2f = O.intermesh_transfer_matrix(Xs_f, lv[0]['EL2NOD'], Xs_c, lv[1]['EL2NOD']).toarray()
+    cols, W = lv[0]['transfer_cols'], lv[0]['transfer_w']
+    dense = np.zeros_like(Ic2f)
+    np.add.at(dense, (np.repeat(np.arange(len(cols)), 10), cols.ravel()), W.ravel())
+    assert np.abs(dense - Ic2f).max() < 1e-12
