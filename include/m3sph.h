@@ -119,6 +119,16 @@ M3SPH_API int m3sph_stokes_setup(m3sph_mesh *mesh, const double *Visc, const dou
 M3SPH_API int m3sph_stokes_solve(m3sph_mesh *mesh, double *U_xyz, double *P, const m3sph_opts *opts,
                        m3sph_info *info);
 
+/* One device-resident hot-path step: rebuild the operator from the resident Visc/Dens/BCs of the
+ * last m3sph_stokes_setup (assembly + restrict_stiffmat + coarse factorisation) and run the
+ * Patera solve from P = 0; U and P stay on the device (read them with m3sph_solution). No
+ * counterpart call in the reference: flow3d_patera_mg_sph_p always starts from host arrays. */
+M3SPH_API int m3sph_stokes_step_device(m3sph_mesh *mesh, const m3sph_opts *opts, m3sph_info *info);
+/* Copy the device-resident solution of the last solve: U_xyz (3*nnod) and P (nvnod). */
+M3SPH_API int m3sph_solution(m3sph_mesh *mesh, double *U_xyz, double *P);
+/* The CUDA stream (cudaStream_t) the handle launches its kernels on. */
+M3SPH_API int m3sph_stream(m3sph_mesh *mesh, void **stream);
+
 /* Replaces one mgpcg_solver_p call (mgpcg_solver_p.m:1-743) on the current operator: solves
  * K1 x = b on the free dofs of the rotated frame (b, x: 3*nnod, fixed dofs ignored / zero).
  * tol is absolute on normdf(r) if is_abs_tol, else relative to the initial residual. */

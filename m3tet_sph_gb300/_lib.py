@@ -72,6 +72,9 @@ SIGNATURES = {
     "m3sph_prolong": ([P, C.c_int32, DP, DP], C.c_int),
     "m3sph_restrict": ([P, C.c_int32, DP, DP], C.c_int),
     "m3sph_vcycle": ([P, DP, DP], C.c_int),
+    "m3sph_stokes_step_device": ([P, C.POINTER(Opts), C.POINTER(Info)], C.c_int),
+    "m3sph_solution": ([P, DP, DP], C.c_int),
+    "m3sph_stream": ([P, C.POINTER(P)], C.c_int),
 }
 
 

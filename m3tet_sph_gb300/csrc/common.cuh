@@ -113,6 +113,8 @@ struct m3sph_mesh {
   m3sph::Finest fin;
   m3sph::Coarse coarse;
   int precision = 0;                  // 0 fp64, 1 fp32 V-cycle
+  m3sph_physics phys{};
+  double last_setup_ms = 0.0;
   bool have_operator = false;
   std::vector<int> h_ifix;            // 0-based fixed dofs (rotated frame)
   std::vector<double> h_vfix;

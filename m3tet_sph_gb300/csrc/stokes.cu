@@ -588,6 +588,79 @@ static int compute_bc_rhs(m3sph_mesh *M, const SetupArgs &base, Work *W) {
   return M3SPH_OK;
 }
 
+// element operator, force vector, Galerkin hierarchy and coarse inverse from the device-resident
+// viscosity, density and boundary conditions (assembly_stokes_sph_3d_double_jacobian +
+// restrict_stiffmat + cholesky_factorization of the reference)
+static int rebuild_operator(m3sph_mesh *M) {
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  Work *W = get_work(M);
+  M3_CUDA(cudaMemsetAsync(M->fin.err, 0, sizeof(int) * 4, s));
+  SetupArgs a{};
+  a.nel = L0.nel; a.nnod = L0.nnod; a.el2nod = L0.el2nod; a.cls = M->fin.cls; a.iso_slot = M->fin.iso_slot;
+  a.cubic = M->fin.cubic; a.niso = M->fin.niso; a.gcoord = M->fin.gcoord; a.gcoord_sph = M->fin.gcoord_sph;
+  a.RR = M->fin.RR; a.visc = M->fin.visc; a.dens = M->fin.dens; a.freemask = L0.freemask;
+  a.g = M->phys.g; a.Bscale = M->phys.Bscale; a.Dens0 = M->phys.Dens0; a.minVisc = M->phys.minVisc; a.maxVisc = M->phys.maxVisc;
+  a.K64 = L0.K64; a.K32 = L0.K32; a.G64 = M->fin.G64; a.M64 = M->fin.M64; a.Fbe = M->fin.Fbe; a.err = M->fin.err;
+  M3_TRY(launch_element_setup(a, s));
+  int herr[4];
+  M3_CUDA(cudaMemcpyAsync(herr, M->fin.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  if (herr[0] & 1) {
+    set_error("negative Jacobi");
+    return M3SPH_ERR_NEGATIVE_JACOBIAN;
+  }
+  if (herr[0] & 2) {
+    set_error("integration point with theta = 0 (det(J_CS) = Inf)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (herr[0] & 4) {
+    set_error(" Calculated a zero or negative viscosity. STOPPING.");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  // assembled force vector, lumped pressure mass, boundary-condition rhs
+  M3_TRY(scatter_elvec(L0, M->fin.Fbe, 30, 3, M->fin.Fb, L0.ndof, s));
+  M3_TRY(mass_apply(L0, M->fin.M64, nullptr, W->pt, s));
+  k_recip<<<(L0.nvnod + 255) / 256, 256, 0, s>>>(W->pt, M->fin.LiMM, L0.nvnod);
+  if (!M->h_ifix.empty()) {
+    M3_TRY(compute_bc_rhs(M, a, W));
+  } else {
+    M3_CUDA(cudaMemsetAsync(M->bc_rhs, 0, sizeof(double) * L0.ndof, s));
+  }
+  // level diagonals and Galerkin coarse operators
+  M3_TRY(level_inverse_diag<double>(L0, L0.K64, W->tmp, s));
+  for (int i = 1; i < M->nmg; ++i) {
+    Level &F = M->lev[i - 1], &C = M->lev[i];
+    if (M->precision == 0) {
+      if (!C.K64) M3_TRY(dalloc(&C.K64, (size_t)NPACK * C.nel));
+      M3_TRY(galerkin<double>(F, F.K64, C, C.K64, s));
+      M3_TRY(level_inverse_diag<double>(C, C.K64, W->tmp, s));
+    } else {
+      if (!C.K32) M3_TRY(dalloc(&C.K32, (size_t)NPACK * C.nel));
+      M3_TRY(galerkin<float>(F, F.K32, C, C.K32, s));
+      M3_TRY(level_inverse_diag<float>(C, C.K32, W->tmp, s));
+    }
+  }
+  // coarsest dense inverse (stands in for cholesky_factorization)
+  Level &Lc = M->lev[M->nmg - 1];
+  const int nc = Lc.ndof;
+  if (nc > 12000) {
+    set_error("coarsest level too large for the dense coarse solve; add a multigrid level");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M->coarse.n = nc;
+  if (M->nmg > 1) {
+    if (M->precision == 0) {
+      if (!M->coarse.A64) M3_TRY(dalloc(&M->coarse.A64, (size_t)nc * nc));
+      M3_TRY(dense_inverse<double>(Lc, Lc.K64, M->coarse.A64, W->cwork64, s));
+    } else {
+      if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
+      M3_TRY(dense_inverse<float>(Lc, Lc.K32, M->coarse.A32, W->cwork32, s));
+    }
+  }
+  return M3SPH_OK;
+}
+
 extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const double *Dens, const int32_t *ifix,
                                   const double *vfix, int32_t nfix, const m3sph_physics *phys, int32_t precision) {
   if (!M || !Visc || !Dens || (nfix > 0 && (!ifix || !vfix)) || !phys) {
@@ -625,7 +698,6 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   if (nfix) k_scatter_vals<<<(nfix + 255) / 256, 256, 0, s>>>(M->Ufix, d_fix, d_vals, nfix);
   M3_CUDA(cudaMemcpyAsync(M->fin.visc, Visc, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
   M3_CUDA(cudaMemcpyAsync(M->fin.dens, Dens, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
-  M3_CUDA(cudaMemsetAsync(M->fin.err, 0, sizeof(int) * 4, s));
   int nfree = 0;
   {
     std::vector<uint8_t> fm(L0.ndof, 1);
@@ -638,71 +710,22 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
     nfree = M->lev[0].nfree;
   }
   (void)nfree;
-  SetupArgs a{};
-  a.nel = L0.nel; a.nnod = L0.nnod; a.el2nod = L0.el2nod; a.cls = M->fin.cls; a.iso_slot = M->fin.iso_slot;
-  a.cubic = M->fin.cubic; a.niso = M->fin.niso; a.gcoord = M->fin.gcoord; a.gcoord_sph = M->fin.gcoord_sph;
-  a.RR = M->fin.RR; a.visc = M->fin.visc; a.dens = M->fin.dens; a.freemask = L0.freemask;
-  a.g = phys->g; a.Bscale = phys->Bscale; a.Dens0 = phys->Dens0; a.minVisc = phys->minVisc; a.maxVisc = phys->maxVisc;
-  a.K64 = L0.K64; a.K32 = L0.K32; a.G64 = M->fin.G64; a.M64 = M->fin.M64; a.Fbe = M->fin.Fbe; a.err = M->fin.err;
-  M3_TRY(launch_element_setup(a, s));
-  int herr[4];
-  M3_CUDA(cudaMemcpyAsync(herr, M->fin.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
-  M3_CUDA(cudaStreamSynchronize(s));
-  if (herr[0] & 1) {
-    set_error("negative Jacobi");
-    return M3SPH_ERR_NEGATIVE_JACOBIAN;
-  }
-  if (herr[0] & 2) {
-    set_error("integration point with theta = 0 (det(J_CS) = Inf)");
-    return M3SPH_ERR_BAD_INPUT;
-  }
-  if (herr[0] & 4) {
-    set_error(" Calculated a zero or negative viscosity. STOPPING.");
-    return M3SPH_ERR_BAD_INPUT;
-  }
-  // assembled force vector, lumped pressure mass, boundary-condition rhs
-  M3_TRY(scatter_elvec(L0, M->fin.Fbe, 30, 3, M->fin.Fb, L0.ndof, s));
-  M3_TRY(mass_apply(L0, M->fin.M64, nullptr, W->pt, s));
-  k_recip<<<(L0.nvnod + 255) / 256, 256, 0, s>>>(W->pt, M->fin.LiMM, L0.nvnod);
-  if (nfix) {
-    M3_TRY(compute_bc_rhs(M, a, W));
-  } else {
-    M3_CUDA(cudaMemsetAsync(M->bc_rhs, 0, sizeof(double) * L0.ndof, s));
-  }
-  // level diagonals and Galerkin coarse operators
-  M3_TRY(level_inverse_diag<double>(L0, L0.K64, W->tmp, s));
-  for (int i = 1; i < M->nmg; ++i) {
-    Level &F = M->lev[i - 1], &C = M->lev[i];
-    if (M->precision == 0) {
-      if (!C.K64) M3_TRY(dalloc(&C.K64, (size_t)NPACK * C.nel));
-      M3_TRY(galerkin<double>(F, F.K64, C, C.K64, s));
-      M3_TRY(level_inverse_diag<double>(C, C.K64, W->tmp, s));
-    } else {
-      if (!C.K32) M3_TRY(dalloc(&C.K32, (size_t)NPACK * C.nel));
-      M3_TRY(galerkin<float>(F, F.K32, C, C.K32, s));
-      M3_TRY(level_inverse_diag<float>(C, C.K32, W->tmp, s));
-    }
-  }
-  // coarsest dense inverse (stands in for cholesky_factorization)
-  Level &Lc = M->lev[M->nmg - 1];
-  const int nc = Lc.ndof;
-  if (nc > 12000) {
-    set_error("coarsest level too large for the dense coarse solve; add a multigrid level");
-    return M3SPH_ERR_BAD_INPUT;
-  }
-  M->coarse.n = nc;
-  if (M->nmg > 1) {
-    if (M->precision == 0) {
-      if (!M->coarse.A64) M3_TRY(dalloc(&M->coarse.A64, (size_t)nc * nc));
-      M3_TRY(dense_inverse<double>(Lc, Lc.K64, M->coarse.A64, W->cwork64, s));
-    } else {
-      if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
-      M3_TRY(dense_inverse<float>(Lc, Lc.K32, M->coarse.A32, W->cwork32, s));
-    }
-  }
+  M->phys = *phys;
   M3_CUDA(cudaStreamSynchronize(s));
   dfree(d_fix);
   dfree(d_vals);
+  cudaEvent_t e0, e1;
+  M3_CUDA(cudaEventCreate(&e0));
+  M3_CUDA(cudaEventCreate(&e1));
+  M3_CUDA(cudaEventRecord(e0, s));
+  M3_TRY(rebuild_operator(M));
+  M3_CUDA(cudaEventRecord(e1, s));
+  M3_CUDA(cudaEventSynchronize(e1));
+  float fms = 0.f;
+  M3_CUDA(cudaEventElapsedTime(&fms, e0, e1));
+  M->last_setup_ms = fms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   M->have_operator = true;
   (void)t0;
   return M3SPH_OK;
@@ -926,24 +949,14 @@ static int precondition_P(m3sph_mesh *M, const double *r, double *d) {
   return M3SPH_OK;
 }
 
-extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const m3sph_opts *opts,
-                                  m3sph_info *info) {
-  if (!M || !U_xyz || !P || !opts) {
-    set_error("m3sph_stokes_solve: bad arguments");
-    return M3SPH_ERR_BAD_INPUT;
-  }
-  if (!M->have_operator) {
-    set_error("m3sph_stokes_solve: call m3sph_stokes_setup first");
-    return M3SPH_ERR_BAD_INPUT;
-  }
-  M3_CUDA(cudaSetDevice(M->device));
+// Patera solve on device-resident data: the initial pressure must be in the workspace pressure
+// vector; U and P stay on the device (workspace U is the rotated-frame velocity).
+static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   Work *W = get_work(M);
   cudaStream_t s = M->stream;
   Level &L0 = M->lev[0];
   const size_t n = L0.ndof;
   const int np = L0.nvnod;
-  m3sph_info inf{};
-  auto t0 = std::chrono::steady_clock::now();
   double rtol_Pat = opts->rtol_Pat > 0 ? opts->rtol_Pat : 1e-4;
   double rtol_U = opts->rtol_U > 0 ? opts->rtol_U : 5e-3;
   const int itmax_Pat = opts->itmax_Pat > 0 ? opts->itmax_Pat : 120;
@@ -952,7 +965,6 @@ extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const
   const double rtol_restart = 0.8 * rtol_Pat;
   const double sqp = std::sqrt((double)np);
   double *U = W->U, *Pd = W->pP, *r = W->pr, *d = W->pd, *q = W->pq, *Sq = W->pSq, *z = W->z, *y = W->y;
-  M3_CUDA(cudaMemcpyAsync(Pd, P, sizeof(double) * np, cudaMemcpyHostToDevice, s));
   M3_CUDA(cudaMemcpyAsync(U, M->Ufix, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   CGStats cs;
   // initial velocity
@@ -1059,15 +1071,112 @@ extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const
   double rel = 0.0;
   M3_TRY(coupled_residual(M, U, Pd, rel));
   inf.rel_residual = rel;
+  return M3SPH_OK;
+}
+
+static int need_op_fwd(m3sph_mesh *M) {
+  if (!M || !M->have_operator) {
+    set_error("operator not set up (call m3sph_stokes_setup)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  return M3SPH_OK;
+}
+
+static int time_since(cudaEvent_t a, cudaEvent_t b, double &ms) {
+  float f = 0.f;
+  M3_CUDA(cudaEventElapsedTime(&f, a, b));
+  ms = f;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const m3sph_opts *opts,
+                                  m3sph_info *info) {
+  if (!M || !U_xyz || !P || !opts) {
+    set_error("m3sph_stokes_solve: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (!M->have_operator) {
+    set_error("m3sph_stokes_solve: call m3sph_stokes_setup first");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  M3_CUDA(cudaMemcpyAsync(W->pP, P, sizeof(double) * L0.nvnod, cudaMemcpyHostToDevice, s));
+  cudaEvent_t e0, e1;
+  M3_CUDA(cudaEventCreate(&e0));
+  M3_CUDA(cudaEventCreate(&e1));
+  M3_CUDA(cudaEventRecord(e0, s));
+  m3sph_info inf{};
+  int st = solve_core(M, opts, inf);
+  if (st) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+  }
+  M3_CUDA(cudaEventRecord(e1, s));
   // back-rotation U_xyz = RR U
-  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(U, M->fin.RR, L0.nnod, W->tmp);
-  M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  M3_CUDA(cudaMemcpyAsync(P, Pd, sizeof(double) * np, cudaMemcpyDeviceToHost, s));
+  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, W->tmp);
+  M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaMemcpyAsync(P, W->pP, sizeof(double) * L0.nvnod, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
-  auto t1 = std::chrono::steady_clock::now();
-  inf.t_iter_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  M3_TRY(time_since(e0, e1, inf.t_iter_ms));
+  inf.t_setup_ms = M->last_setup_ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   inf.status = M3SPH_OK;
   if (info) *info = inf;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_stokes_step_device(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info *info) {
+  if (!M || !opts || !M->have_operator) {
+    set_error("m3sph_stokes_step_device: call m3sph_stokes_setup first");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  cudaEvent_t e0, e1, e2;
+  M3_CUDA(cudaEventCreate(&e0));
+  M3_CUDA(cudaEventCreate(&e1));
+  M3_CUDA(cudaEventCreate(&e2));
+  M3_CUDA(cudaEventRecord(e0, s));
+  M3_TRY(rebuild_operator(M));
+  M3_CUDA(cudaEventRecord(e1, s));
+  M3_CUDA(cudaMemsetAsync(W->pP, 0, sizeof(double) * M->lev[0].nvnod, s));
+  m3sph_info inf{};
+  M3_TRY(solve_core(M, opts, inf));
+  M3_CUDA(cudaEventRecord(e2, s));
+  M3_CUDA(cudaEventSynchronize(e2));
+  M3_TRY(time_since(e0, e1, inf.t_setup_ms));
+  M3_TRY(time_since(e1, e2, inf.t_iter_ms));
+  for (cudaEvent_t e : {e0, e1, e2}) cudaEventDestroy(e);
+  inf.status = M3SPH_OK;
+  if (info) *info = inf;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_stream(m3sph_mesh *M, void **stream) {
+  if (!M || !stream) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  *stream = (void *)M->stream;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_solution(m3sph_mesh *M, double *U_xyz, double *P) {
+  M3_TRY(need_op_fwd(M));
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, W->tmp);
+  if (U_xyz) M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
+  if (P) M3_CUDA(cudaMemcpyAsync(P, W->pP, sizeof(double) * L0.nvnod, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
   return M3SPH_OK;
 }
 

@@ -156,6 +156,26 @@ class DeviceMesh:
         L.check(L.lib().m3sph_stokes_solve(self.h, L.dptr(U), L.dptr(P), C.byref(o), C.byref(info)))
         return U, P, info.as_dict()
 
+    def step_device(self, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20,
+                    target_rel_residual=0.0, smoother=0):
+        """Rebuild the operator from resident inputs and solve from P=0; results stay on device."""
+        o = L.Opts(rtol_Pat=rtol_Pat, rtol_U=rtol_U, itmax_Pat=itmax_Pat, itmin_Pat=itmin_Pat, itmax_U=itmax_U,
+                   precision=int(self.precision or 0), smoother=smoother, target_rel_residual=target_rel_residual)
+        info = L.Info()
+        L.check(L.lib().m3sph_stokes_step_device(self.h, C.byref(o), C.byref(info)))
+        return info.as_dict()
+
+    def solution(self):
+        U = np.empty(self.ndof)
+        P = np.empty(self.nvnod)
+        L.check(L.lib().m3sph_solution(self.h, L.dptr(U), L.dptr(P)))
+        return U, P
+
+    def stream(self):
+        p = C.c_void_p()
+        L.check(L.lib().m3sph_stream(self.h, C.byref(p)))
+        return p.value
+
 
 def flow3d_patera_sph(VAR, MESH, COMM, UBC, SETTINGS, PHYSICS, NUMSCALE, dt):
     """Mirror of flow3d_patera_sph.m:1-8 -> flow3d_patera_mg_sph_p on the GPU.
