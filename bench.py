@@ -1,0 +1,315 @@
+#!/usr/bin/env python3
+"""Benchmark: Stokes solve time to a 1e-8 coupled relative residual on the 8M-DOF shell.
+
+Workload: level-5 icosahedral shell, 32 layers (1,966,080 curved P2 tets, 7,987,590 velocity
+DOF), eta = eta0 exp(-gamma T) with a 1e4 contrast and a 30x jump below 660 km, 12 seeded plate
+caps at the surface, free slip at the CMB. One step = one hot-path pass: rebuild the element
+operator, Galerkin hierarchy and coarse inverse from the resident inputs and run the Patera / MG-PCG
+solve from P = 0 until the coupled FP64 residual is below 1e-8.
+
+Arms:
+  default (--impl gb300): FP32 V-cycle inside FP64 outer CG / Patera on the GPU (libm3sph.so).
+      The plain-FP64 GPU path (FP64 V-cycle) is timed on the same inputs for the comparison.
+  --impl reference: the FP64 CPU oracle (numpy/scipy restatement of the reference algorithm) on
+      the host cores, on a bounded sample of the same workload, extrapolated to one solve.
+
+Prints one JSON line. Multi-GPU runs are independent replicas (the solve does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Stokes solve time to 1e-8 rel. residual: learned+FP32-MG vs plain FP64 on 1 GPU"
+TARGET = 1e-8
+SOLVER_KW = dict(rtol_Pat=1e-9, rtol_U=1e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=TARGET)
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo", init_method="env://")
+        return rank, ws, td
+    return 0, 1, None
+
+
+def barrier(td):
+    if td is not None:
+        td.barrier()
+
+
+def allmax(td, v):
+    if td is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, out):
+        self.out = out
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.out, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self, dev=0):
+        try:
+            rows = [r.split(",") for r in open(self.out).read().strip().splitlines()]
+        except OSError:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9 and r[0].strip() == str(dev)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def apply_bytes(nel, ndof, s):
+    """Algorithmic bytes of one element-by-element operator application: packed element
+    matrices (465 values), connectivity (10 int32), x read and y written once."""
+    return nel * (465 * s + 40) + 2 * s * ndof
+
+
+def run_gb300(args, rank, ws, td):
+    from m3tet_sph_gb300 import build as B
+    B.build()
+    from m3tet_sph_gb300 import _lib, stokes, workloads
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    t0 = time.time()
+    w = workloads.make_workload(args.workload, seed=args.seed)
+    t_mesh = time.time() - t0
+    lv0 = w["levels"][0]
+    nel, ndof = lv0["nel"], 3 * lv0["nnod"]
+    dm = stokes.DeviceMesh(w["levels"], device=dev)
+    torch.cuda.set_device(dev)
+
+    def setup(prec):
+        dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=prec)
+
+    # ---- plain FP64 path (same inputs) ----
+    plain = None
+    if not args.skip_plain:
+        setup(0)
+        for _ in range(max(1, args.plain_warmup)):
+            info64 = dm.step_device(**SOLVER_KW)
+        barrier(td)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        infos64 = [dm.step_device(**SOLVER_KW) for _ in range(args.plain_steps)]
+        torch.cuda.synchronize()
+        t_plain = allmax(td, (time.perf_counter() - t) / args.plain_steps)
+        plain = dict(s_per_solve=t_plain, info=infos64[-1])
+        fp64_apply_ms = dm.apply_timing(0, 0, 5)
+    # ---- mixed path (the product): timed region ----
+    setup(1)
+    for _ in range(args.warmup):
+        dm.step_device(**SOLVER_KW)
+    stream = torch.cuda.ExternalStream(dm.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = _lib.launch_count()
+    barrier(td)
+    torch.cuda.synchronize()
+    clk = ClockSampler(str(ROOT / "gpurun_out" / "clocks_bench.csv") if (ROOT / "gpurun_out").is_dir()
+                       else "/tmp/m3sph_clocks.csv")
+    with clk:
+        ev0.record(stream)
+        infos = [dm.step_device(**SOLVER_KW) for _ in range(args.steps)]
+        ev1.record(stream)
+        ev1.synchronize()
+    launches = _lib.launch_count() - n0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = allmax(td, ms)
+    clocks = clk.summary(dev)
+    last = infos[-1]
+    # ---- operator roofline (FP32 EBE apply, dominant kernel of the V-cycle) ----
+    ms_apply32 = dm.apply_timing(0, 1, 10)
+    hbm, peak_kind = peaks()
+    b32 = apply_bytes(nel, ndof, 4)
+    achieved = b32 / (ms_apply32 * 1e-3) / 1e9
+    # ---- end-to-end through the public API with host buffers ----
+    U = np.empty(ndof)
+    P = np.zeros(lv0["EL2NOD"][:, :4].max() + 1)
+    te = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        setup(1)
+        U, P, einfo = dm.solve(P0=np.zeros_like(P), **SOLVER_KW)
+    t_e2e = allmax(td, (time.perf_counter() - te) / args.e2e_steps)
+    h2d = (w["visc"].nbytes + w["dens"].nbytes + 4 * len(w["ifix"]) + w["vfix"].nbytes + P.nbytes)
+    d2h = U.nbytes + P.nbytes
+    dm.close()
+    # ---- CPU baseline (rank 0, N=1): oracle on a bounded sample ----
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(w, plain["info"] if plain else last, args)
+    out = {
+        "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 outer / f32 V-cycle", "data": "synthetic",
+        "config": {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {nel} P2 tets, {ndof} velocity DOF, "
+                               f"{w['nmg']} MG levels, eta contrast 1e4 x30 jump, 12 plate caps",
+                   "nmg": w["nmg"], "solves_per_s": ws * 1e3 / ms,
+                   "l2": "working set (element matrices 11 GB) > L2; no flush needed",
+                   "parallelism": f"replicas x{ws}"},
+        "solve": {"itPat": last["itPat"], "nitU": last["nitU"], "nitZ": last["nitZ"], "nvcycle": last["nvcycle"],
+                  "rel_residual": last["rel_residual"], "t_setup_ms": last["t_setup_ms"],
+                  "t_iter_ms": last["t_iter_ms"]},
+        "plain_fp64": None if plain is None else {
+            "s_per_solve": plain["s_per_solve"], "rel_residual": plain["info"]["rel_residual"],
+            "itPat": plain["info"]["itPat"], "nitU": plain["info"]["nitU"], "nitZ": plain["info"]["nitZ"],
+            "t_setup_ms": plain["info"]["t_setup_ms"], "fp64_apply_ms": fp64_apply_ms,
+            "speedup_mixed_vs_plain": plain["s_per_solve"] / (ms / 1e3)},
+        "roofline": {"bound": "hbm", "kernel": "k_ebe_apply<float> (all colours)", "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
+                     "traffic": None, "bytes_per_apply": b32, "ms_per_apply": ms_apply32,
+                     "fp64_apply_gbs": apply_bytes(nel, ndof, 8) / (fp64_apply_ms * 1e-3) / 1e9 if plain else None},
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "rel_residual": einfo["rel_residual"]},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "mesh_build_s": t_mesh,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def cpu_baseline(w, gpu_info, args):
+    """FP64 oracle timed on the host: element matrices of a contiguous slice of the benchmark mesh
+    (scaled to all elements) plus MG-PCG iterations on the 3-level 130k-DOF shell (scaled per DOF
+    and by the iteration count the plain-FP64 GPU solve needed on the benchmark mesh)."""
+    from oracle import stokes_oracle as O
+    from m3tet_sph_gb300 import workloads
+    lv0 = w["levels"][0]
+    nel = lv0["nel"]
+    S = args.cpu_sample_els
+    sub = submesh(lv0, np.arange(S))
+    t = time.perf_counter()
+    O.element_matrices(sub, w["visc"][sub["gnodes"]], w["dens"][sub["gnodes"]], **w["phys"])
+    t_el = (time.perf_counter() - t) / S
+    c1 = workloads.make_workload("c1", seed=args.seed)
+    sysm = O.StokesSystem(c1["levels"], c1["visc"], c1["dens"], c1["ifix"], c1["vfix"], c1["phys"])
+    rng = np.random.default_rng(0)
+    b = rng.standard_normal(len(sysm.ifree))
+    t = time.perf_counter()
+    _, it, _ = sysm.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=args.cpu_iters)
+    t_it = (time.perf_counter() - t) / it
+    nU1 = 3 * c1["levels"][0]["nnod"]
+    nU2 = 3 * lv0["nnod"]
+    iters = gpu_info["nitU"] + gpu_info["nitZ"]
+    est = t_el * nel + t_it * (nU2 / nU1) * iters
+    return {"value": est, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"oracle element matrices of {S} of {nel} elements of this mesh ({t_el * 1e3:.3f} ms/el) + "
+                      f"{it} MG-PCG iterations on the 130,662-DOF shell ({t_it:.2f} s/it) scaled by DOF x "
+                      f"{iters} iterations of the plain-FP64 solve"}
+
+
+def submesh(lv, els):
+    """Elements `els` of a level with their nodes renumbered (for bounded oracle samples)."""
+    from m3tet_sph_gb300 import mesh as M
+    EL = lv["EL2NOD"][els]
+    g, inv = np.unique(EL, return_inverse=True)
+    iso_mask = np.isin(lv["els_iso"], els)
+    iso_new = np.searchsorted(els, lv["els_iso"][iso_mask]) if iso_mask.any() else np.zeros(0, np.int64)
+    return {"EL2NOD": inv.reshape(EL.shape), "GCOORD": lv["GCOORD"][:, g], "GCOORD_SPH": lv["GCOORD_SPH"][:, g],
+            "cls": lv["cls"][els], "els_iso": iso_new, "cubic_sph_rot": lv["cubic_sph_rot"][iso_mask],
+            "gnodes": g, "PointID": lv["PointID"][g]}
+
+
+def run_reference(args, rank, ws, td):
+    """CPU reference arm: the FP64 oracle on all host threads it can use, bounded per step."""
+    if rank != 0:
+        return
+    from m3tet_sph_gb300 import workloads
+    w = workloads.make_workload(args.workload, seed=args.seed)
+    fake_info = {"nitU": args.ref_iters // 2, "nitZ": args.ref_iters - args.ref_iters // 2}
+    for _ in range(args.warmup):
+        cpu_baseline(w, fake_info, argparse.Namespace(**{**vars(args), "cpu_sample_els": 2000, "cpu_iters": 1}))
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(w, fake_info, args))
+    v = float(np.mean([c["value"] for c in vals]))
+    out = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {w['levels'][0]['nel']} P2 tets"},
+           "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port", "sample": vals[-1]["sample"]},
+           "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--plain-warmup", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-sample-els", type=int, default=20000)
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--ref-iters", type=int, default=600)
+    args = ap.parse_args()
+    rank, ws, td = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws, td)
+    else:
+        run_gb300(args, rank, ws, td)
+    if td is not None:
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -60,6 +60,21 @@ typedef struct m3sph_level {
 
 typedef struct m3sph_mesh m3sph_mesh;   /* opaque: device-resident MESH + MG hierarchy */
 
+/* Semi-Lagrangian options (OPTS_SLM, default_numerics_M3TET.m:141-158). */
+typedef struct m3sph_slm_opts {
+  int32_t method_BT;      /* 1: PC2 predictor-corrector (the reference default) */
+  int32_t method_interp;  /* 0: 'quadratic' (interp3d_tet), 1: 'cubic' (interp3d_cubic_p) */
+  int32_t monotonic;      /* clamp to the element's nodal min/max */
+  int32_t method_wght;    /* cubic gradient weights: 0 'ones', 1 'dist' */
+  double r_cmb, r_surf;   /* MESH.r_cmb, MESH.r_surf */
+} m3sph_slm_opts;
+
+/* Point-location counters: points placed by the walk, points on shared faces resolved by the
+ * tie rule, points in frame gaps placed with a grown tolerance, brute-force placements, lost. */
+typedef struct m3sph_locate_info {
+  int32_t npt, nwalk, nties, ngap, nbrute, nlost;
+} m3sph_locate_info;
+
 /* Physical parameters used by the element operator (PHYSICS, NUMSCALE fields). */
 typedef struct m3sph_physics {
   double g;          /* PHYSICS.g (e.g. -9.81) */
@@ -128,6 +143,30 @@ M3SPH_API int m3sph_stokes_step_device(m3sph_mesh *mesh, const m3sph_opts *opts,
 M3SPH_API int m3sph_solution(m3sph_mesh *mesh, double *U_xyz, double *P);
 /* The CUDA stream (cudaStream_t) the handle launches its kernels on. */
 M3SPH_API int m3sph_stream(m3sph_mesh *mesh, void **stream);
+
+/* Cumulative number of CUDA kernels this library has launched (all handles). */
+M3SPH_API int m3sph_launch_count(unsigned long long *count);
+/* Operator benchmark: nrep device-resident applications of the level-`img` element operator in
+ * FP64 (precision 0) or FP32 (1); returns the mean time per full application (all colours). */
+M3SPH_API int m3sph_apply_timing(m3sph_mesh *mesh, int32_t img, int32_t precision, int32_t nrep, double *ms_per_apply);
+
+/* Replaces tsearch2_sph + local_coords_3d_sph (tsearch2_sph.m:1-424, local_coords_3d_sph.m:28-147):
+ * element (1-based, 0 = not found) and own-frame local coordinates (npt x 3) of points given as
+ * (theta,phi,r) triplets (npt x 3). els_guess (1-based, may be NULL) seeds the neighbour walk. */
+M3SPH_API int m3sph_tsearch_sph(m3sph_mesh *mesh, const double *thphr, int32_t npt, const int32_t *els_guess,
+                                int32_t *els_out, double *lc_out, m3sph_locate_info *info);
+/* Replaces interp3d_tet (interp3d_tet.m:39-69): V is nnod x nvar (nvar <= 3), Vi npt x nvar. */
+M3SPH_API int m3sph_interp3d_tet(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
+                                 const double *V, int32_t nvar, int32_t monotonic, double *Vi);
+/* Replaces interp3d_cubic_p (interp3d_cubic_p.m:80-382) for one nodal field V (nnod). */
+M3SPH_API int m3sph_interp3d_cubic(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
+                                   const double *V, int32_t monotonic, int32_t method_wght, double *Vi);
+/* Replaces advect3d_slm_p_sph (advect3d_slm_p_sph.m:1-139): Ux,Uy,Uz Cartesian nodal velocity,
+ * T (nnod) advected in place over dt. els_BT / els_INTERP (nnod, 1-based, 0 = unknown) are the
+ * WS_SLM search guesses, updated on return (predictor and departure elements). */
+M3SPH_API int m3sph_advect_slm(m3sph_mesh *mesh, const double *Ux, const double *Uy, const double *Uz, double *T,
+                               double dt, const m3sph_slm_opts *opts, int32_t *els_BT, int32_t *els_INTERP,
+                               m3sph_locate_info *info);
 
 /* Replaces one mgpcg_solver_p call (mgpcg_solver_p.m:1-743) on the current operator: solves
  * K1 x = b on the free dofs of the rotated frame (b, x: 3*nnod, fixed dofs ignored / zero).

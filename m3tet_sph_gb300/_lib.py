@@ -30,6 +30,19 @@ class Level(C.Structure):
                 ("els_iso", C.POINTER(C.c_uint32)), ("cubic_sph_rot", C.POINTER(C.c_double))]
 
 
+class SlmOpts(C.Structure):
+    _fields_ = [("method_BT", C.c_int32), ("method_interp", C.c_int32), ("monotonic", C.c_int32),
+                ("method_wght", C.c_int32), ("r_cmb", C.c_double), ("r_surf", C.c_double)]
+
+
+class LocateInfo(C.Structure):
+    _fields_ = [("npt", C.c_int32), ("nwalk", C.c_int32), ("nties", C.c_int32), ("ngap", C.c_int32),
+                ("nbrute", C.c_int32), ("nlost", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Physics(C.Structure):
     _fields_ = [("g", C.c_double), ("Bscale", C.c_double), ("Dens0", C.c_double),
                 ("minVisc", C.c_double), ("maxVisc", C.c_double)]
@@ -75,6 +88,12 @@ SIGNATURES = {
     "m3sph_stokes_step_device": ([P, C.POINTER(Opts), C.POINTER(Info)], C.c_int),
     "m3sph_solution": ([P, DP, DP], C.c_int),
     "m3sph_stream": ([P, C.POINTER(P)], C.c_int),
+    "m3sph_tsearch_sph": ([P, DP, C.c_int32, IP, IP, DP, C.POINTER(LocateInfo)], C.c_int),
+    "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
+    "m3sph_interp3d_cubic": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
+    "m3sph_advect_slm": ([P, DP, DP, DP, DP, C.c_double, C.POINTER(SlmOpts), IP, IP, C.POINTER(LocateInfo)], C.c_int),
+    "m3sph_launch_count": ([C.POINTER(C.c_ulonglong)], C.c_int),
+    "m3sph_apply_timing": ([P, C.c_int32, C.c_int32, C.c_int32, DP], C.c_int),
 }
 
 
@@ -123,3 +142,9 @@ def device_count():
     n = C.c_int32(0)
     code = lib().m3sph_device_count(C.byref(n))
     return n.value if code == OK else 0
+
+
+def launch_count():
+    n = C.c_ulonglong(0)
+    check(lib().m3sph_launch_count(C.byref(n)))
+    return n.value

@@ -2,11 +2,16 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/m3sph.h"
+
+struct m3sph_mesh;
 
 namespace m3sph {
 
@@ -20,7 +25,15 @@ constexpr int MAX_COLORS = 128;
 __host__ __device__ constexpr int pack_idx(int r, int c) { return c * (2 * NUDOF - c + 1) / 2 + (r - c); }
 
 void set_error(const std::string &msg);
+// host-side count of kernel launches issued by this library (reported by m3sph_launch_count)
+void count_launch();
 int cuda_fail(cudaError_t e, const char *what);
+
+#define M3_TRY(call)                 \
+  do {                               \
+    int _s = (call);                 \
+    if (_s != M3SPH_OK) return _s;   \
+  } while (0)
 
 #define M3_CUDA(call)                                  \
   do {                                                 \
@@ -77,6 +90,7 @@ struct Finest {
   double *G64 = nullptr;              // [120][nel]: G[p][3n+c]
   double *M64 = nullptr;              // [10][nel] packed lower 4x4
   double *Fbe = nullptr;              // [30][nel]
+  double *BCe = nullptr;              // [30][nel] K_unmasked * Ufix per element
   double *Fb = nullptr;               // [ndof] assembled, rotated
   double *LiMM = nullptr;             // [nvnod] inverse lumped M
   int *err = nullptr;                 // device error flags
@@ -100,8 +114,12 @@ struct SetupArgs {
   const uint8_t *freemask;
   double g, Bscale, Dens0, minVisc, maxVisc;
   double *K64; float *K32; double *G64; double *M64; double *Fbe;
+  const double *ufix;       // [3*nnod] prescribed values (rotated frame) or nullptr
+  double *BCe;              // [30][nel] element K_unmasked * ufix (when ufix != nullptr)
   int *err;
 };
+
+int slm_build(m3sph_mesh *M, const m3sph_level &f0);
 
 }  // namespace m3sph
 
@@ -120,10 +138,16 @@ struct m3sph_mesh {
   std::vector<double> h_vfix;
   double *Ufix = nullptr;             // [ndof0] prescribed values (rotated frame)
   double *bc_rhs = nullptr;           // K1_full * Ufix
+  bool has_nonzero_fix = false;
   // scratch
   std::vector<void *> work;           // device buffers owned by the workspace
   void *wk = nullptr;                 // host-side workspace descriptor
   void (*wk_free)(void *) = nullptr;
+  std::vector<std::pair<double *, cudaGraphExec_t>> graphs;   // captured MG-PCG iterations
+  bool use_graphs = true;
+  unsigned long long graph_kernels = 0;   // kernel launches per captured iteration
+  void *slm = nullptr;                // advection / point-location state
+  void (*slm_free)(void *) = nullptr;
   double *red = nullptr;              // reduction partials
   double *scal = nullptr;             // device scalars
   double *h_scal = nullptr;           // pinned host mirror

@@ -37,7 +37,8 @@ constexpr int SM_FG = NIP;              // weight * buoyancy
 constexpr int SM_DIR = NIP * 3;         // radial unit vector in element frame
 constexpr int SM_VC = 60;               // frame (theta,phi,r) of 4 (or 20) geometry nodes
 constexpr int SM_Q = 90;                // per node: Q = R_cls * RR (3x3)
-constexpr int SM_PER_EL = SM_DN + SM_W + SM_W2 + SM_W3 + SM_FG + SM_DIR + SM_VC + SM_Q;
+constexpr int SM_BC = 30;               // unmasked K * Ufix per element dof
+constexpr int SM_PER_EL = SM_DN + SM_W + SM_W2 + SM_W3 + SM_FG + SM_DIR + SM_VC + SM_Q + SM_BC;
 size_t element_setup_smem() { return sizeof(double) * SM_PER_EL * EB + sizeof(int) * 2 * EB; }
 
 
@@ -59,7 +60,8 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
   double *sDIR = sFG + SM_FG * EB;           // [ip][3][EB]
   double *sVC = sDIR + SM_DIR * EB;          // [k][node][EB], node < 4 (or 20 for iso)
   double *sQ = sVC + SM_VC * EB;             // [n][9][EB]
-  int *sMask = reinterpret_cast<int *>(sQ + SM_Q * EB);
+  double *sBC = sQ + SM_Q * EB;              // [30][EB]
+  int *sMask = reinterpret_cast<int *>(sBC + SM_BC * EB);
   int *sCls = sMask + EB;
   const int e0 = blockIdx.x * EB;
   const int tid = threadIdx.x;
@@ -117,6 +119,7 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
     }
     sMask[el] = mask;
     sCls[el] = cls;
+    for (int q = 0; q < 30; ++q) sBC[q * EB + el] = 0.0;
   }
   __syncthreads();
 
@@ -234,11 +237,23 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
     for (int p = 0; p < 3; ++p)
       for (int q = 0; q < 3; ++q) T[p][q] = B[p][0] * Qj[0 * 3 + q] + B[p][1] * Qj[1 * 3 + q] + B[p][2] * Qj[2 * 3 + q];
     const int mask = sMask[el];
+    const bool bc = a.ufix != nullptr;
+    int ni = 0, nj = 0;
+    if (bc) {
+      ni = a.el2nod[(size_t)i * nel + e];
+      nj = a.el2nod[(size_t)j * nel + e];
+    }
     for (int p = 0; p < 3; ++p)
       for (int q = 0; q < 3; ++q) {
         const int rr = 3 * i + p, cc = 3 * j + q;
-        if (rr < cc) continue;
         double v = Qi[0 * 3 + p] * T[0][q] + Qi[1 * 3 + p] * T[1][q] + Qi[2 * 3 + p] * T[2][q];
+        if (bc) {
+          // boundary-condition rhs from the unmasked operator: K(:,ifix) * Ufix
+          // (flow3d_patera_mg_sph_p.m:269-283); each (i,j) block also stands for (j,i) when i > j
+          atomicAdd(&sBC[rr * EB + el], v * a.ufix[3 * nj + q]);
+          if (i != j) atomicAdd(&sBC[cc * EB + el], v * a.ufix[3 * ni + p]);
+        }
+        if (rr < cc) continue;
         if (!((mask >> rr) & 1) || !((mask >> cc) & 1)) v = 0.0;
         const size_t k = (size_t)pack_idx(rr, cc) * nel + e;
         a.K64[k] = v;
@@ -287,13 +302,20 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
       a.Fbe[(size_t)(3 * n + cc) * nel + e] = v;
     }
   }
+  if (a.ufix) {
+    __syncthreads();
+    for (int t = tid; t < 30 * EB; t += SETUP_THREADS) {
+      const int q = t / EB, el = t % EB, e = e0 + el;
+      if (e < nel) a.BCe[(size_t)q * nel + e] = sBC[q * EB + el];
+    }
+  }
 }
 
 int launch_element_setup(const SetupArgs &a, cudaStream_t s) {
   const size_t smem = element_setup_smem();
   M3_CUDA(cudaFuncSetAttribute(k_element_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (a.nel + EB - 1) / EB;
-  k_element_setup<<<grid, SETUP_THREADS, smem, s>>>(a);
+  k_element_setup<<<grid, SETUP_THREADS, smem, s>>>(a); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -340,7 +362,7 @@ int ebe_apply(const Level &L, const T *K, const T *x, T *y, cudaStream_t s) {
   for (int c = 0; c < nc; ++c) {
     const int b = L.cstart[c], e = L.cstart[c + 1];
     if (e <= b) continue;
-    k_ebe_apply<T><<<(e - b + 127) / 128, 128, 0, s>>>(K, L.el2nod, L.nel, b, e, x, y);
+    k_ebe_apply<T><<<(e - b + 127) / 128, 128, 0, s>>>(K, L.el2nod, L.nel, b, e, x, y); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -366,7 +388,7 @@ int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double 
   for (int c = 0; c < nc; ++c) {
     const int b = L.cstart[c], e = L.cstart[c + 1];
     if (e <= b) continue;
-    k_scatter_elvec<<<(e - b + 127) / 128, 128, 0, s>>>(V, nq, per_node, L.el2nod, L.nel, b, e, out);
+    k_scatter_elvec<<<(e - b + 127) / 128, 128, 0, s>>>(V, nq, per_node, L.el2nod, L.nel, b, e, out); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -399,9 +421,9 @@ int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s) {
   for (int c = 0; c < nc; ++c) {
     const int b = L.cstart[c], e = L.cstart[c + 1];
     if (e <= b) continue;
-    k_diag_scatter<T><<<(e - b + 127) / 128, 128, 0, s>>>(K, L.el2nod, L.nel, b, e, work);
+    k_diag_scatter<T><<<(e - b + 127) / 128, 128, 0, s>>>(K, L.el2nod, L.nel, b, e, work); count_launch();
   }
-  k_invert_diag<<<(L.ndof + 255) / 256, 256, 0, s>>>(work, L.freemask, L.ndof, L.Dinv64, L.Dinv32);
+  k_invert_diag<<<(L.ndof + 255) / 256, 256, 0, s>>>(work, L.freemask, L.ndof, L.Dinv64, L.Dinv32); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -469,7 +491,7 @@ int grad_apply(const Level &L, const double *G, const double *q, double *y, cuda
   M3_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * L.ndof, s));
   for (size_t c = 0; c + 1 < L.cstart.size(); ++c) {
     const int b = L.cstart[c], e = L.cstart[c + 1];
-    if (e > b) k_grad<<<(e - b + 127) / 128, 128, 0, s>>>(G, L.el2nod, L.nel, b, e, q, y);
+    if (e > b) k_grad<<<(e - b + 127) / 128, 128, 0, s>>>(G, L.el2nod, L.nel, b, e, q, y); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -478,7 +500,7 @@ int div_apply(const Level &L, const double *G, const double *z, double *out, cud
   M3_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * L.nvnod, s));
   for (size_t c = 0; c + 1 < L.cstart.size(); ++c) {
     const int b = L.cstart[c], e = L.cstart[c + 1];
-    if (e > b) k_div<<<(e - b + 127) / 128, 128, 0, s>>>(G, L.el2nod, L.nel, b, e, z, out);
+    if (e > b) k_div<<<(e - b + 127) / 128, 128, 0, s>>>(G, L.el2nod, L.nel, b, e, z, out); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -487,7 +509,7 @@ int mass_apply(const Level &L, const double *M, const double *d, double *out, cu
   M3_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * L.nvnod, s));
   for (size_t c = 0; c + 1 < L.cstart.size(); ++c) {
     const int b = L.cstart[c], e = L.cstart[c + 1];
-    if (e > b) k_mass<<<(e - b + 127) / 128, 128, 0, s>>>(M, L.el2nod, L.nel, b, e, d, out);
+    if (e > b) k_mass<<<(e - b + 127) / 128, 128, 0, s>>>(M, L.el2nod, L.nel, b, e, d, out); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -579,7 +601,7 @@ __global__ void __launch_bounds__(256) k_galerkin(const T *__restrict__ Kf, int 
 
 template <typename T>
 int galerkin(const Level &F, const T *Kf, Level &C, T *Kc, cudaStream_t s) {
-  k_galerkin<T><<<C.nel, 256, 0, s>>>(Kf, F.nel, C.child, C.child_vloc, C.nel, C.el2nod, C.freemask, Kc);
+  k_galerkin<T><<<C.nel, 256, 0, s>>>(Kf, F.nel, C.child, C.child_vloc, C.nel, C.el2nod, C.freemask, Kc); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -591,7 +613,7 @@ __global__ void k_f64_to_f32(const double *a, float *b, size_t n) {
   if (i < n) b[i] = (float)a[i];
 }
 int convert_f64_f32(const double *a, float *b, size_t n, cudaStream_t s) {
-  k_f64_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n);
+  k_f64_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }

@@ -87,20 +87,20 @@ __global__ void k_sum(const double *__restrict__ a, size_t n, double *partials) 
 }
 
 int dot(const double *a, const double *b, size_t n, double *partials, double *out, cudaStream_t s) {
-  k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n, partials);
-  k_finish<1><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, out);
+  k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n, partials); count_launch();
+  k_finish<1><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, out); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 int dot2(const double *a, const double *c, const double *b, size_t n, double *partials, double *out, cudaStream_t s) {
-  k_dot2<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, c, b, n, partials);
-  k_finish<2><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, out);
+  k_dot2<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, c, b, n, partials); count_launch();
+  k_finish<2><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, out); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 int vsum(const double *a, size_t n, double *partials, double *out, cudaStream_t s) {
-  k_sum<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, n, partials);
-  k_finish<1><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, out);
+  k_sum<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, n, partials); count_launch();
+  k_finish<1><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, out); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -111,6 +111,7 @@ int vsum(const double *a, size_t n, double *partials, double *out, cudaStream_t 
 // ---------------------------------------------------------------------------------------
 // q = d + beta q, beta = -alpha_prev * (Kq_prev . d) / rdlast (Polak-Ribiere: (r - rlast).d / rdlast)
 __global__ void k_cg_dir(const double *__restrict__ d, double *__restrict__ q, size_t n, const double *scal, int first) {
+  if (first < 0) first = scal[6] != 0.0;   // flag kept on the device (graph replay)
   double beta = 0.0;
   if (!first) beta = -scal[5] * scal[1] / scal[4];
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -138,15 +139,15 @@ __global__ void k_cg_roll(double *scal) {
 }
 
 int cg_dir(const double *d, double *q, size_t n, const double *scal, int first, cudaStream_t s) {
-  k_cg_dir<<<RED_BLOCKS, RED_THREADS, 0, s>>>(d, q, n, scal, first);
+  k_cg_dir<<<RED_BLOCKS, RED_THREADS, 0, s>>>(d, q, n, scal, first); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 int cg_update(double *x, double *r, const double *q, const double *Kq, size_t n, double *scal, double *partials,
               cudaStream_t s) {
-  k_cg_update<<<RED_BLOCKS, RED_THREADS, 0, s>>>(x, r, q, Kq, n, scal, partials);
-  k_finish<1><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, scal + 3);
-  k_cg_roll<<<1, 1, 0, s>>>(scal);
+  k_cg_update<<<RED_BLOCKS, RED_THREADS, 0, s>>>(x, r, q, Kq, n, scal, partials); count_launch();
+  k_finish<1><<<1, 1024, 0, s>>>(partials, RED_BLOCKS, scal + 3); count_launch();
+  k_cg_roll<<<1, 1, 0, s>>>(scal); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -159,7 +160,7 @@ __global__ void k_axpby(double a, const double *__restrict__ x, double b, double
     y[i] = a * x[i] + b * y[i];
 }
 int axpby(double a, const double *x, double b, double *y, size_t n, cudaStream_t s) {
-  k_axpby<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, x, b, y, n);
+  k_axpby<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, x, b, y, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -170,7 +171,7 @@ __global__ void k_sub_mask(const double *__restrict__ b, double *__restrict__ y,
     y[i] = mask[i] ? b[i] - y[i] : 0.0;
 }
 int sub_mask(const double *b, double *y, const uint8_t *mask, size_t n, cudaStream_t s) {
-  k_sub_mask<<<RED_BLOCKS, RED_THREADS, 0, s>>>(b, y, mask, n);
+  k_sub_mask<<<RED_BLOCKS, RED_THREADS, 0, s>>>(b, y, mask, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -179,7 +180,7 @@ __global__ void k_mask(double *__restrict__ y, const uint8_t *__restrict__ mask,
     if (!mask[i]) y[i] = 0.0;
 }
 int apply_mask(double *y, const uint8_t *mask, size_t n, cudaStream_t s) {
-  k_mask<<<RED_BLOCKS, RED_THREADS, 0, s>>>(y, mask, n);
+  k_mask<<<RED_BLOCKS, RED_THREADS, 0, s>>>(y, mask, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -189,12 +190,12 @@ __global__ void k_convert(const A *__restrict__ a, B *__restrict__ b, size_t n) 
     b[i] = (B)a[i];
 }
 int d2f(const double *a, float *b, size_t n, cudaStream_t s) {
-  k_convert<double, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n);
+  k_convert<double, float><<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 int f2d(const float *a, double *b, size_t n, cudaStream_t s) {
-  k_convert<float, double><<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n);
+  k_convert<float, double><<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, b, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -217,13 +218,13 @@ __global__ void k_jac(T w, const T *__restrict__ r0, const T *__restrict__ Kd, c
 }
 template <typename T>
 int jac_first(T w, const T *r0, const T *Di, T *d, size_t n, cudaStream_t s) {
-  k_jac_first<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(w, r0, Di, d, n);
+  k_jac_first<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(w, r0, Di, d, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 template <typename T>
 int jac(T w, const T *r0, const T *Kd, const T *Di, T *d, size_t n, cudaStream_t s) {
-  k_jac<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(w, r0, Kd, Di, d, n);
+  k_jac<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(w, r0, Kd, Di, d, n); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -282,13 +283,13 @@ __global__ void k_prolong(const int *__restrict__ ptr, const int *__restrict__ c
 }
 template <typename T>
 int restrict_(const Level &F, const Level &C, const T *a, const T *b, T *out, cudaStream_t s) {
-  k_restrict<T><<<(C.nnod + 255) / 256, 256, 0, s>>>(F.R_ptr, F.R_col, F.R_w, C.nnod, a, b, C.freemask, out);
+  k_restrict<T><<<(C.nnod + 255) / 256, 256, 0, s>>>(F.R_ptr, F.R_col, F.R_w, C.nnod, a, b, C.freemask, out); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 template <typename T>
 int prolong(const Level &F, const Level &C, const T *xc, const T *add, T *out, cudaStream_t s) {
-  k_prolong<T><<<(F.nnod + 255) / 256, 256, 0, s>>>(F.P_ptr, F.P_col, F.P_w, F.nnod, xc, add, F.freemask, out);
+  k_prolong<T><<<(F.nnod + 255) / 256, 256, 0, s>>>(F.P_ptr, F.P_col, F.P_w, F.nnod, xc, add, F.freemask, out); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -348,13 +349,13 @@ template <typename T>
 int dense_inverse(const Level &L, const T *K, T *A, T *work, cudaStream_t s) {
   const int n = L.ndof;
   M3_CUDA(cudaMemsetAsync(A, 0, sizeof(T) * (size_t)n * n, s));
-  k_dense_assemble<T><<<L.nel, 128, 0, s>>>(K, L.el2nod, L.nel, n, A);
-  k_dense_fix_diag<T><<<(n + 255) / 256, 256, 0, s>>>(A, L.freemask, n);
+  k_dense_assemble<T><<<L.nel, 128, 0, s>>>(K, L.el2nod, L.nel, n, A); count_launch();
+  k_dense_fix_diag<T><<<(n + 255) / 256, 256, 0, s>>>(A, L.freemask, n); count_launch();
   T *colk = work, *rowk = work + n;
   dim3 g((n + 255) / 256, n);
   for (int k = 0; k < n; ++k) {
-    k_gj_save<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, k, colk, rowk);
-    k_gj_update<T><<<g, 256, 0, s>>>(A, n, k, colk, rowk);
+    k_gj_save<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, k, colk, rowk); count_launch();
+    k_gj_update<T><<<g, 256, 0, s>>>(A, n, k, colk, rowk); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -377,7 +378,7 @@ __global__ void k_dense_gemv(const T *__restrict__ A, int n, const T *__restrict
 }
 template <typename T>
 int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s) {
-  k_dense_gemv<T><<<(n + 7) / 8, 256, 0, s>>>(A, n, x, mask, y);
+  k_dense_gemv<T><<<(n + 7) / 8, 256, 0, s>>>(A, n, x, mask, y); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }

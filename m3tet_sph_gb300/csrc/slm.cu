@@ -1,0 +1,912 @@
+// Semi-Lagrangian thermal advection on the curved shell: PC2 departure points, curved-element
+// point location by neighbour walk, P2 and quasi-cubic interpolation.
+//
+// Reference behaviour restated (paths inside the reference project):
+//   mfiles_SPH/advect3d_slm_p_sph.m:165-242 (PC2), :298-410 (predictor), :412-440 (corrector)
+//   mfiles_SPH/find_pts_outside_domain_sph.m:27-98 (radial clamp)
+//   mfiles_SPH/local_coords_3d_sph.m:28-147 (per-class frames, barycentric determinant ratios)
+//   mfiles_SPH/local_coords_curved_3d_sph.m:36-168 (Newton on the 10-node map, X-90 frame)
+//   mfiles_SPH/locate_points_interp_vars_3d_sph.m:34-207, mfiles_SPH/tsearch2_sph.m:374-404
+//   mfiles_M3TET/locate_points_in_neighboring_element.m:1-158 (tolerance growth to 15e-3)
+//   mfiles_M3TET/interp3d_tet.m:39-69, mfiles_M3TET/interp3d_cubic_p.m:80-382
+//
+// Point location contract: a point gets the element whose own-frame barycentric coordinates all
+// lie in [0,1]; if several do (points on shared faces), non-isoparametric elements win, then
+// the largest element id; if none does, the vertex-neighbours of the last walked element are
+// searched with a tolerance grown in 1e-6 steps up to 15e-3. Every walk has a step limit.
+#include "common.cuh"
+
+namespace m3sph {
+
+constexpr int WALK_MAX_STEPS = 512;
+constexpr double TIE_EPS = 1e-10;
+
+struct SlmMesh {
+  int nel, nnod, nvnod;
+  const int *el2nod;     // [10][nel] original order
+  const int *nbr;        // [4][nel] neighbour across the face opposite local vertex k, -1 on the boundary
+  const uint8_t *cls;    // [nel]
+  const double *S0;      // [3][nvnod] GCOORD_SPH of vertices
+  const double *SZ;      // [3][nvnod] Z-180 frame of vertices
+  const double *SX;      // [3][nnod]  X-90 frame of all nodes
+  const int *v2e_ptr;    // [nvnod+1]
+  const int *v2e;        // vertex -> elements
+};
+
+__device__ __forceinline__ void sph2cart_d(double th, double ph, double r, double &x, double &y, double &z) {
+  double st, ct, sp, cp;
+  sincos(th, &st, &ct);
+  sincos(ph, &sp, &cp);
+  x = r * st * cp;
+  y = r * st * sp;
+  z = r * ct;
+}
+__device__ __forceinline__ void c2s(double x, double y, double z, double &th, double &ph, double &r) {
+  r = sqrt(x * x + y * y + z * z);
+  th = atan2(sqrt(x * x + y * y), z);
+  ph = atan2(y, x);
+  if (ph < 0.0) ph += 2.0 * M_PI;
+}
+
+struct PointFrames {
+  double p0[3], pz[3], px[3];
+};
+
+__device__ __forceinline__ void point_frames(double th, double ph, double r, PointFrames &f) {
+  f.p0[0] = th; f.p0[1] = ph; f.p0[2] = r;
+  double x, y, z;
+  sph2cart_d(th, ph, r, x, y, z);
+  c2s(-x, -y, z, f.pz[0], f.pz[1], f.pz[2]);     // 180 deg about z
+  c2s(x, -z, y, f.px[0], f.px[1], f.px[2]);      // 90 deg about x
+}
+
+// barycentric determinant ratio of local_coords_3d_sph.m:94-147 for vertex a (b,c,d the others)
+__device__ __forceinline__ double dratio(const double (&t)[4], const double (&p)[4], const double (&q)[4], int b,
+                                         int c, int d, double tp, double pp, double rp, int a) {
+  auto D = [&](double ta, double pa, double ra) {
+    return (t[b] - ta) * (p[c] - pa) * (q[d] - ra) + (t[c] - ta) * (p[d] - pa) * (q[b] - ra) +
+           (t[d] - ta) * (p[b] - pa) * (q[c] - ra) - (q[b] - ra) * (p[c] - pa) * (t[d] - ta) -
+           (q[c] - ra) * (p[d] - pa) * (t[b] - ta) - (q[d] - ra) * (p[b] - pa) * (t[c] - ta);
+  };
+  return D(tp, pp, rp) / D(t[a], p[a], q[a]);
+}
+
+__device__ __forceinline__ void lc_straight(const double (&t)[4], const double (&p)[4], const double (&q)[4],
+                                            const double *pt, double *lc) {
+  lc[0] = dratio(t, p, q, 1, 2, 3, pt[0], pt[1], pt[2], 0);
+  lc[1] = dratio(t, p, q, 0, 2, 3, pt[0], pt[1], pt[2], 1);
+  lc[2] = dratio(t, p, q, 0, 1, 3, pt[0], pt[1], pt[2], 2);
+}
+
+// own-frame local coordinates of point f in element e; returns Newton step size for iso elements
+__device__ double local_coords(const SlmMesh &m, int e, const PointFrames &f, double *lc) {
+  const int cls = m.cls[e];
+  double t[4], p[4], q[4];
+  int v[4];
+  for (int i = 0; i < 4; ++i) v[i] = m.el2nod[(size_t)i * m.nel + e];
+  if (cls == M3SPH_OUT_CONE_NO_CROSS_2PI) {
+    for (int i = 0; i < 4; ++i) { t[i] = m.S0[v[i]]; p[i] = m.S0[m.nvnod + v[i]]; q[i] = m.S0[2 * m.nvnod + v[i]]; }
+    lc_straight(t, p, q, f.p0, lc);
+    return 0.0;
+  }
+  if (cls == M3SPH_OUT_CONE_CROSS_2PI) {
+    for (int i = 0; i < 4; ++i) { t[i] = m.SZ[v[i]]; p[i] = m.SZ[m.nvnod + v[i]]; q[i] = m.SZ[2 * m.nvnod + v[i]]; }
+    lc_straight(t, p, q, f.pz, lc);
+    return 0.0;
+  }
+  for (int i = 0; i < 4; ++i) { t[i] = m.SX[v[i]]; p[i] = m.SX[m.nnod + v[i]]; q[i] = m.SX[2 * m.nnod + v[i]]; }
+  lc_straight(t, p, q, f.px, lc);
+  if (cls != M3SPH_IN_CONE_ISO) return 0.0;
+  // Newton on the 10-node map (local_coords_curved_3d_sph.m:45-168): up to 6 steps, tol 1e-8
+  double G[3][10];
+  for (int n = 0; n < 10; ++n) {
+    const int nod = m.el2nod[(size_t)n * m.nel + e];
+    for (int k = 0; k < 3; ++k) G[k][n] = m.SX[(size_t)k * m.nnod + nod];
+  }
+  double step = 0.0;
+  for (int it = 0; it < 6; ++it) {
+    const double r = lc[0], s = lc[1], tt = lc[2], u = 1.0 - r - s - tt;
+    const double N[10] = {r * (2 * r - 1), s * (2 * s - 1), tt * (2 * tt - 1), u * (2 * u - 1), 4 * r * s,
+                          4 * s * tt, 4 * tt * u, 4 * r * u, 4 * r * tt, 4 * s * u};
+    const double dN[10][3] = {{4 * r - 1, 0, 0}, {0, 4 * s - 1, 0}, {0, 0, 4 * tt - 1},
+                              {1 - 4 * u, 1 - 4 * u, 1 - 4 * u}, {4 * s, 4 * r, 0}, {0, 4 * tt, 4 * s},
+                              {-4 * tt, -4 * tt, 4 * (u - tt)}, {4 * (u - r), -4 * r, -4 * r},
+                              {4 * tt, 0, 4 * r}, {-4 * s, 4 * (u - s), -4 * s}};
+    double d[3], J[3][3];
+    for (int k = 0; k < 3; ++k) {
+      double s0 = 0.0;
+      for (int n = 0; n < 10; ++n) s0 += G[k][n] * N[n];
+      d[k] = f.px[k] - s0;
+      for (int j = 0; j < 3; ++j) {
+        double sj = 0.0;
+        for (int n = 0; n < 10; ++n) sj += G[k][n] * dN[n][j];
+        J[k][j] = sj;
+      }
+    }
+    if (sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < 1e-8) break;
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    const double id = 1.0 / det;
+    const double ds0 = id * ((J[1][1] * J[2][2] - J[1][2] * J[2][1]) * d[0] + (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * d[1] +
+                             (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * d[2]);
+    const double ds1 = id * ((J[1][2] * J[2][0] - J[1][0] * J[2][2]) * d[0] + (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * d[1] +
+                             (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * d[2]);
+    const double ds2 = id * ((J[1][0] * J[2][1] - J[1][1] * J[2][0]) * d[0] + (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * d[1] +
+                             (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * d[2]);
+    lc[0] += ds0;
+    lc[1] += ds1;
+    lc[2] += ds2;
+    step = fabs(ds0) + fabs(ds1) + fabs(ds2);
+  }
+  return step;
+}
+
+__device__ __forceinline__ void bary_minmax(const double *lc, double &mn, double &mx, int &argmn) {
+  const double l4 = 1.0 - lc[0] - lc[1] - lc[2];
+  const double b[4] = {lc[0], lc[1], lc[2], l4};
+  mn = b[0];
+  mx = b[0];
+  argmn = 0;
+  for (int k = 1; k < 4; ++k) {
+    if (b[k] < mn) { mn = b[k]; argmn = k; }
+    mx = fmax(mx, b[k]);
+  }
+}
+
+// tie / gap resolution among elements sharing a vertex with e0
+__device__ int resolve_local(const SlmMesh &m, int e0, const PointFrames &f, double *lc_out, bool gap) {
+  int best = -1, best_iso = 1;
+  double best_need = 1e300;
+  double blc[3] = {0, 0, 0};
+  for (int i = 0; i < 4; ++i) {
+    const int v = m.el2nod[(size_t)i * m.nel + e0];
+    for (int k = m.v2e_ptr[v]; k < m.v2e_ptr[v + 1]; ++k) {
+      const int e = m.v2e[k];
+      double lc[3], mn, mx;
+      int am;
+      local_coords(m, e, f, lc);
+      bary_minmax(lc, mn, mx, am);
+      const double need = fmax(-mn, mx - 1.0);
+      // quantise the tolerance to the reference's 1e-6 steps when searching a gap
+      const double q = gap ? ceil(need / 1e-6 - 1e-9) : (need <= 0.0 ? 0.0 : 1e300);
+      const int iso = m.cls[e] == M3SPH_IN_CONE_ISO;
+      bool better = false;
+      if (q < best_need) better = true;
+      else if (q == best_need) {
+        if (iso < best_iso) better = true;
+        else if (iso == best_iso && e > best) better = true;
+      }
+      if (better) {
+        best = e; best_need = q; best_iso = iso;
+        blc[0] = lc[0]; blc[1] = lc[1]; blc[2] = lc[2];
+      }
+    }
+  }
+  if (best >= 0 && (!gap || best_need * 1e-6 <= 15e-3 + 1e-6) && (gap || best_need == 0.0)) {
+    lc_out[0] = blc[0]; lc_out[1] = blc[1]; lc_out[2] = blc[2];
+    return best;
+  }
+  return -1;
+}
+
+// one thread per point: walk from the guess to the containing element.
+// status bits: 1 = found by walk, 2 = tie resolved locally, 4 = gap (tolerance), 8 = not found
+__global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const int *__restrict__ guess,
+                         const int *__restrict__ node_guess, int *__restrict__ els, double *__restrict__ lc_out,
+                         uint8_t *__restrict__ status, int adjust) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npt) return;
+  PointFrames f;
+  point_frames(P[i], P[npt + i], P[2 * npt + i], f);
+  int e = guess ? guess[i] : -1;
+  if ((e < 0 || e >= m.nel) && node_guess) e = node_guess[i];
+  if (e < 0 || e >= m.nel) e = 0;
+  int prev = -1, found = -1;
+  double lc[3] = {0, 0, 0};
+  uint8_t st = 0;
+  for (int step = 0; step < WALK_MAX_STEPS; ++step) {
+    double mn, mx;
+    int am;
+    local_coords(m, e, f, lc);
+    bary_minmax(lc, mn, mx, am);
+    if (mn >= 0.0 && mx <= 1.0) {
+      found = e;
+      break;
+    }
+    // leave through the face opposite the most negative barycentric; avoid stepping straight back
+    int nb = m.nbr[(size_t)am * m.nel + e];
+    if (nb == prev || nb < 0) {
+      const double b[4] = {lc[0], lc[1], lc[2], 1.0 - lc[0] - lc[1] - lc[2]};
+      int alt = -1;
+      double amin = 1e300;
+      for (int k = 0; k < 4; ++k) {
+        if (k == am || b[k] >= 0.0) continue;
+        const int c = m.nbr[(size_t)k * m.nel + e];
+        if (c >= 0 && c != prev && b[k] < amin) { amin = b[k]; alt = c; }
+      }
+      if (alt < 0) break;
+      nb = alt;
+    }
+    prev = e;
+    e = nb;
+  }
+  if (found >= 0) {
+    st = 1;
+    double mn, mx;
+    int am;
+    bary_minmax(lc, mn, mx, am);
+    if (mn < TIE_EPS || mx > 1.0 - TIE_EPS) {
+      const int r = resolve_local(m, found, f, lc, false);
+      if (r >= 0) {
+        found = r;
+        st |= 2;
+      }
+    }
+  } else {
+    const int r = resolve_local(m, e, f, lc, true);
+    if (r >= 0) {
+      found = r;
+      st = 4;
+    } else {
+      st = 8;
+    }
+  }
+  if (adjust && found >= 0) {   // adjust_local_coords (locate_points_interp_vars_3d_sph.m:180-198)
+    for (int k = 0; k < 3; ++k) lc[k] = fmin(fmax(lc[k], 0.0), 1.0);
+    const double s = lc[0] + lc[1] + lc[2];
+    if (s > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= s;
+  }
+  els[i] = found;
+  lc_out[i] = lc[0];
+  lc_out[npt + i] = lc[1];
+  lc_out[2 * npt + i] = lc[2];
+  status[i] = st;
+}
+
+// brute force over all elements for points the walk could not place (status 8)
+__global__ void k_locate_brute(SlmMesh m, const double *__restrict__ P, int npt, const int *__restrict__ todo,
+                               int ntodo, int *__restrict__ els, double *__restrict__ lc_out, uint8_t *status) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= ntodo) return;
+  const int i = todo[w];
+  PointFrames f;
+  point_frames(P[i], P[npt + i], P[2 * npt + i], f);
+  double best_need = 1e300;
+  int best = -1;
+  for (int e = lane; e < m.nel; e += 32) {
+    double lc[3], mn, mx;
+    int am;
+    local_coords(m, e, f, lc);
+    bary_minmax(lc, mn, mx, am);
+    const double need = fmax(fmax(-mn, mx - 1.0), 0.0);
+    if (need < best_need || (need == best_need && e > best)) { best_need = need; best = e; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double on = __shfl_xor_sync(0xffffffffu, best_need, o);
+    const int oe = __shfl_xor_sync(0xffffffffu, best, o);
+    if (on < best_need || (on == best_need && oe > best)) { best_need = on; best = oe; }
+  }
+  if (lane == 0 && best >= 0 && best_need <= 15e-3) {
+    double lc[3];
+    local_coords(m, best, f, lc);
+    for (int k = 0; k < 3; ++k) lc[k] = fmin(fmax(lc[k], 0.0), 1.0);
+    const double s = lc[0] + lc[1] + lc[2];
+    if (s > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= s;
+    els[i] = best;
+    lc_out[i] = lc[0];
+    lc_out[npt + i] = lc[1];
+    lc_out[2 * npt + i] = lc[2];
+    status[i] = 16;
+  }
+}
+
+// P2 interpolation (interp3d_tet.m:39-69): V is [nvar][nnod], out [nvar][npt]
+__global__ void k_interp_p2(SlmMesh m, const int *__restrict__ els, const double *__restrict__ lc, int npt,
+                            const double *__restrict__ V, int nvar, int monotonic, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npt) return;
+  const int e = els[i];
+  if (e < 0) {
+    for (int k = 0; k < nvar; ++k) out[(size_t)k * npt + i] = nan("");
+    return;
+  }
+  const double r = lc[i], s = lc[npt + i], t = lc[2 * npt + i], u = 1.0 - r - s - t;
+  const double N[10] = {r * (2 * r - 1), s * (2 * s - 1), t * (2 * t - 1), u * (2 * u - 1), 4 * r * s,
+                        4 * s * t, 4 * t * u, 4 * r * u, 4 * r * t, 4 * s * u};
+  int nod[10];
+  for (int n = 0; n < 10; ++n) nod[n] = m.el2nod[(size_t)n * m.nel + e];
+  for (int k = 0; k < nvar; ++k) {
+    const double *Vk = V + (size_t)k * m.nnod;
+    double v = 0.0, lo = 1e300, hi = -1e300;
+    for (int n = 0; n < 10; ++n) {
+      const double x = Vk[nod[n]];
+      v += N[n] * x;
+      lo = fmin(lo, x);
+      hi = fmax(hi, x);
+    }
+    if (monotonic) v = fmin(fmax(v, lo), hi);
+    out[(size_t)k * npt + i] = v;
+  }
+}
+
+// quasi-cubic: element P1 gradients of vertex values and distance weights, per element (original
+// ids); the nodal sums are gathered per colour of the Stokes colouring (atomic-free)
+__global__ void k_cubic_elgrad(SlmMesh m, const double *__restrict__ X, const double *__restrict__ B,
+                               int method_wght, double *__restrict__ gel, double *__restrict__ wel) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nel) return;
+  double x[4], y[4], z[4], b[4];
+  for (int i = 0; i < 4; ++i) {
+    const int v = m.el2nod[(size_t)i * m.nel + e];
+    x[i] = X[v]; y[i] = X[m.nnod + v]; z[i] = X[2 * m.nnod + v];
+    b[i] = B[v];
+  }
+  // gradient of the linear interpolant: solve [x_i - x_4] g = b_i - b_4
+  const double a00 = x[0] - x[3], a01 = y[0] - y[3], a02 = z[0] - z[3];
+  const double a10 = x[1] - x[3], a11 = y[1] - y[3], a12 = z[1] - z[3];
+  const double a20 = x[2] - x[3], a21 = y[2] - y[3], a22 = z[2] - z[3];
+  const double r0 = b[0] - b[3], r1 = b[1] - b[3], r2 = b[2] - b[3];
+  const double det = a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
+  const double id = 1.0 / det;
+  const double gx = id * ((a11 * a22 - a12 * a21) * r0 + (a02 * a21 - a01 * a22) * r1 + (a01 * a12 - a02 * a11) * r2);
+  const double gy = id * ((a12 * a20 - a10 * a22) * r0 + (a00 * a22 - a02 * a20) * r1 + (a02 * a10 - a00 * a12) * r2);
+  const double gz = id * ((a10 * a21 - a11 * a20) * r0 + (a01 * a20 - a00 * a21) * r1 + (a00 * a11 - a01 * a10) * r2);
+  gel[e] = gx; gel[m.nel + e] = gy; gel[2 * (size_t)m.nel + e] = gz;
+  const double cx = 0.25 * (x[0] + x[1] + x[2] + x[3]), cy = 0.25 * (y[0] + y[1] + y[2] + y[3]),
+               cz = 0.25 * (z[0] + z[1] + z[2] + z[3]);
+  for (int i = 0; i < 4; ++i) {
+    double w = 1.0;
+    if (method_wght) w = 1.0 / sqrt((x[i] - cx) * (x[i] - cx) + (y[i] - cy) * (y[i] - cy) + (z[i] - cz) * (z[i] - cz));
+    wel[(size_t)i * m.nel + e] = w;
+  }
+}
+// per colour of the Stokes level-0 colouring (stored order -> original ids via perm)
+__global__ void k_cubic_scatter(const int *__restrict__ perm, int nel, int eb, int ee, const int *__restrict__ el2nod_orig,
+                                const double *__restrict__ gel, const double *__restrict__ wel, double *__restrict__ gn,
+                                double *__restrict__ wn, int nvnod) {
+  const int p = eb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= ee) return;
+  const int e = perm[p];
+  for (int i = 0; i < 4; ++i) {
+    const int v = el2nod_orig[(size_t)i * nel + e];
+    const double w = wel[(size_t)i * nel + e];
+    gn[v] += w * gel[e];
+    gn[nvnod + v] += w * gel[nel + e];
+    gn[2 * (size_t)nvnod + v] += w * gel[2 * (size_t)nel + e];
+    wn[v] += w;
+  }
+}
+
+__global__ void k_cubic_interp(SlmMesh m, const double *__restrict__ X, const int *__restrict__ els,
+                               const double *__restrict__ lc, int npt, const double *__restrict__ B,
+                               const double *__restrict__ gn, const double *__restrict__ wn,
+                               const double *__restrict__ gel, int monotonic, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npt) return;
+  const int e = els[i];
+  if (e < 0) {
+    out[i] = nan("");
+    return;
+  }
+  const double r = lc[i], s = lc[npt + i], t = lc[2 * npt + i], u = 1.0 - r - s - t;
+  const double q2 = 1.4142135623730951;   // sqrt(2)
+  const double N[16] = {r, s, t, u, q2 * r * s, q2 * s * t, t * u, r * u, q2 * r * t, s * u,
+                        q2 * s * r * (s - r), q2 * s * t * (t - s), t * u * (u - t), r * u * (u - r),
+                        q2 * r * t * (t - r), s * u * (u - s)};
+  int v[4];
+  double x[4], y[4], z[4], b[4], dB[4][3];
+  for (int k = 0; k < 4; ++k) {
+    v[k] = m.el2nod[(size_t)k * m.nel + e];
+    x[k] = X[v[k]]; y[k] = X[m.nnod + v[k]]; z[k] = X[2 * m.nnod + v[k]];
+    b[k] = B[v[k]];
+    const double wk = wn[v[k]];
+    for (int c = 0; c < 3; ++c) dB[k][c] = gn[(size_t)c * m.nvnod + v[k]] / wk - gel[(size_t)c * m.nel + e];
+  }
+  double sr[4], ss[4], st[4];
+  for (int k = 0; k < 4; ++k) {
+    sr[k] = (x[0] - x[3]) * dB[k][0] + (y[0] - y[3]) * dB[k][1] + (z[0] - z[3]) * dB[k][2];
+    ss[k] = (x[1] - x[3]) * dB[k][0] + (y[1] - y[3]) * dB[k][1] + (z[1] - z[3]) * dB[k][2];
+    st[k] = (x[2] - x[3]) * dB[k][0] + (y[2] - y[3]) * dB[k][1] + (z[2] - z[3]) * dB[k][2];
+  }
+  const double h = 0.7071067811865476;    // sqrt(1/2)
+  const double q1n2 = h * sr[1] - h * ss[1], q1n1 = h * sr[0] - h * ss[0];
+  const double q2n3 = h * ss[2] - h * st[2], q2n2 = h * ss[1] - h * st[1];
+  const double q5n3 = h * sr[2] - h * st[2], q5n1 = h * sr[0] - h * st[0];
+  const double info[12] = {(q1n2 - q1n1) / 2, (q2n3 - q2n2) / 2, (st[3] - st[2]) / 2, (sr[3] - sr[0]) / 2,
+                           (q5n3 - q5n1) / 2, (ss[3] - ss[1]) / 2, (q1n2 + q1n1) / 2, (q2n3 + q2n2) / 2,
+                           (st[3] + st[2]) / 2, (sr[3] + sr[0]) / 2, (q5n3 + q5n1) / 2, (ss[3] + ss[1]) / 2};
+  double val = N[0] * b[0] + N[1] * b[1] + N[2] * b[2] + N[3] * b[3];
+  for (int k = 0; k < 12; ++k) val += N[4 + k] * info[k];
+  if (monotonic) {
+    const double lo = fmin(fmin(b[0], b[1]), fmin(b[2], b[3])), hi = fmax(fmax(b[0], b[1]), fmax(b[2], b[3]));
+    val = fmin(fmax(val, lo), hi);
+  }
+  out[i] = val;
+}
+
+// PC2 predictor (advect3d_slm_p_sph.m:298-410): U [3][nnod] Cartesian; writes P (3,npt)
+// (theta,phi,r), the unit perpendicular direction and the predicted unit radius vector.
+__global__ void k_predictor(const double *__restrict__ X, const double *__restrict__ S, int nnod,
+                            const double *__restrict__ U, double dt, double r_cmb, double r_surf,
+                            double *__restrict__ P, double *__restrict__ upu, double *__restrict__ rpu) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnod) return;
+  const double rr = S[2 * nnod + i];
+  const double x[3] = {X[i], X[nnod + i], X[2 * nnod + i]};
+  const double u[3] = {U[i], U[nnod + i], U[2 * nnod + i]};
+  double ru[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  const double nru2 = ru[0] * ru[0] + ru[1] * ru[1] + ru[2] * ru[2];
+  const double ud = u[0] * ru[0] + u[1] * ru[1] + u[2] * ru[2];
+  double upar[3], uperp[3];
+  for (int k = 0; k < 3; ++k) {
+    upar[k] = ud * ru[k] / nru2;
+    uperp[k] = u[k] - upar[k];
+  }
+  const double np = sqrt(uperp[0] * uperp[0] + uperp[1] * uperp[1] + uperp[2] * uperp[2]);
+  double e[3];
+  for (int k = 0; k < 3; ++k) e[k] = np > 0.0 ? uperp[k] / np : 0.0;
+  const double lpar = sqrt(upar[0] * upar[0] + upar[1] * upar[1] + upar[2] * upar[2]) * 0.5 * dt;
+  const double lperp = np * 0.5 * dt;
+  const double lprime = rr * tan(lperp / rr);
+  double rp[3];
+  for (int k = 0; k < 3; ++k) rp[k] = x[k] - e[k] * lprime;
+  const double nrp = sqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
+  const double rad = fabs(rr - lpar);
+  double th, ph, r;
+  c2s(rp[0] / nrp * rad, rp[1] / nrp * rad, rp[2] / nrp * rad, th, ph, r);
+  const double rtol = 1e-12 * (r_surf - r_cmb);
+  if (r <= r_cmb + rtol) r = r_cmb + rtol;
+  if (r >= r_surf - rtol) r = r_surf - rtol;
+  P[i] = th; P[nnod + i] = ph; P[2 * nnod + i] = r;
+  for (int k = 0; k < 3; ++k) {
+    upu[(size_t)k * nnod + i] = e[k];
+    rpu[(size_t)k * nnod + i] = rp[k] / nrp;
+  }
+}
+// PC2 corrector (advect3d_slm_p_sph.m:412-440): Ubt [3][nnod] velocity at predictor points
+__global__ void k_corrector(const double *__restrict__ X, const double *__restrict__ S, int nnod,
+                            const double *__restrict__ Ubt, const double *__restrict__ upu,
+                            const double *__restrict__ rpu, double dt, double r_cmb, double r_surf,
+                            double *__restrict__ P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnod) return;
+  const double rr = S[2 * nnod + i];
+  const double x[3] = {X[i], X[nnod + i], X[2 * nnod + i]};
+  const double u[3] = {Ubt[i], Ubt[nnod + i], Ubt[2 * nnod + i]};
+  const double q[3] = {rpu[i], rpu[nnod + i], rpu[2 * nnod + i]};
+  const double e[3] = {upu[i], upu[nnod + i], upu[2 * nnod + i]};
+  const double nq2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+  const double ud = u[0] * q[0] + u[1] * q[1] + u[2] * q[2];
+  double upar[3], uperp[3];
+  for (int k = 0; k < 3; ++k) {
+    upar[k] = ud * q[k] / nq2;
+    uperp[k] = u[k] - upar[k];
+  }
+  const double lpar = sqrt(upar[0] * upar[0] + upar[1] * upar[1] + upar[2] * upar[2]) * dt;
+  const double lperp = sqrt(uperp[0] * uperp[0] + uperp[1] * uperp[1] + uperp[2] * uperp[2]) * dt;
+  const double lprime = rr * tan(lperp / rr);
+  double rp[3];
+  for (int k = 0; k < 3; ++k) rp[k] = x[k] - e[k] * lprime;
+  const double nrp = sqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
+  const double rad = fabs(rr - lpar);
+  double th, ph, r;
+  c2s(rp[0] / nrp * rad, rp[1] / nrp * rad, rp[2] / nrp * rad, th, ph, r);
+  const double rtol = 1e-12 * (r_surf - r_cmb);
+  if (r <= r_cmb + rtol) r = r_cmb + rtol;
+  if (r >= r_surf - rtol) r = r_surf - rtol;
+  P[i] = th; P[nnod + i] = ph; P[2 * nnod + i] = r;
+}
+
+// ======================================================================================
+// host side
+// ======================================================================================
+struct SlmState {
+  bool built = false;
+  int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr;
+  uint8_t *cls = nullptr;
+  double *S0 = nullptr, *SZ = nullptr, *SX = nullptr;
+  // work
+  double *P = nullptr, *lc = nullptr, *V = nullptr, *out = nullptr, *upu = nullptr, *rpu = nullptr, *U = nullptr;
+  double *gel = nullptr, *wel = nullptr, *gn = nullptr, *wn = nullptr;
+  int *els = nullptr, *guess = nullptr, *todo = nullptr;
+  uint8_t *status = nullptr;
+  size_t cap = 0;
+  SlmMesh view{};
+};
+
+}  // namespace m3sph
+
+namespace m3sph {
+
+template <typename T>
+static int sl_alloc(T **p, size_t n) {
+  *p = nullptr;
+  M3_CUDA(cudaMalloc((void **)p, sizeof(T) * (n ? n : 1)));
+  return M3SPH_OK;
+}
+template <typename T>
+static int sl_upload(T **p, const T *h, size_t n, cudaStream_t s) {
+  int st = sl_alloc(p, n);
+  if (st) return st;
+  M3_CUDA(cudaMemcpyAsync(*p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+  return M3SPH_OK;
+}
+
+// face neighbours, vertex->element adjacency, per-frame node coordinates (set-up, host + upload)
+int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
+  SlmState *S = new SlmState();
+  M->slm = S;
+  M->slm_free = [](void *p) {
+    SlmState *S = reinterpret_cast<SlmState *>(p);
+    for (void *q : {(void *)S->el2nod, (void *)S->nbr, (void *)S->v2e_ptr, (void *)S->v2e, (void *)S->node_guess,
+                    (void *)S->cls, (void *)S->S0, (void *)S->SZ, (void *)S->SX, (void *)S->P, (void *)S->lc,
+                    (void *)S->V, (void *)S->out, (void *)S->upu, (void *)S->rpu, (void *)S->U, (void *)S->gel,
+                    (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->els, (void *)S->guess,
+                    (void *)S->todo, (void *)S->status})
+      if (q) cudaFree(q);
+    delete S;
+  };
+  cudaStream_t s = M->stream;
+  const int nel = f0.nel, nnod = f0.nnod, nv = f0.nvnod;
+  const std::vector<int> &el = M->lev[0].h_el2nod_orig;   // [nel][10]
+  std::vector<int> soa((size_t)nel * 10);
+  for (int e = 0; e < nel; ++e)
+    for (int n = 0; n < 10; ++n) soa[(size_t)n * nel + e] = el[(size_t)e * 10 + n];
+  // face neighbours: face k is opposite local vertex k
+  struct Face { uint64_t key; int c; int ek; };
+  std::vector<Face> faces((size_t)nel * 4);
+  for (int e = 0; e < nel; ++e)
+    for (int k = 0; k < 4; ++k) {
+      int v[3], j = 0;
+      for (int i = 0; i < 4; ++i)
+        if (i != k) v[j++] = el[(size_t)e * 10 + i];
+      std::sort(v, v + 3);
+      faces[(size_t)e * 4 + k] = {(uint64_t)v[0] * (uint64_t)nv + (uint64_t)v[1], v[2], e * 4 + k};
+    }
+  std::sort(faces.begin(), faces.end(), [](const Face &a, const Face &b) {
+    return a.key < b.key || (a.key == b.key && (a.c < b.c || (a.c == b.c && a.ek < b.ek)));
+  });
+  std::vector<int> nbr((size_t)nel * 4, -1);
+  for (size_t i = 0; i + 1 < faces.size(); ++i)
+    if (faces[i].key == faces[i + 1].key && faces[i].c == faces[i + 1].c) {
+      const int a = faces[i].ek, b = faces[i + 1].ek;
+      nbr[(size_t)(a % 4) * nel + a / 4] = b / 4;
+      nbr[(size_t)(b % 4) * nel + b / 4] = a / 4;
+      ++i;
+    }
+  // vertex -> elements
+  std::vector<int> ptr(nv + 1, 0), adj((size_t)nel * 4);
+  for (int e = 0; e < nel; ++e)
+    for (int i = 0; i < 4; ++i) ptr[el[(size_t)e * 10 + i] + 1]++;
+  for (int v = 0; v < nv; ++v) ptr[v + 1] += ptr[v];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int e = 0; e < nel; ++e)
+    for (int i = 0; i < 4; ++i) adj[fill[el[(size_t)e * 10 + i]]++] = e;
+  // first element listing each node (guess_elems, locate_points_interp_vars_3d_sph.m:203-207)
+  std::vector<int> first(nnod, -1);
+  for (size_t i = 0; i < (size_t)nel * 10; ++i)
+    if (first[el[i]] < 0) first[el[i]] = (int)(i / 10);
+  // frames
+  std::vector<double> S0(3 * (size_t)nv), SZ(3 * (size_t)nv), SX(3 * (size_t)nnod);
+  for (int n = 0; n < nnod; ++n) {
+    const double x = f0.GCOORD[3 * (size_t)n], y = f0.GCOORD[3 * (size_t)n + 1], z = f0.GCOORD[3 * (size_t)n + 2];
+    auto c2sh = [](double a, double b, double c, double *o) {
+      o[2] = std::sqrt(a * a + b * b + c * c);
+      o[0] = std::atan2(std::sqrt(a * a + b * b), c);
+      o[1] = std::atan2(b, a);
+      if (o[1] < 0) o[1] += 2 * M_PI;
+    };
+    double o[3];
+    c2sh(x, -z, y, o);
+    for (int k = 0; k < 3; ++k) SX[(size_t)k * nnod + n] = o[k];
+    if (n < nv) {
+      c2sh(-x, -y, z, o);
+      for (int k = 0; k < 3; ++k) {
+        SZ[(size_t)k * nv + n] = o[k];
+        S0[(size_t)k * nv + n] = f0.GCOORD_SPH[3 * (size_t)n + k];
+      }
+    }
+  }
+  std::vector<uint8_t> cls(f0.elclass, f0.elclass + nel);
+  int st;
+  if ((st = sl_upload(&S->el2nod, soa.data(), soa.size(), s)) || (st = sl_upload(&S->nbr, nbr.data(), nbr.size(), s)) ||
+      (st = sl_upload(&S->v2e_ptr, ptr.data(), ptr.size(), s)) || (st = sl_upload(&S->v2e, adj.data(), adj.size(), s)) ||
+      (st = sl_upload(&S->node_guess, first.data(), first.size(), s)) ||
+      (st = sl_upload(&S->cls, cls.data(), cls.size(), s)) || (st = sl_upload(&S->S0, S0.data(), S0.size(), s)) ||
+      (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)))
+    return st;
+  M3_CUDA(cudaStreamSynchronize(s));
+  S->view = SlmMesh{nel, nnod, nv, S->el2nod, S->nbr, S->cls, S->S0, S->SZ, S->SX, S->v2e_ptr, S->v2e};
+  S->built = true;
+  return M3SPH_OK;
+}
+
+static int slm_reserve(SlmState *S, size_t npt, int nel, int nnod, int nv) {
+  if (npt <= S->cap && S->P) return M3SPH_OK;
+  for (void *q : {(void *)S->P, (void *)S->lc, (void *)S->V, (void *)S->out, (void *)S->upu, (void *)S->rpu,
+                  (void *)S->U, (void *)S->els, (void *)S->guess, (void *)S->todo, (void *)S->status})
+    if (q) cudaFree(q);
+  const size_t n = std::max(npt, (size_t)nnod);
+  int st;
+  if ((st = sl_alloc(&S->P, 3 * n)) || (st = sl_alloc(&S->lc, 3 * n)) || (st = sl_alloc(&S->V, 3 * (size_t)nnod)) ||
+      (st = sl_alloc(&S->out, 3 * n)) || (st = sl_alloc(&S->upu, 3 * (size_t)nnod)) ||
+      (st = sl_alloc(&S->rpu, 3 * (size_t)nnod)) || (st = sl_alloc(&S->U, 3 * (size_t)nnod)) ||
+      (st = sl_alloc(&S->els, n)) || (st = sl_alloc(&S->guess, n)) || (st = sl_alloc(&S->todo, n)) ||
+      (st = sl_alloc(&S->status, n)))
+    return st;
+  if (!S->gel) {
+    if ((st = sl_alloc(&S->gel, 3 * (size_t)nel)) || (st = sl_alloc(&S->wel, 4 * (size_t)nel)) ||
+        (st = sl_alloc(&S->gn, 3 * (size_t)nv)) || (st = sl_alloc(&S->wn, (size_t)nv)))
+      return st;
+  }
+  S->cap = n;
+  return M3SPH_OK;
+}
+
+// locate S->P (npt points) with optional guesses (S->guess valid if use_guess), writing S->els,
+// S->lc, S->status; unplaced points get a brute-force pass. Returns counts in info.
+static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool node_guess, bool adjust,
+                      m3sph_locate_info *info) {
+  cudaStream_t s = M->stream;
+  k_locate<<<(npt + 127) / 128, 128, 0, s>>>(S->view, S->P, npt, use_guess ? S->guess : nullptr,
+                                              node_guess ? S->node_guess : nullptr, S->els, S->lc, S->status,
+                                              adjust ? 1 : 0); count_launch();
+  M3_CUDA(cudaGetLastError());
+  std::vector<uint8_t> hs(npt);
+  M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> todo;
+  int nwalk = 0, ntie = 0, ngap = 0;
+  for (int i = 0; i < npt; ++i) {
+    if (hs[i] & 1) nwalk++;
+    if (hs[i] & 2) ntie++;
+    if (hs[i] & 4) ngap++;
+    if (hs[i] & 8) todo.push_back(i);
+  }
+  int nbrute = 0, nlost = 0;
+  if (!todo.empty()) {
+    M3_CUDA(cudaMemcpyAsync(S->todo, todo.data(), sizeof(int) * todo.size(), cudaMemcpyHostToDevice, s));
+    const int nt = (int)todo.size();
+    k_locate_brute<<<(nt * 32 + 255) / 256, 256, 0, s>>>(S->view, S->P, npt, S->todo, nt, S->els, S->lc, S->status); count_launch();
+    M3_CUDA(cudaGetLastError());
+    M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
+    M3_CUDA(cudaStreamSynchronize(s));
+    for (int i : todo) {
+      if (hs[i] & 16) nbrute++;
+      else nlost++;
+    }
+  }
+  if (info) {
+    info->npt = npt;
+    info->nwalk = nwalk;
+    info->nties = ntie;
+    info->ngap = ngap;
+    info->nbrute = nbrute;
+    info->nlost = nlost;
+  }
+  if (nlost) {
+    set_error("some nodes have not been located");
+    return M3SPH_ERR_POINT_NOT_FOUND;
+  }
+  return M3SPH_OK;
+}
+
+static int slm_cubic_gradients(m3sph_mesh *M, SlmState *S, const double *B, int method_wght) {
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  const int nel = L0.nel, nv = L0.nvnod;
+  k_cubic_elgrad<<<(nel + 127) / 128, 128, 0, s>>>(S->view, M->fin.gcoord, B, method_wght, S->gel, S->wel); count_launch();
+  M3_CUDA(cudaMemsetAsync(S->gn, 0, sizeof(double) * 3 * nv, s));
+  M3_CUDA(cudaMemsetAsync(S->wn, 0, sizeof(double) * nv, s));
+  for (size_t c = 0; c + 1 < L0.cstart.size(); ++c) {
+    const int b = L0.cstart[c], e = L0.cstart[c + 1];
+    if (e > b) k_cubic_scatter<<<(e - b + 127) / 128, 128, 0, s>>>(L0.perm, nel, b, e, S->el2nod, S->gel, S->wel,
+                                                                   S->gn, S->wn, nv); count_launch();
+  }
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+static SlmState *slm_state(m3sph_mesh *M) { return reinterpret_cast<SlmState *>(M->slm); }
+
+}  // namespace m3sph
+
+using namespace m3sph;
+
+static int slm_check(m3sph_mesh *M) {
+  if (!M || !M->slm) {
+    set_error("mesh handle without advection data");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_tsearch_sph(m3sph_mesh *M, const double *thphr, int32_t npt, const int32_t *els_guess,
+                                 int32_t *els_out, double *lc_out, m3sph_locate_info *info) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (npt < 0 || (npt > 0 && (!thphr || !els_out))) {
+    set_error("m3sph_tsearch_sph: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (npt == 0) return M3SPH_OK;
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
+  cudaStream_t s = M->stream;
+  std::vector<double> P(3 * (size_t)npt);
+  for (int i = 0; i < npt; ++i)
+    for (int k = 0; k < 3; ++k) P[(size_t)k * npt + i] = thphr[3 * (size_t)i + k];
+  M3_CUDA(cudaMemcpyAsync(S->P, P.data(), sizeof(double) * P.size(), cudaMemcpyHostToDevice, s));
+  if (els_guess) {
+    std::vector<int> g(npt);
+    for (int i = 0; i < npt; ++i) g[i] = els_guess[i] - 1;
+    M3_CUDA(cudaMemcpyAsync(S->guess, g.data(), sizeof(int) * npt, cudaMemcpyHostToDevice, s));
+  }
+  st = slm_locate(M, S, npt, els_guess != nullptr, npt == L0.nnod, false, info);
+  if (st && st != M3SPH_ERR_POINT_NOT_FOUND) return st;
+  std::vector<int> e(npt);
+  std::vector<double> lc(3 * (size_t)npt);
+  M3_CUDA(cudaMemcpyAsync(e.data(), S->els, sizeof(int) * npt, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaMemcpyAsync(lc.data(), S->lc, sizeof(double) * lc.size(), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < npt; ++i) {
+    els_out[i] = e[i] + 1;
+    if (lc_out)
+      for (int k = 0; k < 3; ++k) lc_out[3 * (size_t)i + k] = lc[(size_t)k * npt + i];
+  }
+  return st;
+}
+
+extern "C" int m3sph_interp3d_tet(m3sph_mesh *M, const int32_t *els, const double *lc, int32_t npt, const double *V,
+                                  int32_t nvar, int32_t monotonic, double *Vi) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (npt <= 0 || nvar < 1 || nvar > 3 || !els || !lc || !V || !Vi) {
+    set_error("m3sph_interp3d_tet: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
+  cudaStream_t s = M->stream;
+  std::vector<int> e(npt);
+  std::vector<double> l(3 * (size_t)npt), v((size_t)nvar * L0.nnod);
+  for (int i = 0; i < npt; ++i) {
+    e[i] = els[i] - 1;
+    for (int k = 0; k < 3; ++k) l[(size_t)k * npt + i] = lc[3 * (size_t)i + k];
+  }
+  for (int n = 0; n < L0.nnod; ++n)
+    for (int k = 0; k < nvar; ++k) v[(size_t)k * L0.nnod + n] = V[(size_t)n * nvar + k];
+  M3_CUDA(cudaMemcpyAsync(S->els, e.data(), sizeof(int) * npt, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->lc, l.data(), sizeof(double) * l.size(), cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->V, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, s));
+  k_interp_p2<<<(npt + 127) / 128, 128, 0, s>>>(S->view, S->els, S->lc, npt, S->V, nvar, monotonic, S->out); count_launch();
+  M3_CUDA(cudaGetLastError());
+  std::vector<double> o((size_t)nvar * npt);
+  M3_CUDA(cudaMemcpyAsync(o.data(), S->out, sizeof(double) * o.size(), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < npt; ++i)
+    for (int k = 0; k < nvar; ++k) Vi[(size_t)i * nvar + k] = o[(size_t)k * npt + i];
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_interp3d_cubic(m3sph_mesh *M, const int32_t *els, const double *lc, int32_t npt, const double *V,
+                                    int32_t monotonic, int32_t method_wght, double *Vi) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (npt <= 0 || !els || !lc || !V || !Vi) {
+    set_error("m3sph_interp3d_cubic: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
+  cudaStream_t s = M->stream;
+  std::vector<int> e(npt);
+  std::vector<double> l(3 * (size_t)npt);
+  for (int i = 0; i < npt; ++i) {
+    e[i] = els[i] - 1;
+    for (int k = 0; k < 3; ++k) l[(size_t)k * npt + i] = lc[3 * (size_t)i + k];
+  }
+  M3_CUDA(cudaMemcpyAsync(S->els, e.data(), sizeof(int) * npt, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->lc, l.data(), sizeof(double) * l.size(), cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->V, V, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
+  if ((st = slm_cubic_gradients(M, S, S->V, method_wght))) return st;
+  k_cubic_interp<<<(npt + 127) / 128, 128, 0, s>>>(S->view, M->fin.gcoord, S->els, S->lc, npt, S->V, S->gn, S->wn,
+                                                    S->gel, monotonic, S->out); count_launch();
+  M3_CUDA(cudaGetLastError());
+  M3_CUDA(cudaMemcpyAsync(Vi, S->out, sizeof(double) * npt, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+// advect3d_slm_p_sph with PC2 backtracking: T (nnod) updated in place; els_BT / els_INTERP
+// (nnod, 1-based, 0 = none) are the WS_SLM guesses, updated on return.
+static int advect_device(m3sph_mesh *M, double dt, const m3sph_slm_opts *o, bool use_ws, m3sph_locate_info *info) {
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  const int n = L0.nnod;
+  k_predictor<<<(n + 127) / 128, 128, 0, s>>>(M->fin.gcoord, M->fin.gcoord_sph, n, S->U, dt, o->r_cmb, o->r_surf,
+                                               S->P, S->upu, S->rpu); count_launch();
+  M3_CUDA(cudaGetLastError());
+  m3sph_locate_info i1{}, i2{};
+  M3_TRY(slm_locate(M, S, n, use_ws, true, true, &i1));
+  // guesses for the next step's predictor search (els_BT) are this step's predictor elements
+  k_interp_p2<<<(n + 127) / 128, 128, 0, s>>>(S->view, S->els, S->lc, n, S->U, 3, 0, S->out); count_launch();
+  M3_CUDA(cudaMemcpyAsync(S->guess, S->els, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  k_corrector<<<(n + 127) / 128, 128, 0, s>>>(M->fin.gcoord, M->fin.gcoord_sph, n, S->out, S->upu, S->rpu, dt,
+                                               o->r_cmb, o->r_surf, S->P); count_launch();
+  M3_CUDA(cudaGetLastError());
+  M3_TRY(slm_locate(M, S, n, true, true, true, &i2));
+  if (o->method_interp == 1) {
+    M3_TRY(slm_cubic_gradients(M, S, S->V, o->method_wght));
+    k_cubic_interp<<<(n + 127) / 128, 128, 0, s>>>(S->view, M->fin.gcoord, S->els, S->lc, n, S->V, S->gn, S->wn,
+                                                    S->gel, o->monotonic, S->out); count_launch();
+  } else {
+    k_interp_p2<<<(n + 127) / 128, 128, 0, s>>>(S->view, S->els, S->lc, n, S->V, 1, o->monotonic, S->out); count_launch();
+  }
+  M3_CUDA(cudaGetLastError());
+  if (info) {
+    info->npt = i1.npt + i2.npt;
+    info->nwalk = i1.nwalk + i2.nwalk;
+    info->nties = i1.nties + i2.nties;
+    info->ngap = i1.ngap + i2.ngap;
+    info->nbrute = i1.nbrute + i2.nbrute;
+    info->nlost = i1.nlost + i2.nlost;
+  }
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_advect_slm(m3sph_mesh *M, const double *Ux, const double *Uy, const double *Uz, double *T,
+                                double dt, const m3sph_slm_opts *o, int32_t *els_BT, int32_t *els_INTERP,
+                                m3sph_locate_info *info) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (!Ux || !Uy || !Uz || !T || !o) {
+    set_error("m3sph_advect_slm: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (o->method_BT != 1) {
+    set_error("m3sph_advect_slm: only PC2 backtracking (method_BT = 1) is implemented");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  const int n = L0.nnod;
+  if ((st = slm_reserve(S, n, L0.nel, n, L0.nvnod))) return st;
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(S->U, Ux, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->U + n, Uy, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->U + 2 * (size_t)n, Uz, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->V, T, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  bool use_ws = false;
+  if (els_BT) {
+    std::vector<int> g(n);
+    bool any = false;
+    for (int i = 0; i < n; ++i) {
+      g[i] = (int)els_BT[i] - 1;
+      any |= g[i] >= 0;
+    }
+    if (any) {
+      use_ws = true;
+      M3_CUDA(cudaMemcpyAsync(S->guess, g.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    }
+  }
+  M3_TRY(advect_device(M, dt, o, use_ws, info));
+  std::vector<int> e(n);
+  M3_CUDA(cudaMemcpyAsync(T, S->out, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaMemcpyAsync(e.data(), S->els, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  std::vector<int> g(n);
+  M3_CUDA(cudaMemcpyAsync(g.data(), S->guess, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  // WS_SLM: els_BT = predictor elements (still in `guess`), els_INTERP = departure elements
+  for (int i = 0; i < n; ++i) {
+    if (els_BT) els_BT[i] = g[i] + 1;
+    if (els_INTERP) els_INTERP[i] = e[i] + 1;
+  }
+  return M3SPH_OK;
+}

@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -47,18 +48,16 @@ template <typename T> int dense_inverse(const Level &L, const T *K, T *A, T *wor
 template <typename T> int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s);
 size_t element_setup_smem();
 
-// ---- errors ----
+// ---- errors and counters ----
 static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static void add_launches(unsigned long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 void set_error(const std::string &msg) { g_err = msg; }
 int cuda_fail(cudaError_t e, const char *what) {
   g_err = std::string("CUDA error ") + cudaGetErrorString(e) + " in " + what;
   return M3SPH_ERR_CUDA;
 }
-#define M3_TRY(call)                 \
-  do {                               \
-    int _s = (call);                 \
-    if (_s != M3SPH_OK) return _s;   \
-  } while (0)
 
 // ---- quadrature and shape functions (host) ----
 void build_shape_tables(ShapeTables &t) {
@@ -340,6 +339,8 @@ static int build_transfer(m3sph_mesh *M, Level &F, Level &C, const uint8_t *ispl
   return M3SPH_OK;
 }
 
+static void clear_graphs(m3sph_mesh *M);
+
 static void free_level(Level &L) {
   for (void *p : {(void *)L.el2nod, (void *)L.perm, (void *)L.invperm, (void *)L.freemask, (void *)L.K64,
                   (void *)L.K32, (void *)L.Dinv64, (void *)L.Dinv32, (void *)L.child, (void *)L.child_vloc,
@@ -356,7 +357,7 @@ extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
   Finest &f = M->fin;
   for (void *p : {(void *)f.gcoord, (void *)f.gcoord_sph, (void *)f.RR, (void *)f.cls, (void *)f.iso_slot,
                   (void *)f.cubic, (void *)f.visc, (void *)f.dens, (void *)f.G64, (void *)f.M64, (void *)f.Fbe,
-                  (void *)f.Fb, (void *)f.LiMM, (void *)f.err})
+                  (void *)f.BCe, (void *)f.Fb, (void *)f.LiMM, (void *)f.err})
     dfree(p);
   dfree(M->coarse.A64);
   dfree(M->coarse.A32);
@@ -366,7 +367,9 @@ extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
   dfree(M->scal);
   for (void *p : M->work) dfree(p);
   if (M->h_scal) cudaFreeHost(M->h_scal);
+  clear_graphs(M);
   if (M->wk && M->wk_free) M->wk_free(M->wk);
+  if (M->slm && M->slm_free) M->slm_free(M->slm);
   if (M->stream) cudaStreamDestroy(M->stream);
   delete M;
   return M3SPH_OK;
@@ -470,6 +473,7 @@ extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t
       (st = upload(&F.cubic, cub.data(), cub.size(), s)) || (st = dalloc(&F.visc, nnod)) ||
       (st = dalloc(&F.dens, nnod)) || (st = dalloc(&F.G64, 120 * (size_t)nel)) ||
       (st = dalloc(&F.M64, 10 * (size_t)nel)) || (st = dalloc(&F.Fbe, 30 * (size_t)nel)) ||
+      (st = dalloc(&F.BCe, 30 * (size_t)nel)) ||
       (st = dalloc(&F.Fb, L0.ndof)) || (st = dalloc(&F.LiMM, L0.nvnod)) || (st = dalloc(&F.err, 4)) ||
       (st = dalloc(&L0.K64, (size_t)NPACK * nel)) || (st = dalloc(&L0.K32, (size_t)NPACK * nel)) ||
       (st = dalloc(&M->Ufix, L0.ndof)) || (st = dalloc(&M->bc_rhs, L0.ndof)) || (st = dalloc(&M->red, 4096)) ||
@@ -477,6 +481,8 @@ extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t
     return fail(st);
   if (cudaMallocHost((void **)&M->h_scal, 64 * sizeof(double)) != cudaSuccess) return fail(M3SPH_ERR_CUDA);
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "mesh upload"));
+  st = slm_build(M, f0);
+  if (st) return fail(st);
   *out = M;
   return M3SPH_OK;
 }
@@ -505,7 +511,6 @@ struct Work {
 };
 }  // namespace
 
-static std::mutex g_work_mu;
 
 static Work *get_work(m3sph_mesh *M) { return reinterpret_cast<Work *>(M->wk); }
 
@@ -559,35 +564,6 @@ __global__ void k_recip(const double *a, double *b, int n) {
   if (i < n) b[i] = 1.0 / a[i];
 }
 
-// bc_rhs = K_full Ufix where K_full is the rotated (unmasked) operator: only columns of fixed
-// dofs matter, so apply the element operator with masks lifted on a vector that is zero on free
-// dofs. The stored K has fixed rows/cols zeroed, hence a dedicated pass on unmasked matrices.
-static int compute_bc_rhs(m3sph_mesh *M, const SetupArgs &base, Work *W) {
-  Level &L0 = M->lev[0];
-  cudaStream_t s = M->stream;
-  // temporary unmasked element matrices
-  double *Ku = nullptr;
-  float *Ku32 = nullptr;
-  double *Gt = nullptr, *Mt = nullptr, *Ft = nullptr;
-  uint8_t *ones = nullptr;
-  M3_TRY(dalloc(&Ku, (size_t)NPACK * L0.nel));
-  M3_TRY(dalloc(&Ku32, (size_t)NPACK * L0.nel));
-  M3_TRY(dalloc(&Gt, 120 * (size_t)L0.nel));
-  M3_TRY(dalloc(&Mt, 10 * (size_t)L0.nel));
-  M3_TRY(dalloc(&Ft, 30 * (size_t)L0.nel));
-  M3_TRY(dalloc(&ones, L0.ndof));
-  M3_CUDA(cudaMemsetAsync(ones, 1, L0.ndof, s));
-  SetupArgs a = base;
-  a.freemask = ones;
-  a.K64 = Ku; a.K32 = Ku32; a.G64 = Gt; a.M64 = Mt; a.Fbe = Ft;
-  M3_TRY(launch_element_setup(a, s));
-  M3_TRY(ebe_apply<double>(L0, Ku, M->Ufix, M->bc_rhs, s));
-  M3_CUDA(cudaStreamSynchronize(s));
-  for (void *p : {(void *)Ku, (void *)Ku32, (void *)Gt, (void *)Mt, (void *)Ft, (void *)ones}) dfree(p);
-  (void)W;
-  return M3SPH_OK;
-}
-
 // element operator, force vector, Galerkin hierarchy and coarse inverse from the device-resident
 // viscosity, density and boundary conditions (assembly_stokes_sph_3d_double_jacobian +
 // restrict_stiffmat + cholesky_factorization of the reference)
@@ -602,6 +578,12 @@ static int rebuild_operator(m3sph_mesh *M) {
   a.RR = M->fin.RR; a.visc = M->fin.visc; a.dens = M->fin.dens; a.freemask = L0.freemask;
   a.g = M->phys.g; a.Bscale = M->phys.Bscale; a.Dens0 = M->phys.Dens0; a.minVisc = M->phys.minVisc; a.maxVisc = M->phys.maxVisc;
   a.K64 = L0.K64; a.K32 = L0.K32; a.G64 = M->fin.G64; a.M64 = M->fin.M64; a.Fbe = M->fin.Fbe; a.err = M->fin.err;
+  a.ufix = nullptr;
+  a.BCe = nullptr;
+  if (M->has_nonzero_fix) {
+    a.ufix = M->Ufix;
+    a.BCe = M->fin.BCe;
+  }
   M3_TRY(launch_element_setup(a, s));
   int herr[4];
   M3_CUDA(cudaMemcpyAsync(herr, M->fin.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
@@ -621,9 +603,9 @@ static int rebuild_operator(m3sph_mesh *M) {
   // assembled force vector, lumped pressure mass, boundary-condition rhs
   M3_TRY(scatter_elvec(L0, M->fin.Fbe, 30, 3, M->fin.Fb, L0.ndof, s));
   M3_TRY(mass_apply(L0, M->fin.M64, nullptr, W->pt, s));
-  k_recip<<<(L0.nvnod + 255) / 256, 256, 0, s>>>(W->pt, M->fin.LiMM, L0.nvnod);
-  if (!M->h_ifix.empty()) {
-    M3_TRY(compute_bc_rhs(M, a, W));
+  k_recip<<<(L0.nvnod + 255) / 256, 256, 0, s>>>(W->pt, M->fin.LiMM, L0.nvnod); count_launch();
+  if (M->has_nonzero_fix) {
+    M3_TRY(scatter_elvec(L0, M->fin.BCe, 30, 3, M->bc_rhs, L0.ndof, s));
   } else {
     M3_CUDA(cudaMemsetAsync(M->bc_rhs, 0, sizeof(double) * L0.ndof, s));
   }
@@ -672,6 +654,7 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   auto t0 = std::chrono::steady_clock::now();
   Level &L0 = M->lev[0];
   M->precision = precision ? 1 : 0;
+  clear_graphs(M);
   M3_TRY(alloc_work(M));
   Work *W = get_work(M);
   // masks
@@ -685,6 +668,8 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   }
   M->h_ifix = fx;
   M->h_vfix.assign(vfix, vfix + nfix);
+  M->has_nonzero_fix = false;
+  for (int i = 0; i < nfix; ++i) M->has_nonzero_fix |= vfix[i] != 0.0;
   int *d_fix = nullptr;
   double *d_vals = nullptr;
   M3_TRY(upload(&d_fix, fx.data(), std::max<size_t>(1, fx.size()), s));
@@ -692,10 +677,10 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   for (int i = 0; i < M->nmg; ++i) {
     Level &L = M->lev[i];
     M3_CUDA(cudaMemsetAsync(L.freemask, 1, L.ndof, s));
-    if (nfix) k_set_masks<<<(nfix + 255) / 256, 256, 0, s>>>(L.freemask, d_fix, nfix, L.ndof);
+    if (nfix) k_set_masks<<<(nfix + 255) / 256, 256, 0, s>>>(L.freemask, d_fix, nfix, L.ndof); count_launch();
   }
   M3_CUDA(cudaMemsetAsync(M->Ufix, 0, sizeof(double) * L0.ndof, s));
-  if (nfix) k_scatter_vals<<<(nfix + 255) / 256, 256, 0, s>>>(M->Ufix, d_fix, d_vals, nfix);
+  if (nfix) k_scatter_vals<<<(nfix + 255) / 256, 256, 0, s>>>(M->Ufix, d_fix, d_vals, nfix); count_launch();
   M3_CUDA(cudaMemcpyAsync(M->fin.visc, Visc, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
   M3_CUDA(cudaMemcpyAsync(M->fin.dens, Dens, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
   int nfree = 0;
@@ -811,6 +796,65 @@ static int read_scal(m3sph_mesh *M, int idx, double &v) {
   return M3SPH_OK;
 }
 
+__global__ void k_set_scal(double *scal, int idx, double v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) scal[idx] = v;
+}
+static int set_first_flag(m3sph_mesh *M, double v) {
+  k_set_scal<<<1, 1, 0, M->stream>>>(M->scal, 6, v); count_launch();
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+// one flexible-PCG iteration on device-resident data (no host synchronisation): V-cycle,
+// Polak-Ribiere direction, K q, step and residual norm into scal[3]
+static int cg_iteration(m3sph_mesh *M, double *x) {
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  const size_t n = L0.ndof;
+  M3_TRY(vcycle(M, W->r, W->d));
+  M3_TRY(dot2(W->r, W->Kq, W->d, n, M->red, M->scal + 0, s));   // scal[0]=r.d, scal[1]=Kq_prev.d
+  M3_TRY(cg_dir(W->d, W->q, n, M->scal, -1, s));                // first-iteration flag in scal[6]
+  M3_TRY(ebe_apply<double>(L0, L0.K64, W->q, W->Kq, s));
+  M3_TRY(dot(W->q, W->Kq, n, M->red, M->scal + 2, s));
+  M3_TRY(cg_update(x, W->r, W->q, W->Kq, n, M->scal, M->red, s));
+  M3_TRY(set_first_flag(M, 0.0));
+  return M3SPH_OK;
+}
+
+// the iteration captured once per solution-vector pointer as a CUDA graph and replayed
+static int iteration_graph(m3sph_mesh *M, double *x, cudaGraphExec_t *out) {
+  for (auto &g : M->graphs)
+    if (g.first == x) {
+      *out = g.second;
+      return M3SPH_OK;
+    }
+  cudaStream_t s = M->stream;
+  cudaGraph_t graph;
+  const unsigned long long n0 = g_launches.load();
+  M3_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  const int st = cg_iteration(M, x);
+  // kernels in the graph are counted at each replay, not at capture
+  const unsigned long long nk = g_launches.load() - n0;
+  g_launches.fetch_sub(nk);
+  M->graph_kernels = nk;
+  cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (st) return st;
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+  cudaGraphExec_t exec;
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+  M->graphs.push_back({x, exec});
+  *out = exec;
+  return M3SPH_OK;
+}
+
+static void clear_graphs(m3sph_mesh *M) {
+  for (auto &g : M->graphs) cudaGraphExecDestroy(g.second);
+  M->graphs.clear();
+}
+
 // b masked to free dofs on entry; x holds the initial guess (fixed entries are left unchanged)
 static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs_tol, int itmax, CGStats &st) {
   Work *W = get_work(M);
@@ -831,14 +875,17 @@ static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs
   if (!abs_tol) tol = tol * rrms;
   st.it = 0;
   int it = 0;
+  M3_TRY(set_first_flag(M, 1.0));
+  cudaGraphExec_t exec = nullptr;
+  if (M->use_graphs) M3_TRY(iteration_graph(M, x, &exec));
   for (it = 1; it <= itmax; ++it) {
-    M3_TRY(vcycle(M, W->r, W->d));
+    if (exec) {
+      M3_CUDA(cudaGraphLaunch(exec, s));
+      add_launches(M->graph_kernels);
+    } else {
+      M3_TRY(cg_iteration(M, x));
+    }
     st.nvc++;
-    M3_TRY(dot2(W->r, W->Kq, W->d, n, M->red, M->scal + 0, s));   // scal[0]=r.d, scal[1]=Kq_prev.d
-    M3_TRY(cg_dir(W->d, W->q, n, M->scal, it == 1, s));
-    M3_TRY(ebe_apply<double>(L0, L0.K64, W->q, W->Kq, s));
-    M3_TRY(dot(W->q, W->Kq, n, M->red, M->scal + 2, s));
-    M3_TRY(cg_update(x, W->r, W->q, W->Kq, n, M->scal, M->red, s));
     M3_TRY(read_scal(M, 3, rr));
     rrms = std::sqrt(rr) / sq;
     if (std::isnan(rrms)) {
@@ -894,7 +941,7 @@ static int remove_mean(m3sph_mesh *M, double *a) {
   M3_TRY(vsum(a, np, M->red, M->scal + 9, M->stream));
   double sm;
   M3_TRY(read_scal(M, 9, sm));
-  k_shift<<<(np + 255) / 256, 256, 0, M->stream>>>(a, -sm / np, np);
+  k_shift<<<(np + 255) / 256, 256, 0, M->stream>>>(a, -sm / np, np); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -918,7 +965,7 @@ static int coupled_residual(m3sph_mesh *M, const double *U, const double *P, dou
   const int np = L0.nvnod;
   // f = mask(Fb - bc_rhs)
   M3_CUDA(cudaMemsetAsync(W->tmp, 0, sizeof(double) * n, s));
-  k_rhs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M->fin.Fb, W->tmp, M->bc_rhs, L0.freemask, W->Rhs, n);
+  k_rhs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M->fin.Fb, W->tmp, M->bc_rhs, L0.freemask, W->Rhs, n); count_launch();
   double ff;
   M3_TRY(dot(W->Rhs, W->Rhs, n, M->red, M->scal + 10, s));
   M3_TRY(read_scal(M, 10, ff));
@@ -942,9 +989,9 @@ static int coupled_residual(m3sph_mesh *M, const double *U, const double *P, dou
 static int precondition_P(m3sph_mesh *M, const double *r, double *d) {
   Work *W = get_work(M);
   const int np = M->lev[0].nvnod;
-  k_precond_p1<<<(np + 255) / 256, 256, 0, M->stream>>>(r, M->fin.LiMM, d, np);
+  k_precond_p1<<<(np + 255) / 256, 256, 0, M->stream>>>(r, M->fin.LiMM, d, np); count_launch();
   M3_TRY(mass_apply(M->lev[0], M->fin.M64, d, W->pSq, M->stream));   // pSq used as temp (Md)
-  k_precond_p2<<<(np + 255) / 256, 256, 0, M->stream>>>(r, W->pSq, M->fin.LiMM, d, np);
+  k_precond_p2<<<(np + 255) / 256, 256, 0, M->stream>>>(r, W->pSq, M->fin.LiMM, d, np); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
@@ -973,7 +1020,7 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   inf.nitU += cs.it;
   // initial pressure residual r = -G'U
   M3_TRY(div_apply(L0, M->fin.G64, U, r, s));
-  k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np);
+  k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np); count_launch();
   M3_TRY(remove_mean(M, r));
   double rr;
   M3_TRY(pdot(M, r, r, rr));
@@ -1045,7 +1092,7 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
       M3_TRY(mgpcg(M, W->Rhs, U, tol_U_restart, true, itmax_U, cs));
       inf.nitU += cs.it;
       M3_TRY(div_apply(L0, M->fin.G64, U, r, s));
-      k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np);
+      k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np); count_launch();
       double rt;
       M3_TRY(pdot(M, r, r, rt));
       const double norm_rP_true = std::sqrt(rt) / sqp;
@@ -1118,7 +1165,7 @@ extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const
   }
   M3_CUDA(cudaEventRecord(e1, s));
   // back-rotation U_xyz = RR U
-  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, W->tmp);
+  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, W->tmp); count_launch();
   M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaMemcpyAsync(P, W->pP, sizeof(double) * L0.nvnod, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
@@ -1173,7 +1220,7 @@ extern "C" int m3sph_solution(m3sph_mesh *M, double *U_xyz, double *P) {
   Work *W = get_work(M);
   cudaStream_t s = M->stream;
   Level &L0 = M->lev[0];
-  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, W->tmp);
+  k_rotate_back<<<(L0.nnod + 255) / 256, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, W->tmp); count_launch();
   if (U_xyz) M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
   if (P) M3_CUDA(cudaMemcpyAsync(P, W->pP, sizeof(double) * L0.nvnod, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
@@ -1356,5 +1403,49 @@ extern "C" int m3sph_mgpcg(m3sph_mesh *M, const double *b, double *x, double tol
   M3_CUDA(cudaStreamSynchronize(s));
   if (itCG) *itCG = cs.it;
   if (rrms_final) *rrms_final = cs.rrms;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_launch_count(unsigned long long *count) {
+  if (!count) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  *count = g_launches.load();
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_apply_timing(m3sph_mesh *M, int32_t img, int32_t precision, int32_t nrep, double *ms_per_apply) {
+  M3_TRY(need_op(M));
+  if (img < 0 || img >= M->nmg || nrep < 1 || !ms_per_apply) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Level &L = M->lev[img];
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  const bool f32 = precision != 0;
+  if ((f32 && !L.K32) || (!f32 && !L.K64)) {
+    set_error("no element matrices of that precision on this level");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  cudaEvent_t e0, e1;
+  M3_CUDA(cudaEventCreate(&e0));
+  M3_CUDA(cudaEventCreate(&e1));
+  // warm-up
+  if (f32) M3_TRY(ebe_apply<float>(L, L.K32, W->r32[img], W->kd32[img], s));
+  else M3_TRY(ebe_apply<double>(L, L.K64, W->r64[img], W->kd64[img], s));
+  M3_CUDA(cudaEventRecord(e0, s));
+  for (int i = 0; i < nrep; ++i) {
+    if (f32) M3_TRY(ebe_apply<float>(L, L.K32, W->r32[img], W->kd32[img], s));
+    else M3_TRY(ebe_apply<double>(L, L.K64, W->r64[img], W->kd64[img], s));
+  }
+  M3_CUDA(cudaEventRecord(e1, s));
+  M3_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  M3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  *ms_per_apply = ms / nrep;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   return M3SPH_OK;
 }

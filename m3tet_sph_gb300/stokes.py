@@ -171,6 +171,11 @@ class DeviceMesh:
         L.check(L.lib().m3sph_solution(self.h, L.dptr(U), L.dptr(P)))
         return U, P
 
+    def apply_timing(self, img=0, precision=1, nrep=10):
+        ms = C.c_double()
+        L.check(L.lib().m3sph_apply_timing(self.h, img, precision, nrep, C.byref(ms)))
+        return ms.value
+
     def stream(self):
         p = C.c_void_p()
         L.check(L.lib().m3sph_stream(self.h, C.byref(p)))

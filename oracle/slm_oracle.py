@@ -1,0 +1,326 @@
+"""ORACLE (test infrastructure only): CPU FP64 restatement of the semi-Lagrangian advection path.
+
+Checker for the CUDA point-location / interpolation / backtracking kernels and the timed CPU
+baseline of that path. Only tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU leg use it.
+
+Restated reference behaviour (paths inside the reference project):
+* mfiles_SPH/advect3d_slm_p_sph.m:165-242 (PC2), :298-410 (predictor), :412-440 (corrector)
+* mfiles_SPH/find_pts_outside_domain_sph.m:27-98 (radial clamp)
+* mfiles_SPH/local_coords_3d_sph.m:28-147 (per-class frames, barycentric determinant ratios)
+* mfiles_SPH/local_coords_curved_3d_sph.m:36-168 (6 Newton steps on the 10-node map, tol 1e-8)
+* mfiles_SPH/locate_points_interp_vars_3d_sph.m:34-207 (guess, check, search, adjust_local_coords)
+* mfiles_M3TET/locate_points_in_neighboring_element.m:1-158 (tolerance growth 1e-6 .. 15e-3)
+* mfiles_M3TET/interp3d_tet.m:39-69 (P2 interpolation, monotone clamp)
+* mfiles_M3TET/interp3d_cubic_p.m:80-382 (quasi-cubic interpolation, 'dist' weighted gradients)
+
+Point location. The reference's ``tsearch2_sph`` runs MUTILS ``tsearch2`` (not vendored, not runnable
+here) in up to five rotated frames and filters by element class. Its semantics for a point that
+lies strictly inside exactly one element, in that element's own frame, is that element; this
+oracle finds every containing element by an exhaustive own-frame barycentric test over the
+nearest elements and applies a deterministic rule for ties: prefer non-isoparametric elements,
+then the largest element id (the reference takes ``max`` over its candidate columns,
+tsearch2_sph.m:404). MUTILS's own choice among tied elements is unpinned.
+"""
+from __future__ import annotations
+
+import numpy as np
+from scipy.spatial import cKDTree
+
+RX90 = np.array([[1.0, 0, 0], [0, 0, -1.0], [0, 1.0, 0]])
+RZ180 = np.diag([-1.0, -1.0, 1.0])
+
+
+def cart2sph(X):
+    x, y, z = X
+    r = np.sqrt(x * x + y * y + z * z)
+    th = np.arctan2(np.sqrt(x * x + y * y), z)
+    ph = np.arctan2(y, x)
+    ph = np.where(ph < 0, ph + 2 * np.pi, ph)
+    return np.array([th, ph, r])
+
+
+def sph2cart(S):
+    th, ph, r = S
+    return np.array([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)])
+
+
+class Frames:
+    """Node coordinates in the three spherical frames used by local_coords_3d_sph."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        self.S0 = mesh['GCOORD_SPH']
+        self.SZ = cart2sph(RZ180 @ mesh['GCOORD'])
+        self.SX = cart2sph(RX90 @ mesh['GCOORD'])
+        self.EL = mesh['EL2NOD']
+        self.cls = mesh['cls']
+
+    def point_frames(self, P):
+        X = sph2cart(P)
+        return P, cart2sph(RZ180 @ X), cart2sph(RX90 @ X)
+
+
+def compute_lc(V, p):
+    """Barycentric (r,s,t) of points p (3,n) in straight tets with vertex coords V (n,3,4)
+    (determinant ratios of local_coords_3d_sph.m:94-147)."""
+    th, ph, r = V[:, 0, :].T, V[:, 1, :].T, V[:, 2, :].T   # (4,n)
+    thp, php, rp = p
+
+    def D(a, b, c, d, ta, pa, ra):
+        # det of [x_b - x_a; x_c - x_a; x_d - x_a] style expression used in the reference
+        return ((th[b] - ta) * (ph[c] - pa) * (r[d] - ra) + (th[c] - ta) * (ph[d] - pa) * (r[b] - ra)
+                + (th[d] - ta) * (ph[b] - pa) * (r[c] - ra) - (r[b] - ra) * (ph[c] - pa) * (th[d] - ta)
+                - (r[c] - ra) * (ph[d] - pa) * (th[b] - ta) - (r[d] - ra) * (ph[b] - pa) * (th[c] - ta))
+    l1 = D(0, 1, 2, 3, thp, php, rp) / D(0, 1, 2, 3, th[0], ph[0], r[0])
+    l2 = D(1, 0, 2, 3, thp, php, rp) / D(1, 0, 2, 3, th[1], ph[1], r[1])
+    l3 = D(2, 0, 1, 3, thp, php, rp) / D(2, 0, 1, 3, th[2], ph[2], r[2])
+    return np.array([l1, l2, l3])
+
+
+def sf10(r, s, t):
+    u = 1 - r - s - t
+    N = np.array([r * (2 * r - 1), s * (2 * s - 1), t * (2 * t - 1), u * (2 * u - 1),
+                  4 * r * s, 4 * s * t, 4 * t * u, 4 * r * u, 4 * r * t, 4 * s * u])
+    z = np.zeros_like(r)
+    dN = np.array([
+        [4 * r - 1, z, z], [z, 4 * s - 1, z], [z, z, 4 * t - 1], [1 - 4 * u, 1 - 4 * u, 1 - 4 * u],
+        [4 * s, 4 * r, z], [z, 4 * t, 4 * s], [-4 * t, -4 * t, 4 * (u - t)], [4 * (u - r), -4 * r, -4 * r],
+        [4 * t, z, 4 * r], [-4 * s, 4 * (u - s), -4 * s]])
+    return N, dN
+
+
+def local_coords_curved(SX, EL, els, pX):
+    """local_coords_curved_3d_sph: linear guess + up to 6 Newton steps on the 10-node map in the
+    X-90 frame, stopping when the largest error of all points is below 1e-8. Returns lc and the
+    last Newton step delS."""
+    V = SX[:, EL[els, :4]].transpose(1, 0, 2)
+    lc = compute_lc(V, pX)
+    G = SX[:, EL[els]]                      # (3,n,10)
+    delS = np.zeros_like(lc)
+    for _ in range(6):
+        N, dN = sf10(*lc)                   # N (10,n), dN (10,3,n)
+        TH0 = np.einsum('kni,in->kn', G, N)
+        dTH = pX - TH0
+        err = np.sqrt((dTH * dTH).sum(0))
+        if err.size == 0 or err.max() < 1e-8:
+            break
+        J = np.einsum('kni,ijn->nkj', G, dN)    # (n,3,3): d TH_k / d s_j
+        delS = np.linalg.solve(J, dTH.T[:, :, None])[:, :, 0].T
+        lc = lc + delS
+    return lc, delS
+
+
+def local_coords(F, els, P):
+    """Own-frame local coordinates (3,n) of points P (3,n, original (theta,phi,r)) in elements els."""
+    els = np.asarray(els, dtype=np.int64)
+    P0, PZ, PX = F.point_frames(P)
+    lc = np.zeros((3, len(els)))
+    cls = F.cls[els]
+    EL = F.EL
+    for c, S, Pp in ((0, F.S0, P0), (1, F.SZ, PZ), (2, F.SX, PX)):
+        m = cls == c
+        if m.any():
+            V = S[:, EL[els[m], :4]].transpose(1, 0, 2)
+            lc[:, m] = compute_lc(V, Pp[:, m])
+    m = cls == 3
+    if m.any():
+        lc[:, m], _ = local_coords_curved(F.SX, EL, els[m], PX[:, m])
+    return lc
+
+
+def inside(lc, tol=0.0):
+    l4 = 1 - lc.sum(0)
+    return (lc.min(0) >= -tol) & (lc.max(0) <= 1 + tol) & (l4 >= -tol) & (l4 <= 1 + tol)
+
+
+class Locator:
+    """Exhaustive own-frame point location over the k nearest elements (by centroid)."""
+
+    def __init__(self, mesh, k=48):
+        self.F = Frames(mesh)
+        X = mesh['GCOORD']
+        EL = mesh['EL2NOD']
+        self.cent = X[:, EL[:, :4]].mean(axis=2).T
+        self.tree = cKDTree(self.cent)
+        self.k = k
+        self.iso = mesh['cls'] == 3
+
+    def locate(self, P, return_info=False):
+        """Element ids (0-based) and lc of points P (3,n). info: number of candidates per point
+        with exact containment, and min barycentric margin of the chosen element."""
+        n = P.shape[1]
+        Xp = sph2cart(P).T
+        _, nb = self.tree.query(Xp, k=self.k)
+        els = np.full(n, -1, np.int64)
+        lcs = np.zeros((3, n))
+        ncand = np.zeros(n, np.int32)
+        margin = np.full(n, -np.inf)
+        Pk = np.repeat(P, self.k, axis=1)
+        cand = nb.ravel()
+        lc = local_coords(self.F, cand, Pk).reshape(3, n, self.k)
+        l4 = 1 - lc.sum(0)
+        mn = np.minimum(lc.min(0), l4)          # (n,k) smallest barycentric
+        mx = np.maximum(lc.max(0), l4)
+        ok = (mn >= 0) & (mx <= 1)
+        ncand = ok.sum(1)
+        for i in range(n):
+            c = np.nonzero(ok[i])[0]
+            if len(c) == 0:
+                # grow the tolerance in 1e-6 steps up to 15e-3 (locate_points_in_neighboring_element.m)
+                need = np.maximum(-mn[i], mx[i] - 1.0)
+                steps = np.ceil(need / 1e-6 - 1e-9)
+                smin = steps.min()
+                if smin * 1e-6 > 15e-3 + 1e-6:
+                    continue
+                c = np.nonzero(steps == smin)[0]
+            ids = nb[i, c]
+            noniso = ~self.iso[ids]
+            if noniso.any() and not noniso.all():
+                c, ids = c[noniso], ids[noniso]
+            j = np.argmax(ids)
+            els[i] = ids[j]
+            lcs[:, i] = lc[:, i, c[j]]
+            margin[i] = mn[i, c[j]]
+        if return_info:
+            return els, lcs, dict(ncand=ncand, margin=margin)
+        return els, lcs
+
+
+def adjust_local_coords(lc):
+    lc = np.clip(lc, 0.0, 1.0)
+    s = lc.sum(0)
+    bad = s > 1
+    lc[:, bad] = lc[:, bad] / s[bad]
+    return lc
+
+
+def interp3d_tet(EL, els, lc, V, monotonic=False):
+    """P2 interpolation of nodal V (nnod,) or (nnod,nvar) (interp3d_tet.m:39-69)."""
+    N, _ = sf10(*lc)
+    V2 = V[:, None] if V.ndim == 1 else V
+    out = np.einsum('in,nik->nk', N, V2[EL[els]])
+    if monotonic:
+        vals = V2[EL[els]]                       # (n,10,nvar)
+        out = np.clip(out, vals.min(1), vals.max(1))
+    return out[:, 0] if V.ndim == 1 else out
+
+
+def calc_derivatives(GCOORD, EL4, B, method_wght='dist'):
+    """Nodal gradients of vertex values B from P1 element gradients (interp3d_cubic_p.m:244-375)."""
+    nnod = GCOORD.shape[1]
+    X = GCOORD[:, EL4]                           # (3,nel,4)
+    Mx, My, Mz = X[0], X[1], X[2]
+    if method_wght == 'dist':
+        C = X.mean(axis=2, keepdims=True)
+        w = 1.0 / np.sqrt(((X - C) ** 2).sum(0))
+    else:
+        w = np.ones_like(Mx)
+    A = np.stack([np.ones_like(Mx), Mx, My, Mz], axis=2)   # (nel,4,4): rows = vertices
+    Bv = B[EL4]
+    coef = np.linalg.solve(A, Bv[:, :, None])[:, :, 0]      # [c0, dB/dx, dB/dy, dB/dz]
+    grad_el = coef[:, 1:]
+    num = np.zeros((nnod, 3))
+    den = np.zeros(nnod)
+    for k in range(3):
+        num[:, k] = np.bincount(EL4.ravel(), weights=(w * grad_el[:, k:k + 1]).ravel(), minlength=nnod)
+    den = np.bincount(EL4.ravel(), weights=w.ravel(), minlength=nnod)
+    return num, grad_el, den
+
+
+def interp3d_cubic(GCOORD, EL, els, lc, B, monotonic=True, method_wght='dist'):
+    """Quasi-cubic interpolation of vertex values of B (interp3d_cubic_p.m:80-226)."""
+    EL4 = EL[:, :4]
+    num, gel, den = calc_derivatives(GCOORD, EL4, B, method_wght)
+    with np.errstate(invalid='ignore', divide='ignore'):
+        gn = num / den[:, None]
+    r, s, t = lc
+    u = 1 - r - s - t
+    q2 = np.sqrt(2.0)
+    N = np.array([r, s, t, u, q2 * r * s, q2 * s * t, t * u, r * u, q2 * r * t, s * u,
+                  q2 * s * r * (s - r), q2 * s * t * (t - s), t * u * (u - t), r * u * (u - r),
+                  q2 * r * t * (t - r), s * u * (u - s)])
+    v = EL4[els]                                 # (n,4)
+    X = GCOORD[:, v]                             # (3,n,4)
+    dB = gn[v] - gel[els][:, None, :]            # (n,4,3)
+    e_r = X[:, :, 0] - X[:, :, 3]
+    e_s = X[:, :, 1] - X[:, :, 3]
+    e_t = X[:, :, 2] - X[:, :, 3]
+    sr = np.einsum('kn,njk->jn', e_r, dB)         # slopeDev_r(node j)
+    ss = np.einsum('kn,njk->jn', e_s, dB)
+    st = np.einsum('kn,njk->jn', e_t, dB)
+    h = np.sqrt(0.5)
+    q1n2, q1n1 = h * sr[1] - h * ss[1], h * sr[0] - h * ss[0]
+    q2n3, q2n2 = h * ss[2] - h * st[2], h * ss[1] - h * st[1]
+    q5n3, q5n1 = h * sr[2] - h * st[2], h * sr[0] - h * st[0]
+    info = np.array([(q1n2 - q1n1) / 2, (q2n3 - q2n2) / 2, (st[3] - st[2]) / 2, (sr[3] - sr[0]) / 2,
+                     (q5n3 - q5n1) / 2, (ss[3] - ss[1]) / 2, (q1n2 + q1n1) / 2, (q2n3 + q2n2) / 2,
+                     (st[3] + st[2]) / 2, (sr[3] + sr[0]) / 2, (q5n3 + q5n1) / 2, (ss[3] + ss[1]) / 2])
+    Bi = (N[:4] * B[v].T).sum(0) + (N[4:] * info).sum(0)
+    if monotonic:
+        Bv = B[v]
+        Bi = np.clip(Bi, Bv.min(1), Bv.max(1))
+    return Bi
+
+
+def clamp_radius(P, r_cmb, r_surf):
+    """find_pts_outside_domain_sph: move points outside [r_cmb, r_surf] just inside."""
+    P = P.copy()
+    r_tol = 1e-12 * (r_surf - r_cmb)
+    P[2] = np.where(P[2] <= r_cmb + r_tol, r_cmb + r_tol, P[2])
+    P[2] = np.where(P[2] >= r_surf - r_tol, r_surf - r_tol, P[2])
+    return P
+
+
+def predictor(X, S, U, dt):
+    """predictor_step_with_projections (advect3d_slm_p_sph.m:298-410); U (3,n) Cartesian."""
+    rr = S[2]
+    ru = X / rr
+    upar = (U * ru).sum(0) * ru / (np.sqrt((ru ** 2).sum(0)) ** 2)
+    uperp = U - upar
+    nperp = np.sqrt((uperp ** 2).sum(0))
+    with np.errstate(invalid='ignore', divide='ignore'):
+        upu = uperp / nperp
+    upu = np.where(np.isnan(upu), 0.0, upu)
+    lpar = np.sqrt((upar ** 2).sum(0)) * 0.5 * dt
+    lperp = nperp * 0.5 * dt
+    lprime = rr * np.tan(lperp / rr)
+    rp = X - upu * lprime
+    rbu = rp / np.sqrt((rp ** 2).sum(0))
+    xyz = rbu * np.abs(rr - lpar)
+    return cart2sph(xyz), upu, rbu
+
+
+def corrector(X, S, U, upu, rpu, dt):
+    """corrector_step_with_projections (advect3d_slm_p_sph.m:412-440)."""
+    rr = S[2]
+    upar = (U * rpu).sum(0) * rpu / (np.sqrt((rpu ** 2).sum(0)) ** 2)
+    uperp = U - upar
+    lpar = np.sqrt((upar ** 2).sum(0)) * dt
+    lperp = np.sqrt((uperp ** 2).sum(0)) * dt
+    lprime = rr * np.tan(lperp / rr)
+    rp = X - upu * lprime
+    rbu = rp / np.sqrt((rp ** 2).sum(0))
+    xyz = rbu * np.abs(rr - lpar)
+    return cart2sph(xyz)
+
+
+def advect_pc2(mesh, U, T, dt, r_cmb, r_surf, method_interp='quadratic', monotonic=True, k=48):
+    """advect3d_slm_p_sph with PC2 backtracking; U (nnod,3) Cartesian; returns new T, departure
+    points (3,nnod), element ids of the predictor and departure points."""
+    X = mesh['GCOORD']
+    S = mesh['GCOORD_SPH']
+    loc = Locator(mesh, k)
+    Pp, upu, rpu = predictor(X, S, U.T, dt)
+    Pp = clamp_radius(Pp, r_cmb, r_surf)
+    e1, lc1 = loc.locate(Pp)
+    lc1 = adjust_local_coords(lc1)
+    Ubt = interp3d_tet(mesh['EL2NOD'], e1, lc1, U, monotonic=False)
+    Pd = corrector(X, S, Ubt.T, upu, rpu, dt)
+    Pd = clamp_radius(Pd, r_cmb, r_surf)
+    e2, lc2 = loc.locate(Pd)
+    lc2 = adjust_local_coords(lc2)
+    if method_interp == 'cubic':
+        Tn = interp3d_cubic(X, mesh['EL2NOD'], e2, lc2, T, monotonic)
+    else:
+        Tn = interp3d_tet(mesh['EL2NOD'], e2, lc2, T, monotonic)
+    return Tn, Pd, e1, e2
