@@ -32,7 +32,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Stokes solve time to 1e-8 rel. residual: learned+FP32-MG vs plain FP64 on 1 GPU"
 TARGET = 1e-8
-SOLVER_KW = dict(rtol_Pat=1e-9, rtol_U=1e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=TARGET)
+# Patera / MG-PCG tolerances: the reference's rtol_U (5e-3) and a pressure tolerance that the
+# coupled-residual check tightens (x0.1) until the 1e-8 target is met
+SOLVER_KW = dict(rtol_Pat=1e-7, rtol_U=5e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=TARGET)
 
 
 def dist_init():

@@ -24,6 +24,19 @@ constexpr int MAX_COLORS = 128;
 // packed lower-triangle index of (r, c), r >= c, column-major (MUTILS sparse_create layout)
 __host__ __device__ constexpr int pack_idx(int r, int c) { return c * (2 * NUDOF - c + 1) / 2 + (r - c); }
 
+// Element matrices are stored as vectorised SoA: packed entry k of element e of a level with nel
+// elements lives at ((k / V) * nel + e) * V + k % V with V = 4 (float) or 2 (double), so one
+// thread loads 16 bytes at a time and a warp's loads stay contiguous (512 B per load).
+template <typename T> struct KVec;
+template <> struct KVec<float> { static constexpr int V = 4; };
+template <> struct KVec<double> { static constexpr int V = 2; };
+template <typename T>
+__host__ __device__ __forceinline__ size_t kidx(int k, size_t e, size_t nel) {
+  constexpr int V = KVec<T>::V;
+  return ((size_t)(k / V) * nel + e) * V + (k % V);
+}
+template <typename T> constexpr int kpad() { return ((NPACK + KVec<T>::V - 1) / KVec<T>::V) * KVec<T>::V; }
+
 void set_error(const std::string &msg);
 // host-side count of kernel launches issued by this library (reported by m3sph_launch_count)
 void count_launch();
@@ -64,6 +77,7 @@ struct Level {
   uint8_t *freemask = nullptr;        // [ndof], 1 = free dof
   double *K64 = nullptr;              // [465][nel] rotated, masked element matrices
   float *K32 = nullptr;
+  float *KL32 = nullptr;              // K64 - K32 rounded to FP32 (finest level, mixed precision)
   double *Dinv64 = nullptr;           // [ndof] inverse diagonal (0 on fixed dofs)
   float *Dinv32 = nullptr;
   // children (coarse levels): fine stored index of child k, and parent-local vertex indices
@@ -74,6 +88,12 @@ struct Level {
   float *P_w = nullptr;
   int *R_ptr = nullptr, *R_col = nullptr;   // coarse node rows (transpose)
   float *R_w = nullptr;
+  // assembled 3x3-block CSR of the level operator (coarse levels): one launch per application
+  int nnzb = 0;
+  int *bsr_ptr = nullptr, *bsr_col = nullptr;   // [nnod+1], [nnzb]
+  int *bsr_cptr = nullptr, *bsr_contrib = nullptr;   // per block: contributions e*100 + a*10 + b
+  double *B64 = nullptr;                         // [nnzb][9]
+  float *B32 = nullptr;
   // host copies needed at set-up
   std::vector<int> h_el2nod_orig;     // [nel][10] original order, 0-based
 };
@@ -114,6 +134,7 @@ struct SetupArgs {
   const uint8_t *freemask;
   double g, Bscale, Dens0, minVisc, maxVisc;
   double *K64; float *K32; double *G64; double *M64; double *Fbe;
+  float *KL32;              // low FP32 part of K64 - K32 (double-float outer operator) or nullptr
   const double *ufix;       // [3*nnod] prescribed values (rotated frame) or nullptr
   double *BCe;              // [30][nel] element K_unmasked * ufix (when ufix != nullptr)
   int *err;
@@ -145,6 +166,7 @@ struct m3sph_mesh {
   void (*wk_free)(void *) = nullptr;
   std::vector<std::pair<double *, cudaGraphExec_t>> graphs;   // captured MG-PCG iterations
   bool use_graphs = true;
+  bool df_outer = true;               // double-float outer operator on the mixed path
   unsigned long long graph_kernels = 0;   // kernel launches per captured iteration
   void *slm = nullptr;                // advection / point-location state
   void (*slm_free)(void *) = nullptr;

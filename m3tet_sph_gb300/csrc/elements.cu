@@ -255,9 +255,11 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
         }
         if (rr < cc) continue;
         if (!((mask >> rr) & 1) || !((mask >> cc) & 1)) v = 0.0;
-        const size_t k = (size_t)pack_idx(rr, cc) * nel + e;
-        a.K64[k] = v;
-        a.K32[k] = (float)v;
+        const int k = pack_idx(rr, cc);
+        a.K64[kidx<double>(k, e, nel)] = v;
+        const float hi = (float)v;
+        a.K32[kidx<float>(k, e, nel)] = hi;
+        if (a.KL32) a.KL32[kidx<float>(k, e, nel)] = (float)(v - (double)hi);
       }
   }
   // phase 2b: gradient matrix G[p][3n+c'] (rotated, not masked)
@@ -323,9 +325,22 @@ int launch_element_setup(const SetupArgs &a, cudaStream_t s) {
 // ----------------------------------------------------------------------------------------
 // element-by-element y += K x over one colour (no two elements of a colour share a node)
 // ----------------------------------------------------------------------------------------
+template <typename T> struct Vec;
+template <> struct Vec<float> { using type = float4; };
+template <> struct Vec<double> { using type = double2; };
+template <typename V, typename T> __device__ __forceinline__ T lane(const V &v, int i);
+template <> __device__ __forceinline__ float lane<float4, float>(const float4 &v, int i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+template <> __device__ __forceinline__ double lane<double2, double>(const double2 &v, int i) {
+  return i == 0 ? v.x : v.y;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_ebe_apply(const T *__restrict__ K, const int *__restrict__ el2nod, int nel,
                                                    int e_begin, int e_end, const T *__restrict__ x, T *__restrict__ y) {
+  using VT = typename Vec<T>::type;
+  constexpr int V = KVec<T>::V;
   const int e = e_begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= e_end) return;
   int nod[10];
@@ -339,20 +354,96 @@ __global__ void __launch_bounds__(128) k_ebe_apply(const T *__restrict__ K, cons
       xe[3 * n + c] = x[3 * nod[n] + c];
       ye[3 * n + c] = T(0);
     }
-  const T *Ke = K + e;
+  const VT *Kv = reinterpret_cast<const VT *>(K) + e;
+  VT v4;
+  int k = 0;
 #pragma unroll
   for (int c = 0; c < 30; ++c) {
 #pragma unroll
     for (int r = c; r < 30; ++r) {
-      const T v = __ldcs(Ke + (size_t)pack_idx(r, c) * nel);
+      if (k % V == 0) v4 = __ldcs(Kv + (size_t)(k / V) * nel);
+      const T v = lane<VT, T>(v4, k % V);
       ye[r] += v * xe[c];
       if (r != c) ye[c] += v * xe[r];
+      ++k;
     }
   }
 #pragma unroll
   for (int n = 0; n < 10; ++n)
 #pragma unroll
     for (int c = 0; c < 3; ++c) y[3 * nod[n] + c] += ye[3 * n + c];
+}
+
+// y += K x in FP64 accuracy from FP32 arithmetic: K = hi + lo (two FP32 arrays, hi is the FP32
+// operator of the V-cycle), x split the same way at the gather; each product is formed exactly
+// (FMA error term) and accumulated in double-float (Knuth two-sum). ~10 FP32 operations per
+// multiply-add instead of one FP64 FMA, which GB300 issues at 1/62 of its FP32 rate.
+__device__ __forceinline__ void df_mac(float vh, float vl, float xh, float xl, float &sh, float &sl) {
+  const float p = vh * xh;
+  float e = fmaf(vh, xh, -p);
+  e = fmaf(vh, xl, e);
+  e = fmaf(vl, xh, e);
+  const float s = sh + p;
+  const float bb = s - sh;
+  const float err = (sh - (s - bb)) + (p - bb);
+  sh = s;
+  sl += err + e;
+}
+
+__global__ void __launch_bounds__(128) k_ebe_apply_df(const float *__restrict__ Kh, const float *__restrict__ Kl,
+                                                      const int *__restrict__ el2nod, int nel, int e_begin, int e_end,
+                                                      const double *__restrict__ x, double *__restrict__ y) {
+  const int e = e_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e_end) return;
+  int nod[10];
+#pragma unroll
+  for (int n = 0; n < 10; ++n) nod[n] = __ldg(el2nod + (size_t)n * nel + e);
+  float xh[30], xl[30], sh[30], sl[30];
+#pragma unroll
+  for (int n = 0; n < 10; ++n)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double xv = x[3 * nod[n] + c];
+      const float h = (float)xv;
+      xh[3 * n + c] = h;
+      xl[3 * n + c] = (float)(xv - (double)h);
+      sh[3 * n + c] = 0.f;
+      sl[3 * n + c] = 0.f;
+    }
+  const float4 *Hv = reinterpret_cast<const float4 *>(Kh) + e;
+  const float4 *Lv = reinterpret_cast<const float4 *>(Kl) + e;
+  float4 h4, l4;
+  int k = 0;
+#pragma unroll
+  for (int c = 0; c < 30; ++c) {
+#pragma unroll
+    for (int r = c; r < 30; ++r) {
+      if (k % 4 == 0) {
+        h4 = __ldcs(Hv + (size_t)(k / 4) * nel);
+        l4 = __ldcs(Lv + (size_t)(k / 4) * nel);
+      }
+      const float vh = lane<float4, float>(h4, k % 4), vl = lane<float4, float>(l4, k % 4);
+      df_mac(vh, vl, xh[c], xl[c], sh[r], sl[r]);
+      if (r != c) df_mac(vh, vl, xh[r], xl[r], sh[c], sl[c]);
+      ++k;
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < 10; ++n)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) y[3 * nod[n] + c] += (double)sh[3 * n + c] + (double)sl[3 * n + c];
+}
+
+int ebe_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s) {
+  M3_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * L.ndof, s));
+  const int nc = (int)L.cstart.size() - 1;
+  for (int c = 0; c < nc; ++c) {
+    const int b = L.cstart[c], e = L.cstart[c + 1];
+    if (e <= b) continue;
+    k_ebe_apply_df<<<(e - b + 127) / 128, 128, 0, s>>>(Kh, Kl, L.el2nod, L.nel, b, e, x, y); count_launch();
+  }
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
 }
 
 template <typename T>
@@ -402,7 +493,7 @@ __global__ void k_diag_scatter(const T *__restrict__ K, const int *__restrict__ 
   if (e >= e_end) return;
   for (int q = 0; q < 30; ++q) {
     const int nod = el2nod[(size_t)(q / 3) * nel + e];
-    D[3 * nod + q % 3] += (double)K[(size_t)pack_idx(q, q) * nel + e];
+    D[3 * nod + q % 3] += (double)K[kidx<T>(pack_idx(q, q), e, nel)];
   }
 }
 
@@ -563,7 +654,7 @@ __global__ void __launch_bounds__(256) k_galerkin(const T *__restrict__ Kf, int 
     for (int q = tid; q < 900; q += blockDim.x) {
       const int r = q / 30, c = q % 30;
       const int rr = r > c ? r : c, cc = r > c ? c : r;
-      sK[r][c] = Kf[(size_t)pack_idx(rr, cc) * nel_f + fe];
+      sK[r][c] = Kf[kidx<T>(pack_idx(rr, cc), fe, nel_f)];
     }
     __syncthreads();
     // T[a][(j,c)] = sum_i K[a][(i,c)] W[i][j]
@@ -595,7 +686,7 @@ __global__ void __launch_bounds__(256) k_galerkin(const T *__restrict__ Kf, int 
     const int nr = el2nod_c[(size_t)(rr / 3) * nel_c + pc], nc = el2nod_c[(size_t)(cc / 3) * nel_c + pc];
     T v = sAcc[q];
     if (!mask_c[3 * nr + rr % 3] || !mask_c[3 * nc + cc % 3]) v = T(0);
-    Kc[(size_t)q * nel_c + pc] = v;
+    Kc[kidx<T>(q, pc, nel_c)] = v;
   }
 }
 
@@ -607,6 +698,72 @@ int galerkin(const Level &F, const T *Kf, Level &C, T *Kc, cudaStream_t s) {
 }
 template int galerkin<double>(const Level &, const double *, Level &, double *, cudaStream_t);
 template int galerkin<float>(const Level &, const float *, Level &, float *, cudaStream_t);
+
+// ----------------------------------------------------------------------------------------
+// assembled block operator for coarse levels: gather-assembly (deterministic, no atomics) and
+// block-row SpMV. Block (i,j) of the level operator is the sum over elements containing nodes i
+// and j of the element block (a,b) with node(a) = i, node(b) = j.
+// ----------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_bsr_assemble(const T *__restrict__ K, int nel, int nnzb, const int *__restrict__ cptr,
+                               const int *__restrict__ contrib, T *__restrict__ B) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnzb) return;
+  T acc[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q] = T(0);
+  for (int c = cptr[k]; c < cptr[k + 1]; ++c) {
+    const int code = contrib[c];
+    const int p = code / 100, a = (code / 10) % 10, b = code % 10;
+#pragma unroll
+    for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+      for (int qq = 0; qq < 3; ++qq) {
+        const int r = 3 * a + pp, cc = 3 * b + qq;
+        const int idx = r >= cc ? pack_idx(r, cc) : pack_idx(cc, r);
+        acc[pp * 3 + qq] += K[kidx<T>(idx, p, nel)];
+      }
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) B[(size_t)k * 9 + q] = acc[q];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_bsr_spmv(const int *__restrict__ ptr, const int *__restrict__ col,
+                                                  const T *__restrict__ B, int nrow, const T *__restrict__ x,
+                                                  T *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrow) return;
+  T s0 = 0, s1 = 0, s2 = 0;
+  for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+    const int j = col[k];
+    const T *b = B + (size_t)k * 9;
+    const T x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+    s0 += b[0] * x0 + b[1] * x1 + b[2] * x2;
+    s1 += b[3] * x0 + b[4] * x1 + b[5] * x2;
+    s2 += b[6] * x0 + b[7] * x1 + b[8] * x2;
+  }
+  y[3 * i] = s0;
+  y[3 * i + 1] = s1;
+  y[3 * i + 2] = s2;
+}
+
+template <typename T>
+int bsr_assemble(const Level &L, const T *K, T *B, cudaStream_t s) {
+  k_bsr_assemble<T><<<(L.nnzb + 127) / 128, 128, 0, s>>>(K, L.nel, L.nnzb, L.bsr_cptr, L.bsr_contrib, B); count_launch();
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+template <typename T>
+int bsr_apply(const Level &L, const T *B, const T *x, T *y, cudaStream_t s) {
+  k_bsr_spmv<T><<<(L.nnod + 127) / 128, 128, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, x, y); count_launch();
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+template int bsr_assemble<double>(const Level &, const double *, double *, cudaStream_t);
+template int bsr_assemble<float>(const Level &, const float *, float *, cudaStream_t);
+template int bsr_apply<double>(const Level &, const double *, const double *, double *, cudaStream_t);
+template int bsr_apply<float>(const Level &, const float *, const float *, float *, cudaStream_t);
 
 __global__ void k_f64_to_f32(const double *a, float *b, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;

@@ -311,7 +311,7 @@ __global__ void k_dense_assemble(const T *__restrict__ K, const int *__restrict_
     const int rr = cc + rem;
     const int gr = 3 * el2nod[(size_t)(rr / 3) * nel + e] + rr % 3;
     const int gc = 3 * el2nod[(size_t)(cc / 3) * nel + e] + cc % 3;
-    const T v = K[(size_t)q * nel + e];
+    const T v = K[kidx<T>(q, e, nel)];
     if (v == T(0)) continue;
     atomicAdd(&A[(size_t)gr * n + gc], v);
     if (gr != gc) atomicAdd(&A[(size_t)gc * n + gr], v);

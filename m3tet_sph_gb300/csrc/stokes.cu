@@ -23,12 +23,15 @@ namespace m3sph {
 
 int launch_element_setup(const SetupArgs &a, cudaStream_t s);
 template <typename T> int ebe_apply(const Level &L, const T *K, const T *x, T *y, cudaStream_t s);
+int ebe_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
 int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
 template <typename T> int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s);
 int grad_apply(const Level &L, const double *G, const double *q, double *y, cudaStream_t s);
 int div_apply(const Level &L, const double *G, const double *z, double *out, cudaStream_t s);
 int mass_apply(const Level &L, const double *M, const double *d, double *out, cudaStream_t s);
 template <typename T> int galerkin(const Level &F, const T *Kf, Level &C, T *Kc, cudaStream_t s);
+template <typename T> int bsr_assemble(const Level &L, const T *K, T *B, cudaStream_t s);
+template <typename T> int bsr_apply(const Level &L, const T *B, const T *x, T *y, cudaStream_t s);
 int dot(const double *a, const double *b, size_t n, double *partials, double *out, cudaStream_t s);
 int dot2(const double *a, const double *c, const double *b, size_t n, double *partials, double *out, cudaStream_t s);
 int vsum(const double *a, size_t n, double *partials, double *out, cudaStream_t s);
@@ -194,6 +197,59 @@ extern "C" int m3sph_device_count(int *count) {
   return M3SPH_OK;
 }
 
+// block sparsity pattern of a level and the element contributions of every block
+static int build_bsr(m3sph_mesh *M, Level &L, const std::vector<int> &perm) {
+  const int nel = L.nel, nnod = L.nnod;
+  std::vector<int> invp(nel);
+  for (int p = 0; p < nel; ++p) invp[perm[p]] = p;
+  // node -> (stored element, local index)
+  std::vector<int> nptr(nnod + 1, 0);
+  for (size_t i = 0; i < (size_t)nel * 10; ++i) nptr[L.h_el2nod_orig[i] + 1]++;
+  for (int n = 0; n < nnod; ++n) nptr[n + 1] += nptr[n];
+  std::vector<int> nfill(nptr.begin(), nptr.end() - 1), nel_of((size_t)nel * 10), nloc((size_t)nel * 10);
+  for (int e = 0; e < nel; ++e)
+    for (int a = 0; a < 10; ++a) {
+      const int n = L.h_el2nod_orig[(size_t)e * 10 + a];
+      const int pos = nfill[n]++;
+      nel_of[pos] = invp[e];
+      nloc[pos] = a;
+    }
+  std::vector<int> ptr(nnod + 1, 0), col, cptr(1, 0), contrib;
+  col.reserve((size_t)nnod * 32);
+  contrib.reserve((size_t)nel * 100);
+  std::vector<std::pair<int, int>> row;   // (col node, contribution code)
+  for (int i = 0; i < nnod; ++i) {
+    row.clear();
+    for (int k = nptr[i]; k < nptr[i + 1]; ++k) {
+      const int p = nel_of[k], a = nloc[k];
+      const int e = perm[p];
+      for (int b = 0; b < 10; ++b) row.push_back({L.h_el2nod_orig[(size_t)e * 10 + b], p * 100 + a * 10 + b});
+    }
+    std::sort(row.begin(), row.end());
+    for (size_t k = 0; k < row.size(); ++k) {
+      if (k == 0 || row[k].first != row[k - 1].first) {
+        col.push_back(row[k].first);
+        if (k) cptr.push_back((int)contrib.size());
+      }
+      contrib.push_back(row[k].second);
+    }
+    if (!row.empty()) cptr.push_back((int)contrib.size());
+    ptr[i + 1] = (int)col.size();
+  }
+  if ((size_t)nel * 100 > 2147483647ull / 2) {
+    set_error("level too large for the block operator contribution list");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  L.nnzb = (int)col.size();
+  cudaStream_t s = M->stream;
+  M3_TRY(upload(&L.bsr_ptr, ptr.data(), ptr.size(), s));
+  M3_TRY(upload(&L.bsr_col, col.data(), col.size(), s));
+  M3_TRY(upload(&L.bsr_cptr, cptr.data(), cptr.size(), s));
+  M3_TRY(upload(&L.bsr_contrib, contrib.data(), contrib.size(), s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
 static int build_level(m3sph_mesh *M, int img, const m3sph_level &in, Level &L) {
   cudaStream_t s = M->stream;
   L.nel = in.nel;
@@ -236,6 +292,7 @@ static int build_level(m3sph_mesh *M, int img, const m3sph_level &in, Level &L) 
   M3_CUDA(cudaMemsetAsync(L.freemask, 1, L.ndof, s));
   M3_TRY(dalloc(&L.Dinv64, L.ndof));
   M3_TRY(dalloc(&L.Dinv32, L.ndof));
+  if (img > 0) M3_TRY(build_bsr(M, L, perm));
   M3_CUDA(cudaStreamSynchronize(s));
   return M3SPH_OK;
 }
@@ -343,8 +400,10 @@ static void clear_graphs(m3sph_mesh *M);
 
 static void free_level(Level &L) {
   for (void *p : {(void *)L.el2nod, (void *)L.perm, (void *)L.invperm, (void *)L.freemask, (void *)L.K64,
-                  (void *)L.K32, (void *)L.Dinv64, (void *)L.Dinv32, (void *)L.child, (void *)L.child_vloc,
-                  (void *)L.P_ptr, (void *)L.P_col, (void *)L.P_w, (void *)L.R_ptr, (void *)L.R_col, (void *)L.R_w})
+                  (void *)L.K32, (void *)L.KL32, (void *)L.Dinv64, (void *)L.Dinv32, (void *)L.child, (void *)L.child_vloc,
+                  (void *)L.P_ptr, (void *)L.P_col, (void *)L.P_w, (void *)L.R_ptr, (void *)L.R_col, (void *)L.R_w,
+                  (void *)L.bsr_ptr, (void *)L.bsr_col, (void *)L.bsr_cptr, (void *)L.bsr_contrib, (void *)L.B64,
+                  (void *)L.B32})
     dfree(p);
   L = Level();
 }
@@ -475,7 +534,8 @@ extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t
       (st = dalloc(&F.M64, 10 * (size_t)nel)) || (st = dalloc(&F.Fbe, 30 * (size_t)nel)) ||
       (st = dalloc(&F.BCe, 30 * (size_t)nel)) ||
       (st = dalloc(&F.Fb, L0.ndof)) || (st = dalloc(&F.LiMM, L0.nvnod)) || (st = dalloc(&F.err, 4)) ||
-      (st = dalloc(&L0.K64, (size_t)NPACK * nel)) || (st = dalloc(&L0.K32, (size_t)NPACK * nel)) ||
+      (st = dalloc(&L0.K64, (size_t)kpad<double>() * nel)) || (st = dalloc(&L0.K32, (size_t)kpad<float>() * nel)) ||
+      (st = dalloc(&L0.KL32, (size_t)kpad<float>() * nel)) ||
       (st = dalloc(&M->Ufix, L0.ndof)) || (st = dalloc(&M->bc_rhs, L0.ndof)) || (st = dalloc(&M->red, 4096)) ||
       (st = dalloc(&M->scal, 64)))
     return fail(st);
@@ -580,6 +640,7 @@ static int rebuild_operator(m3sph_mesh *M) {
   a.K64 = L0.K64; a.K32 = L0.K32; a.G64 = M->fin.G64; a.M64 = M->fin.M64; a.Fbe = M->fin.Fbe; a.err = M->fin.err;
   a.ufix = nullptr;
   a.BCe = nullptr;
+  a.KL32 = L0.KL32;
   if (M->has_nonzero_fix) {
     a.ufix = M->Ufix;
     a.BCe = M->fin.BCe;
@@ -614,13 +675,17 @@ static int rebuild_operator(m3sph_mesh *M) {
   for (int i = 1; i < M->nmg; ++i) {
     Level &F = M->lev[i - 1], &C = M->lev[i];
     if (M->precision == 0) {
-      if (!C.K64) M3_TRY(dalloc(&C.K64, (size_t)NPACK * C.nel));
+      if (!C.K64) M3_TRY(dalloc(&C.K64, (size_t)kpad<double>() * C.nel));
       M3_TRY(galerkin<double>(F, F.K64, C, C.K64, s));
       M3_TRY(level_inverse_diag<double>(C, C.K64, W->tmp, s));
+      if (!C.B64) M3_TRY(dalloc(&C.B64, 9 * (size_t)C.nnzb));
+      M3_TRY(bsr_assemble<double>(C, C.K64, C.B64, s));
     } else {
-      if (!C.K32) M3_TRY(dalloc(&C.K32, (size_t)NPACK * C.nel));
+      if (!C.K32) M3_TRY(dalloc(&C.K32, (size_t)kpad<float>() * C.nel));
       M3_TRY(galerkin<float>(F, F.K32, C, C.K32, s));
       M3_TRY(level_inverse_diag<float>(C, C.K32, W->tmp, s));
+      if (!C.B32) M3_TRY(dalloc(&C.B32, 9 * (size_t)C.nnzb));
+      M3_TRY(bsr_assemble<float>(C, C.K32, C.B32, s));
     }
   }
   // coarsest dense inverse (stands in for cholesky_factorization)
@@ -716,6 +781,14 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   return M3SPH_OK;
 }
 
+// FP64-accurate finest-level operator for the outer iterations: native FP64 on the plain path,
+// double-float FP32 arithmetic on the mixed path
+static int outer_apply(m3sph_mesh *M, const double *x, double *y) {
+  Level &L0 = M->lev[0];
+  if (M->precision == 1 && M->df_outer) return ebe_apply_df(L0, L0.K32, L0.KL32, x, y, M->stream);
+  return ebe_apply<double>(L0, L0.K64, x, y, M->stream);
+}
+
 // ======================================================================================
 // V-cycle (MG_V_cycle_v2) in precision T; level-0 residual r0 given in T, d0 out in T
 // ======================================================================================
@@ -725,6 +798,17 @@ static const double WDc[3] = {0.25, 0.4, 0.9}, WUc[3] = {0.9, 0.4, 0.25};
 template <typename T> static const T *levK(const Level &L);
 template <> const double *levK<double>(const Level &L) { return L.K64; }
 template <> const float *levK<float>(const Level &L) { return L.K32; }
+template <typename T> static const T *levB(const Level &L);
+template <> const double *levB<double>(const Level &L) { return L.B64; }
+template <> const float *levB<float>(const Level &L) { return L.B32; }
+
+// level operator: element-by-element on the finest level, assembled blocks on coarse levels
+template <typename T>
+static int level_op(const Level &L, int img, const T *x, T *y, cudaStream_t s) {
+  if (img > 0 && levB<T>(L)) return bsr_apply<T>(L, levB<T>(L), x, y, s);
+  return ebe_apply<T>(L, levK<T>(L), x, y, s);
+}
+
 template <typename T> static const T *levDi(const Level &L);
 template <> const double *levDi<double>(const Level &L) { return L.Dinv64; }
 template <> const float *levDi<float>(const Level &L) { return L.Dinv32; }
@@ -742,10 +826,10 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     const double *w = j == 0 ? WD0 : WDc;
     const size_t n = L.ndof;
     M3_TRY(jac_first<T>((T)w[0], r[j], levDi<T>(L), d[j], n, s));
-    M3_TRY(ebe_apply<T>(L, levK<T>(L), d[j], kd[j], s));
+    M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
     for (int k = 1; k < 3; ++k) {
       M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
-      M3_TRY(ebe_apply<T>(L, levK<T>(L), d[j], kd[j], s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
     }
     M3_TRY(restrict_<T>(L, M->lev[j + 1], r[j], kd[j], r[j + 1], s));
   }
@@ -756,7 +840,7 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     const size_t n = L.ndof;
     M3_TRY(prolong<T>(L, M->lev[j + 1], d[j + 1], d[j], d[j], s));
     for (int k = 0; k < 3; ++k) {
-      M3_TRY(ebe_apply<T>(L, levK<T>(L), d[j], kd[j], s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
       M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
     }
   }
@@ -815,7 +899,7 @@ static int cg_iteration(m3sph_mesh *M, double *x) {
   M3_TRY(vcycle(M, W->r, W->d));
   M3_TRY(dot2(W->r, W->Kq, W->d, n, M->red, M->scal + 0, s));   // scal[0]=r.d, scal[1]=Kq_prev.d
   M3_TRY(cg_dir(W->d, W->q, n, M->scal, -1, s));                // first-iteration flag in scal[6]
-  M3_TRY(ebe_apply<double>(L0, L0.K64, W->q, W->Kq, s));
+  M3_TRY(outer_apply(M, W->q, W->Kq));
   M3_TRY(dot(W->q, W->Kq, n, M->red, M->scal + 2, s));
   M3_TRY(cg_update(x, W->r, W->q, W->Kq, n, M->scal, M->red, s));
   M3_TRY(set_first_flag(M, 0.0));
@@ -862,7 +946,7 @@ static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs
   Level &L0 = M->lev[0];
   const size_t n = L0.ndof;
   const double sq = std::sqrt((double)std::max(1, L0.nfree));
-  M3_TRY(ebe_apply<double>(L0, L0.K64, x, W->r, s));
+  M3_TRY(outer_apply(M, x, W->r));
   M3_TRY(sub_mask(b, W->r, L0.freemask, n, s));
   M3_TRY(dot(W->r, W->r, n, M->red, M->scal + 3, s));
   double rr;
@@ -971,7 +1055,7 @@ static int coupled_residual(m3sph_mesh *M, const double *U, const double *P, dou
   M3_TRY(read_scal(M, 10, ff));
   // ru = mask(Fb + G P - bc - K U)
   M3_TRY(build_rhs(M, P, W->Rhs));
-  M3_TRY(ebe_apply<double>(L0, L0.K64, U, W->tmp, s));
+  M3_TRY(outer_apply(M, U, W->tmp));
   M3_TRY(sub_mask(W->Rhs, W->tmp, L0.freemask, n, s));
   double ru;
   M3_TRY(dot(W->tmp, W->tmp, n, M->red, M->scal + 10, s));
@@ -1245,7 +1329,7 @@ extern "C" int m3sph_stokes_apply(m3sph_mesh *M, const double *x, double *y) {
   Level &L0 = M->lev[0];
   cudaStream_t s = M->stream;
   M3_CUDA(cudaMemcpyAsync(W->tmp, x, sizeof(double) * L0.ndof, cudaMemcpyHostToDevice, s));
-  M3_TRY(ebe_apply<double>(L0, L0.K64, W->tmp, W->y, s));
+  M3_TRY(outer_apply(M, W->tmp, W->y));
   M3_CUDA(cudaMemcpyAsync(y, W->y, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
   return M3SPH_OK;
@@ -1286,7 +1370,7 @@ extern "C" int m3sph_element_matrices(m3sph_mesh *M, double *K, double *G, doubl
   M3_TRY(need_op(M));
   Level &L0 = M->lev[0];
   const int nel = L0.nel;
-  std::vector<double> hk((size_t)NPACK * nel), hg(120 * (size_t)nel), hm(10 * (size_t)nel);
+  std::vector<double> hk((size_t)kpad<double>() * nel), hg(120 * (size_t)nel), hm(10 * (size_t)nel);
   std::vector<int> perm(nel);
   M3_CUDA(cudaMemcpy(hk.data(), L0.K64, sizeof(double) * hk.size(), cudaMemcpyDeviceToHost));
   M3_CUDA(cudaMemcpy(hg.data(), M->fin.G64, sizeof(double) * hg.size(), cudaMemcpyDeviceToHost));
@@ -1297,7 +1381,7 @@ extern "C" int m3sph_element_matrices(m3sph_mesh *M, double *K, double *G, doubl
     if (K)
       for (int c = 0; c < 30; ++c)
         for (int r = c; r < 30; ++r) {
-          const double v = hk[(size_t)pack_idx(r, c) * nel + p];
+          const double v = hk[kidx<double>(pack_idx(r, c), p, nel)];
           K[(size_t)e * 900 + r * 30 + c] = v;
           K[(size_t)e * 900 + c * 30 + r] = v;
         }
@@ -1330,12 +1414,12 @@ extern "C" int m3sph_level_apply(m3sph_mesh *M, int32_t img, const double *x, do
   const size_t n = L.ndof;
   if (img == 0 || M->precision == 0) {
     M3_CUDA(cudaMemcpyAsync(W->r64[img], x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    M3_TRY(ebe_apply<double>(L, L.K64, W->r64[img], W->kd64[img], s));
+    M3_TRY(level_op<double>(L, img, W->r64[img], W->kd64[img], s));
     M3_CUDA(cudaMemcpyAsync(y, W->kd64[img], sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   } else {
     M3_CUDA(cudaMemcpyAsync(W->r64[img], x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     M3_TRY(d2f(W->r64[img], W->r32[img], n, s));
-    M3_TRY(ebe_apply<float>(L, L.K32, W->r32[img], W->kd32[img], s));
+    M3_TRY(level_op<float>(L, img, W->r32[img], W->kd32[img], s));
     M3_TRY(f2d(W->kd32[img], W->kd64[img], n, s));
     M3_CUDA(cudaMemcpyAsync(y, W->kd64[img], sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   }

@@ -135,6 +135,9 @@ def make_workload(name, seed=0, nmg=None, level=None, nlayer=None):
         L, n, g, contrast, jump, bc = 5, 32, 5, 1e4, 30.0, 'plates'
     elif name == 'c5':
         L, n, g, contrast, jump, bc = 6, 64, 6, 1e6, 30.0, 'plates'
+    elif name == 'mid':
+        # 1/8 of the 8M-DOF shell (level 4, 16 layers): the profiling case (> L2, a few GB on device)
+        L, n, g, contrast, jump, bc = 4, 16, 4, 1e4, 30.0, 'plates'
     elif name == 'tiny':
         L, n, g, contrast, jump, bc = 2, 4, 2, 1.0, 1.0, 'free_slip'
     elif name == 'tiny_plates':

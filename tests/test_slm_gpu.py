@@ -39,8 +39,13 @@ def test_tsearch_bit_exact_on_unique_points(mesh_case):
     unique = (rinfo['ncand'] == 1) & (rinfo['margin'] >= 1e-12)
     assert unique.mean() > 0.99
     assert np.array_equal(els[unique] - 1, e_ref[unique])
-    # local coordinates in the chosen element agree to rounding
-    assert np.abs(lc[:, unique] - lc_ref[:, unique]).max() < 1e-9
+    # local coordinates agree to rounding in straight elements; in isoparametric elements both
+    # sides stop Newton at the reference's 1e-8 step tolerance (local_coords_curved_3d_sph.m:50)
+    iso = w['levels'][0]['cls'][np.maximum(els - 1, 0)] == 3
+    d = np.abs(lc - lc_ref).max(0)
+    assert d[unique & ~iso].max() < 1e-9
+    if (unique & iso).any():
+        assert d[unique & iso].max() < 1e-6
     # ties and gaps are reported, and follow the same rule in the vast majority of cases
     tied = ~unique
     if tied.any():

@@ -157,3 +157,29 @@ def test_mixed_precision_solution(case):
         assert eU < 1e-8 and eP < 1e-8, (eU, eP, info)
     finally:
         dm2.close()
+
+
+def test_mixed_operators_parity(case):
+    """Mixed-precision set-up: the double-float outer operator keeps FP64 accuracy; the FP32
+    coarse block operator matches the FP64 Galerkin operator to FP32 rounding."""
+    w, S, dm = case
+    from m3tet_sph_gb300 import stokes
+    dm2 = stokes.DeviceMesh(w['levels'])
+    try:
+        dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
+        rng = np.random.default_rng(7)
+        x = np.zeros(S.nU)
+        x[S.ifree] = rng.standard_normal(len(S.ifree))
+        y_ref = np.zeros(S.nU)
+        y_ref[S.ifree] = S.K1 @ x[S.ifree]
+        y = dm2.apply(x)
+        assert np.linalg.norm(y - y_ref) < 1e-12 * np.linalg.norm(y_ref)
+        ifree_c = S.ifree[S.ifree < 3 * w['levels'][1]['nnod']]
+        xc = np.zeros(3 * w['levels'][1]['nnod'])
+        xc[ifree_c] = rng.standard_normal(len(ifree_c))
+        yc_ref = np.zeros_like(xc)
+        yc_ref[ifree_c] = S.KK[1] @ xc[ifree_c]
+        yc = dm2.level_apply(1, xc)
+        assert np.linalg.norm(yc - yc_ref) < 1e-5 * np.linalg.norm(yc_ref)
+    finally:
+        dm2.close()
