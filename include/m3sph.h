@@ -144,6 +144,10 @@ M3SPH_API int m3sph_solution(m3sph_mesh *mesh, double *U_xyz, double *P);
 /* The CUDA stream (cudaStream_t) the handle launches its kernels on. */
 M3SPH_API int m3sph_stream(m3sph_mesh *mesh, void **stream);
 
+/* Kernel-variant switches for measurement and tests: "split_apply" (4-warp split element
+ * kernels, default 1), "graphs" (CUDA-graph replay of MG-PCG iterations, default 1),
+ * "df_outer" (double-float outer operator on the mixed path, default 1). */
+M3SPH_API int m3sph_set_option(m3sph_mesh *mesh, const char *name, int32_t value);
 /* Cumulative number of CUDA kernels this library has launched (all handles). */
 M3SPH_API int m3sph_launch_count(unsigned long long *count);
 /* Operator benchmark: nrep device-resident applications of the level-`img` element operator in

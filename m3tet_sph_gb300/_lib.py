@@ -92,6 +92,7 @@ SIGNATURES = {
     "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_interp3d_cubic": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_advect_slm": ([P, DP, DP, DP, DP, C.c_double, C.POINTER(SlmOpts), IP, IP, C.POINTER(LocateInfo)], C.c_int),
+    "m3sph_set_option": ([P, C.c_char_p, C.c_int32], C.c_int),
     "m3sph_launch_count": ([C.POINTER(C.c_ulonglong)], C.c_int),
     "m3sph_apply_timing": ([P, C.c_int32, C.c_int32, C.c_int32, DP], C.c_int),
 }

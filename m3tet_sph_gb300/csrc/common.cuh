@@ -167,6 +167,7 @@ struct m3sph_mesh {
   std::vector<std::pair<double *, cudaGraphExec_t>> graphs;   // captured MG-PCG iterations
   bool use_graphs = true;
   bool df_outer = true;               // double-float outer operator on the mixed path
+  bool split_apply = true;            // 4-warp split element-by-element kernels on the finest level
   unsigned long long graph_kernels = 0;   // kernel launches per captured iteration
   void *slm = nullptr;                // advection / point-location state
   void (*slm_free)(void *) = nullptr;

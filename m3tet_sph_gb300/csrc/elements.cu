@@ -10,6 +10,8 @@
 //   mfiles_M3TET/calc_element_visc.m:5-7,43-48, calc_element_dens.m:5-7
 //   mfiles_M3TET/flow3d_patera_mg_sph_p.m:225-243 (K1 = RR' K RR), :294-298 (free dofs)
 //   mfiles_M3TET/restrict_stiffmat.m:118-127 (KK{k+1} = Ic2f' KK{k} Ic2f)
+#include <utility>
+
 #include "common.cuh"
 
 namespace m3sph {
@@ -444,6 +446,196 @@ int ebe_apply_df(const Level &L, const float *Kh, const float *Kl, const double 
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
+}
+
+// ----------------------------------------------------------------------------------------
+// split element-by-element apply: a CTA of 4 warps handles 32 elements of one colour; warp w
+// streams the w-th quarter of the packed matrix (lanes = elements, so every load of a warp is
+// one contiguous 512-byte segment), partial results are summed in shared memory and scattered.
+// Packed entry k -> (row, col) is resolved at compile time.
+// ----------------------------------------------------------------------------------------
+__host__ __device__ constexpr int unpack_c(int k) {
+  int c = 0;
+  while (k >= 30 - c) { k -= 30 - c; ++c; }
+  return c;
+}
+__host__ __device__ constexpr int unpack_r(int k) {
+  int c = 0;
+  while (k >= 30 - c) { k -= 30 - c; ++c; }
+  return c + k;
+}
+
+struct OpF32 {   // FP32 V-cycle operator
+  using acc_t = float;
+  static constexpr bool two_part = false;
+  static constexpr int V = 4;
+  static constexpr int NCH = 117;
+  const float4 *K;
+  __device__ __forceinline__ void init(float (&y)[30], float (&)[30]) const {
+#pragma unroll
+    for (int i = 0; i < 30; ++i) y[i] = 0.f;
+  }
+  template <int Q>
+  __device__ __forceinline__ void chunk(size_t off, const float (&xh)[30], const float (&)[30], float (&y)[30],
+                                        float (&)[30]) const {
+    const float4 v = __ldcs(K + off);
+    entry<4 * Q + 0>(v.x, xh, y);
+    entry<4 * Q + 1>(v.y, xh, y);
+    entry<4 * Q + 2>(v.z, xh, y);
+    entry<4 * Q + 3>(v.w, xh, y);
+  }
+  template <int k>
+  __device__ __forceinline__ static void entry(float v, const float (&x)[30], float (&y)[30]) {
+    if constexpr (k < NPACK) {
+      constexpr int c = unpack_c(k), r = unpack_r(k);
+      y[r] += v * x[c];
+      if constexpr (r != c) y[c] += v * x[r];
+    }
+  }
+};
+
+struct OpF64 {   // native FP64 operator (plain path)
+  using acc_t = double;
+  static constexpr bool two_part = false;
+  static constexpr int V = 2;
+  static constexpr int NCH = 233;
+  const double2 *K;
+  __device__ __forceinline__ void init(double (&y)[30], double (&)[30]) const {
+#pragma unroll
+    for (int i = 0; i < 30; ++i) y[i] = 0.0;
+  }
+  template <int Q>
+  __device__ __forceinline__ void chunk(size_t off, const double (&xh)[30], const double (&)[30], double (&y)[30],
+                                        double (&)[30]) const {
+    const double2 v = __ldcs(K + off);
+    entry<2 * Q + 0>(v.x, xh, y);
+    entry<2 * Q + 1>(v.y, xh, y);
+  }
+  template <int k>
+  __device__ __forceinline__ static void entry(double v, const double (&x)[30], double (&y)[30]) {
+    if constexpr (k < NPACK) {
+      constexpr int c = unpack_c(k), r = unpack_r(k);
+      y[r] += v * x[c];
+      if constexpr (r != c) y[c] += v * x[r];
+    }
+  }
+};
+
+struct OpDF {    // double-float operator (mixed path, outer iterations)
+  using acc_t = float;
+  static constexpr bool two_part = true;
+  static constexpr int V = 4;
+  static constexpr int NCH = 117;
+  const float4 *Kh, *Kl;
+  __device__ __forceinline__ void init(float (&sh)[30], float (&sl)[30]) const {
+#pragma unroll
+    for (int i = 0; i < 30; ++i) { sh[i] = 0.f; sl[i] = 0.f; }
+  }
+  template <int Q>
+  __device__ __forceinline__ void chunk(size_t off, const float (&xh)[30], const float (&xl)[30], float (&sh)[30],
+                                        float (&sl)[30]) const {
+    const float4 h = __ldcs(Kh + off), l = __ldcs(Kl + off);
+    entry<4 * Q + 0>(h.x, l.x, xh, xl, sh, sl);
+    entry<4 * Q + 1>(h.y, l.y, xh, xl, sh, sl);
+    entry<4 * Q + 2>(h.z, l.z, xh, xl, sh, sl);
+    entry<4 * Q + 3>(h.w, l.w, xh, xl, sh, sl);
+  }
+  template <int k>
+  __device__ __forceinline__ static void entry(float vh, float vl, const float (&xh)[30], const float (&xl)[30],
+                                               float (&sh)[30], float (&sl)[30]) {
+    if constexpr (k < NPACK) {
+      constexpr int c = unpack_c(k), r = unpack_r(k);
+      df_mac(vh, vl, xh[c], xl[c], sh[r], sl[r]);
+      if constexpr (r != c) df_mac(vh, vl, xh[r], xl[r], sh[c], sl[c]);
+    }
+  }
+};
+
+template <class Op, int Q0, int... Is>
+__device__ __forceinline__ void run_chunks(const Op &op, int e, size_t nel, const typename Op::acc_t (&xh)[30],
+                                           const typename Op::acc_t (&xl)[30], typename Op::acc_t (&y)[30],
+                                           typename Op::acc_t (&yl)[30], std::integer_sequence<int, Is...>) {
+  (op.template chunk<Q0 + Is>((size_t)(Q0 + Is) * nel + e, xh, xl, y, yl), ...);
+}
+
+template <class Op, int P>
+__device__ __forceinline__ void run_part(const Op &op, int e, size_t nel, const typename Op::acc_t (&xh)[30],
+                                         const typename Op::acc_t (&xl)[30], typename Op::acc_t (&y)[30],
+                                         typename Op::acc_t (&yl)[30]) {
+  constexpr int b = (Op::NCH * P) / 4, en = (Op::NCH * (P + 1)) / 4;
+  run_chunks<Op, b>(op, e, nel, xh, xl, y, yl, std::make_integer_sequence<int, en - b>{});
+}
+
+template <class Op, typename XT>
+__global__ void __launch_bounds__(128) k_ebe_apply_split(Op op, const int *__restrict__ el2nod, int nel, int e_begin,
+                                                         int e_end, const XT *__restrict__ x, XT *__restrict__ y) {
+  using A = typename Op::acc_t;
+  __shared__ XT sY[4][30][33];
+  __shared__ int sNod[10][32];
+  const int lane = threadIdx.x & 31, part = threadIdx.x >> 5;
+  const int e0 = e_begin + blockIdx.x * 32;
+  const int e = e0 + lane;
+  const bool valid = e < e_end;
+  if (part == 0)
+#pragma unroll
+    for (int n = 0; n < 10; ++n) sNod[n][lane] = valid ? __ldg(el2nod + (size_t)n * nel + e) : 0;
+  __syncthreads();
+  A xh[30], xl[30], yh[30], yl[30];
+  op.init(yh, yl);
+  if (valid) {
+#pragma unroll
+    for (int n = 0; n < 10; ++n)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const XT xv = x[3 * sNod[n][lane] + c];
+        const A h = (A)xv;
+        xh[3 * n + c] = h;
+        xl[3 * n + c] = (A)(xv - (XT)h);
+      }
+    switch (part) {
+      case 0: run_part<Op, 0>(op, e, nel, xh, xl, yh, yl); break;
+      case 1: run_part<Op, 1>(op, e, nel, xh, xl, yh, yl); break;
+      case 2: run_part<Op, 2>(op, e, nel, xh, xl, yh, yl); break;
+      default: run_part<Op, 3>(op, e, nel, xh, xl, yh, yl); break;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 30; ++q) {
+    if constexpr (Op::two_part)
+      sY[part][q][lane] = (XT)yh[q] + (XT)yl[q];
+    else
+      sY[part][q][lane] = (XT)yh[q];
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < 30 * 32; o += 128) {
+    const int q = o >> 5, el = o & 31;
+    if (e0 + el >= e_end) continue;
+    const XT v = sY[0][q][el] + sY[1][q][el] + sY[2][q][el] + sY[3][q][el];
+    y[3 * sNod[q / 3][el] + q % 3] += v;
+  }
+}
+
+template <class Op, typename XT>
+static int ebe_apply_split(const Level &L, const Op &op, const XT *x, XT *y, cudaStream_t s) {
+  M3_CUDA(cudaMemsetAsync(y, 0, sizeof(XT) * L.ndof, s));
+  const int nc = (int)L.cstart.size() - 1;
+  for (int c = 0; c < nc; ++c) {
+    const int b = L.cstart[c], e = L.cstart[c + 1];
+    if (e <= b) continue;
+    k_ebe_apply_split<Op, XT><<<(e - b + 31) / 32, 128, 0, s>>>(op, L.el2nod, L.nel, b, e, x, y); count_launch();
+  }
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+int ebe_apply_split_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
+  return ebe_apply_split(L, OpF32{reinterpret_cast<const float4 *>(K)}, x, y, s);
+}
+int ebe_apply_split_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s) {
+  return ebe_apply_split(L, OpF64{reinterpret_cast<const double2 *>(K)}, x, y, s);
+}
+int ebe_apply_split_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s) {
+  return ebe_apply_split(L, OpDF{reinterpret_cast<const float4 *>(Kh), reinterpret_cast<const float4 *>(Kl)}, x, y, s);
 }
 
 template <typename T>

@@ -24,6 +24,9 @@ namespace m3sph {
 int launch_element_setup(const SetupArgs &a, cudaStream_t s);
 template <typename T> int ebe_apply(const Level &L, const T *K, const T *x, T *y, cudaStream_t s);
 int ebe_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
+int ebe_apply_split_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s);
+int ebe_apply_split_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
+int ebe_apply_split_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
 int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
 template <typename T> int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s);
 int grad_apply(const Level &L, const double *G, const double *q, double *y, cudaStream_t s);
@@ -785,8 +788,11 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
 // double-float FP32 arithmetic on the mixed path
 static int outer_apply(m3sph_mesh *M, const double *x, double *y) {
   Level &L0 = M->lev[0];
-  if (M->precision == 1 && M->df_outer) return ebe_apply_df(L0, L0.K32, L0.KL32, x, y, M->stream);
-  return ebe_apply<double>(L0, L0.K64, x, y, M->stream);
+  if (M->precision == 1 && M->df_outer)
+    return M->split_apply ? ebe_apply_split_df(L0, L0.K32, L0.KL32, x, y, M->stream)
+                          : ebe_apply_df(L0, L0.K32, L0.KL32, x, y, M->stream);
+  return M->split_apply ? ebe_apply_split_f64(L0, L0.K64, x, y, M->stream)
+                        : ebe_apply<double>(L0, L0.K64, x, y, M->stream);
 }
 
 // ======================================================================================
@@ -803,9 +809,17 @@ template <> const double *levB<double>(const Level &L) { return L.B64; }
 template <> const float *levB<float>(const Level &L) { return L.B32; }
 
 // level operator: element-by-element on the finest level, assembled blocks on coarse levels
+static bool g_split_apply = true;
+static int split_apply_T(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
+  return ebe_apply_split_f32(L, K, x, y, s);
+}
+static int split_apply_T(const Level &L, const double *K, const double *x, double *y, cudaStream_t s) {
+  return ebe_apply_split_f64(L, K, x, y, s);
+}
 template <typename T>
 static int level_op(const Level &L, int img, const T *x, T *y, cudaStream_t s) {
   if (img > 0 && levB<T>(L)) return bsr_apply<T>(L, levB<T>(L), x, y, s);
+  if (g_split_apply) return split_apply_T(L, levK<T>(L), x, y, s);
   return ebe_apply<T>(L, levK<T>(L), x, y, s);
 }
 
@@ -1508,22 +1522,32 @@ extern "C" int m3sph_apply_timing(m3sph_mesh *M, int32_t img, int32_t precision,
   Level &L = M->lev[img];
   Work *W = get_work(M);
   cudaStream_t s = M->stream;
-  const bool f32 = precision != 0;
-  if ((f32 && !L.K32) || (!f32 && !L.K64)) {
+  const bool f32 = precision == 1;
+  if ((f32 && !L.K32 && !L.B32) || (!f32 && !L.K64 && !L.B64)) {
     set_error("no element matrices of that precision on this level");
     return M3SPH_ERR_BAD_INPUT;
   }
   cudaEvent_t e0, e1;
   M3_CUDA(cudaEventCreate(&e0));
   M3_CUDA(cudaEventCreate(&e1));
-  // warm-up
-  if (f32) M3_TRY(ebe_apply<float>(L, L.K32, W->r32[img], W->kd32[img], s));
-  else M3_TRY(ebe_apply<double>(L, L.K64, W->r64[img], W->kd64[img], s));
+  // precision 0: FP64 operator, 1: FP32 operator, 2: double-float outer operator (finest level)
+  auto run = [&]() -> int {
+    if (precision == 2 && img == 0) {
+      const bool old = M->df_outer;
+      const int oldp = M->precision;
+      M->df_outer = true;
+      M->precision = 1;
+      const int st = outer_apply(M, W->r64[0], W->kd64[0]);
+      M->df_outer = old;
+      M->precision = oldp;
+      return st;
+    }
+    if (f32) return level_op<float>(L, img, W->r32[img], W->kd32[img], s);
+    return level_op<double>(L, img, W->r64[img], W->kd64[img], s);
+  };
+  M3_TRY(run());
   M3_CUDA(cudaEventRecord(e0, s));
-  for (int i = 0; i < nrep; ++i) {
-    if (f32) M3_TRY(ebe_apply<float>(L, L.K32, W->r32[img], W->kd32[img], s));
-    else M3_TRY(ebe_apply<double>(L, L.K64, W->r64[img], W->kd64[img], s));
-  }
+  for (int i = 0; i < nrep; ++i) M3_TRY(run());
   M3_CUDA(cudaEventRecord(e1, s));
   M3_CUDA(cudaEventSynchronize(e1));
   float ms = 0.f;
@@ -1531,5 +1555,26 @@ extern "C" int m3sph_apply_timing(m3sph_mesh *M, int32_t img, int32_t precision,
   *ms_per_apply = ms / nrep;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) {
+  if (!M || !name) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  const std::string n(name);
+  if (n == "split_apply") {
+    M->split_apply = value != 0;
+    g_split_apply = value != 0;
+  } else if (n == "graphs") {
+    M->use_graphs = value != 0;
+  } else if (n == "df_outer") {
+    M->df_outer = value != 0;
+  } else {
+    set_error("unknown option " + n);
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  clear_graphs(M);
   return M3SPH_OK;
 }

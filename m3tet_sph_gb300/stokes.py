@@ -171,6 +171,9 @@ class DeviceMesh:
         L.check(L.lib().m3sph_solution(self.h, L.dptr(U), L.dptr(P)))
         return U, P
 
+    def set_option(self, name, value):
+        L.check(L.lib().m3sph_set_option(self.h, name.encode(), int(value)))
+
     def apply_timing(self, img=0, precision=1, nrep=10):
         ms = C.c_double()
         L.check(L.lib().m3sph_apply_timing(self.h, img, precision, nrep, C.byref(ms)))

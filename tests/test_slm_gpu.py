@@ -59,7 +59,7 @@ def test_tsearch_known_elements(mesh_case):
     w, dm, loc = mesh_case
     f = w['levels'][0]
     rng = np.random.default_rng(3)
-    els0 = rng.choice(f['nel'], 5000, replace=False)
+    els0 = rng.choice(f['nel'], min(5000, f['nel']), replace=False)
     lc0 = rng.dirichlet([3, 3, 3, 3], size=len(els0)).T[:3]
     N, _ = SO.sf10(*lc0)
     X = np.einsum('in,kni->kn', N, f['GCOORD'][:, f['EL2NOD'][els0]])
@@ -129,4 +129,8 @@ def test_pc2_advection_parity(mesh_case):
         agree = np.mean(WS['els_INTERP'] - 1 == e2)
         assert agree > 0.995, agree
         same = WS['els_INTERP'] - 1 == e2
-        assert np.abs(Tg[same] - Tr[same]).max() < 1e-9, method
+        # T in [0,1]; differences come from local coordinates in isoparametric elements, where
+        # both sides stop Newton at the reference's 1e-8 tolerance
+        iso = f['cls'][np.maximum(e2, 0)] == 3
+        assert np.abs(Tg[same & ~iso] - Tr[same & ~iso]).max() < 1e-9, method
+        assert np.abs(Tg[same] - Tr[same]).max() < 1e-6, method

@@ -55,8 +55,10 @@ def test_element_matrices_parity(case):
     assert np.abs(Mg - Mm).max() < 1e-12 * np.abs(Mm).max()
 
 
-def test_operator_apply_parity(case):
+@pytest.mark.parametrize("split", [1, 0])
+def test_operator_apply_parity(case, split):
     w, S, dm = case
+    dm.set_option("split_apply", split)
     rng = np.random.default_rng(1)
     x = rng.standard_normal(S.nU)
     m = _free(S)
@@ -69,6 +71,7 @@ def test_operator_apply_parity(case):
     x2 = x.copy()
     x2[~m] = 1e3
     assert np.linalg.norm(dm.apply(x2) - y) < 1e-13 * np.linalg.norm(y_ref)
+    dm.set_option("split_apply", 1)
 
 
 def test_grad_div_force_parity(case):
@@ -172,8 +175,11 @@ def test_mixed_operators_parity(case):
         x[S.ifree] = rng.standard_normal(len(S.ifree))
         y_ref = np.zeros(S.nU)
         y_ref[S.ifree] = S.K1 @ x[S.ifree]
-        y = dm2.apply(x)
-        assert np.linalg.norm(y - y_ref) < 1e-12 * np.linalg.norm(y_ref)
+        for split in (1, 0):
+            dm2.set_option("split_apply", split)
+            y = dm2.apply(x)
+            assert np.linalg.norm(y - y_ref) < 1e-12 * np.linalg.norm(y_ref)
+        dm2.set_option("split_apply", 1)
         ifree_c = S.ifree[S.ifree < 3 * w['levels'][1]['nnod']]
         xc = np.zeros(3 * w['levels'][1]['nnod'])
         xc[ifree_c] = rng.standard_normal(len(ifree_c))
