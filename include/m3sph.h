@@ -62,7 +62,8 @@ typedef struct m3sph_mesh m3sph_mesh;   /* opaque: device-resident MESH + MG hie
 
 /* Semi-Lagrangian options (OPTS_SLM, default_numerics_M3TET.m:141-158). */
 typedef struct m3sph_slm_opts {
-  int32_t method_BT;      /* 1: PC2 predictor-corrector (the reference default) */
+  int32_t method_BT;      /* 1: PC2 predictor-corrector (the reference default); 2: RK4 over 3
+                             substeps (the reference's RK4 is an error stub, advect3d_slm_p_sph.m:103) */
   int32_t method_interp;  /* 0: 'quadratic' (interp3d_tet), 1: 'cubic' (interp3d_cubic_p) */
   int32_t monotonic;      /* clamp to the element's nodal min/max */
   int32_t method_wght;    /* cubic gradient weights: 0 'ones', 1 'dist' */
@@ -143,6 +144,28 @@ M3SPH_API int m3sph_stokes_step_device(m3sph_mesh *mesh, const m3sph_opts *opts,
 M3SPH_API int m3sph_solution(m3sph_mesh *mesh, double *U_xyz, double *P);
 /* The CUDA stream (cudaStream_t) the handle launches its kernels on. */
 M3SPH_API int m3sph_stream(m3sph_mesh *mesh, void **stream);
+
+/* Learned element smoother (no counterpart in the reference: M3TET_SPH smooths with weighted
+ * Jacobi only). A 52-128-30 MLP (BF16 tensor cores, FP32 accumulation) replaces Jacobi sweeps on
+ * the two finest levels when m3sph_opts.smoother = 1 and trained weights are loaded; the outer
+ * FP64 CG falls back to Jacobi when its contraction factor exceeds 0.95.
+ * Parameters are a flat FP32 vector of m3sph_ml_nparam() values: W1 [128][64] (input columns
+ * >= 52 are zero), b1 [128], W2 [32][128] (rows >= 30 zero), b2 [32]. */
+M3SPH_API int m3sph_ml_nparam(int32_t *n);
+M3SPH_API int m3sph_ml_set_params(m3sph_mesh *mesh, const float *params, int32_t trained);
+M3SPH_API int m3sph_ml_get_params(m3sph_mesh *mesh, float *params);
+/* Training data: reserve room for `capacity` samples, then append (local residual, local error)
+ * pairs of the current operator: a seeded random right-hand side is solved with the plain
+ * multigrid to 1e-10 and every `stride`-th element of n_iterates plain-multigrid iterates
+ * contributes one sample. */
+M3SPH_API int m3sph_ml_reserve(m3sph_mesh *mesh, int64_t capacity);
+M3SPH_API int m3sph_ml_collect(m3sph_mesh *mesh, uint64_t seed, int32_t n_iterates, int32_t stride, int64_t *count);
+/* One Adam epoch over the shuffled samples (batch a multiple of 64); mse = mean squared error. */
+M3SPH_API int m3sph_ml_train_epoch(m3sph_mesh *mesh, int32_t batch, float lr, uint64_t seed, double *mse);
+/* Gradient of the MSE loss (flat layout, same as the parameters) and forward outputs on caller
+ * rows X (n x 64 FP32, rounded to BF16), targets T (n x 32): for checks against a CPU autograd. */
+M3SPH_API int m3sph_ml_gradients(m3sph_mesh *mesh, const float *X, const float *T, int32_t n, float *grad, double *loss);
+M3SPH_API int m3sph_ml_forward(m3sph_mesh *mesh, const float *X, int32_t n, float *Y);
 
 /* Kernel-variant switches for measurement and tests: "split_apply" (4-warp split element
  * kernels, default 1), "graphs" (CUDA-graph replay of MG-PCG iterations, default 1),

@@ -92,6 +92,14 @@ SIGNATURES = {
     "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_interp3d_cubic": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_advect_slm": ([P, DP, DP, DP, DP, C.c_double, C.POINTER(SlmOpts), IP, IP, C.POINTER(LocateInfo)], C.c_int),
+    "m3sph_ml_nparam": ([IP], C.c_int),
+    "m3sph_ml_set_params": ([P, C.POINTER(C.c_float), C.c_int32], C.c_int),
+    "m3sph_ml_get_params": ([P, C.POINTER(C.c_float)], C.c_int),
+    "m3sph_ml_reserve": ([P, C.c_int64], C.c_int),
+    "m3sph_ml_collect": ([P, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_int64)], C.c_int),
+    "m3sph_ml_train_epoch": ([P, C.c_int32, C.c_float, C.c_uint64, DP], C.c_int),
+    "m3sph_ml_gradients": ([P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float), DP], C.c_int),
+    "m3sph_ml_forward": ([P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float)], C.c_int),
     "m3sph_set_option": ([P, C.c_char_p, C.c_int32], C.c_int),
     "m3sph_launch_count": ([C.POINTER(C.c_ulonglong)], C.c_int),
     "m3sph_apply_timing": ([P, C.c_int32, C.c_int32, C.c_int32, DP], C.c_int),
@@ -149,3 +157,8 @@ def launch_count():
     n = C.c_ulonglong(0)
     check(lib().m3sph_launch_count(C.byref(n)))
     return n.value
+
+
+def fptr(a):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_float))

@@ -63,12 +63,13 @@ def advect3d_slm_p_sph(MESH, COMM, Ux, Uy, Uz, T, dt, OPTS_SLM=None, WS_SLM=None
     WS_SLM = dict(WS_SLM or {})
     dm = _dm(MESH)
     n = dm.nnod
-    o = L.SlmOpts(method_BT=1, method_interp=1 if OPTS_SLM.get('method_interp', 'quadratic') == 'cubic' else 0,
+    bt = OPTS_SLM.get('method_BT', 'PC2')
+    if bt not in ('PC2', 'RK4'):
+        raise NotImplementedError("method_BT must be 'PC2' or 'RK4' (3 substeps)")
+    o = L.SlmOpts(method_BT=1 if bt == 'PC2' else 2, method_interp=1 if OPTS_SLM.get('method_interp', 'quadratic') == 'cubic' else 0,
                   monotonic=int(OPTS_SLM.get('monotonic', 1)),
                   method_wght=1 if OPTS_SLM.get('method_wght', 'dist') == 'dist' else 0,
                   r_cmb=MESH.get('r_cmb', 3480.0), r_surf=MESH.get('r_surf', 6371.0))
-    if OPTS_SLM.get('method_BT', 'PC2') != 'PC2':
-        raise NotImplementedError("only PC2 backtracking is available (the reference's RK4 is an error stub)")
     Tn = np.ascontiguousarray(T, dtype=np.float64).copy()
     elsBT = np.ascontiguousarray(WS_SLM.get('els_BT', np.zeros(n, np.int32)), dtype=np.int32).copy()
     elsIN = np.zeros(n, np.int32)

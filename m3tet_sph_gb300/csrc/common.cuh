@@ -141,6 +141,21 @@ struct SetupArgs {
 };
 
 int slm_build(m3sph_mesh *M, const m3sph_level &f0);
+int ml_build(m3sph_mesh *M);
+int ml_features(m3sph_mesh *M, const double *h_visc);
+template <typename T> int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *tmp, T *d);
+int ml_init_kernels();
+bool ml_ready(m3sph_mesh *M);
+int ml_add_samples(m3sph_mesh *M, const double *r, const double *err, int stride, int offset);
+int ml_reserve(m3sph_mesh *M, long cap);
+int ml_set_params(m3sph_mesh *M, const float *h);
+int ml_get_params(m3sph_mesh *M, float *h);
+int ml_epoch(m3sph_mesh *M, int batch, float lr, unsigned long long seed, double *mse);
+int ml_gradients(m3sph_mesh *M, const float *hX, const float *hT, int n, float *hgrad, double *loss);
+int ml_forward(m3sph_mesh *M, const float *hX, int n, float *hY);
+int ml_nparam();
+long ml_count(m3sph_mesh *M);
+void ml_mark_trained(m3sph_mesh *M, bool t);
 
 }  // namespace m3sph
 
@@ -169,6 +184,12 @@ struct m3sph_mesh {
   bool df_outer = true;               // double-float outer operator on the mixed path
   bool split_apply = true;            // 4-warp split element-by-element kernels on the finest level
   unsigned long long graph_kernels = 0;   // kernel launches per captured iteration
+  void *ml = nullptr;                 // learned smoother state
+  void (*ml_free)(void *) = nullptr;
+  int smoother = 0;                   // 0 Jacobi, 1 learned smoother on the two finest levels
+  bool smoother_active = false;       // learned smoother in use for the current solve
+  int smoother_fallbacks = 0;
+  double r_min = 0.0, r_max = 0.0;    // shell radii (features)
   void *slm = nullptr;                // advection / point-location state
   void (*slm_free)(void *) = nullptr;
   double *red = nullptr;              // reduction partials

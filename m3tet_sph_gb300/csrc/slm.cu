@@ -498,6 +498,49 @@ __global__ void k_corrector(const double *__restrict__ X, const double *__restri
   P[i] = th; P[nnod + i] = ph; P[2 * nnod + i] = r;
 }
 
+// RK4 backtracking (no working counterpart in the reference: advect3d_slm_p_sph.m:103-104 stops
+// with 'RK4 is not working for spherical coordinates'). Each substep of length h integrates
+// dx/dt = U(x) backwards in Cartesian coordinates with the classical RK4 weights; every stage
+// point is moved radially into [r_cmb + tol, r_surf - tol] (find_pts_outside_domain_sph.m rule)
+// before it is located and U is interpolated there.
+__global__ void k_rk_point(const double *__restrict__ Xc, const double *__restrict__ k, int n, double c, double r_cmb,
+                           double r_surf, double *__restrict__ P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = Xc[i] - c * k[i], y = Xc[n + i] - c * k[n + i], z = Xc[2 * n + i] - c * k[2 * n + i];
+  double th, ph, r;
+  c2s(x, y, z, th, ph, r);
+  const double rtol = 1e-12 * (r_surf - r_cmb);
+  if (r <= r_cmb + rtol) r = r_cmb + rtol;
+  if (r >= r_surf - rtol) r = r_surf - rtol;
+  P[i] = th; P[n + i] = ph; P[2 * n + i] = r;
+}
+// acc = (first ? 0 : acc) + w * k
+__global__ void k_rk_accum(double *__restrict__ acc, const double *__restrict__ k, int n3, double w, int first) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  acc[i] = (first ? 0.0 : acc[i]) + w * k[i];
+}
+// Xc -= h/6 acc, radius clamped
+__global__ void k_rk_update(double *__restrict__ Xc, const double *__restrict__ acc, int n, double h, double r_cmb,
+                            double r_surf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = Xc[i] - h / 6.0 * acc[i], y = Xc[n + i] - h / 6.0 * acc[n + i], z = Xc[2 * n + i] - h / 6.0 * acc[2 * n + i];
+  const double r = sqrt(x * x + y * y + z * z);
+  const double rtol = 1e-12 * (r_surf - r_cmb);
+  const double rc = fmin(fmax(r, r_cmb + rtol), r_surf - rtol);
+  const double f = rc / r;
+  Xc[i] = x * f; Xc[n + i] = y * f; Xc[2 * n + i] = z * f;
+}
+__global__ void k_cart_to_sph(const double *__restrict__ Xc, int n, double *__restrict__ P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double th, ph, r;
+  c2s(Xc[i], Xc[n + i], Xc[2 * n + i], th, ph, r);
+  P[i] = th; P[n + i] = ph; P[2 * n + i] = r;
+}
+
 // ======================================================================================
 // host side
 // ======================================================================================
@@ -509,6 +552,7 @@ struct SlmState {
   // work
   double *P = nullptr, *lc = nullptr, *V = nullptr, *out = nullptr, *upu = nullptr, *rpu = nullptr, *U = nullptr;
   double *gel = nullptr, *wel = nullptr, *gn = nullptr, *wn = nullptr;
+  double *Xc = nullptr, *kk = nullptr, *acc = nullptr;   // RK4 point, stage slope, weighted sum
   int *els = nullptr, *guess = nullptr, *todo = nullptr;
   uint8_t *status = nullptr;
   size_t cap = 0;
@@ -542,7 +586,8 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
     for (void *q : {(void *)S->el2nod, (void *)S->nbr, (void *)S->v2e_ptr, (void *)S->v2e, (void *)S->node_guess,
                     (void *)S->cls, (void *)S->S0, (void *)S->SZ, (void *)S->SX, (void *)S->P, (void *)S->lc,
                     (void *)S->V, (void *)S->out, (void *)S->upu, (void *)S->rpu, (void *)S->U, (void *)S->gel,
-                    (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->els, (void *)S->guess,
+                    (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->Xc, (void *)S->kk, (void *)S->acc,
+                    (void *)S->els, (void *)S->guess,
                     (void *)S->todo, (void *)S->status})
       if (q) cudaFree(q);
     delete S;
@@ -637,7 +682,9 @@ static int slm_reserve(SlmState *S, size_t npt, int nel, int nnod, int nv) {
     return st;
   if (!S->gel) {
     if ((st = sl_alloc(&S->gel, 3 * (size_t)nel)) || (st = sl_alloc(&S->wel, 4 * (size_t)nel)) ||
-        (st = sl_alloc(&S->gn, 3 * (size_t)nv)) || (st = sl_alloc(&S->wn, (size_t)nv)))
+        (st = sl_alloc(&S->gn, 3 * (size_t)nv)) || (st = sl_alloc(&S->wn, (size_t)nv)) ||
+        (st = sl_alloc(&S->Xc, 3 * (size_t)nnod)) || (st = sl_alloc(&S->kk, 3 * (size_t)nnod)) ||
+        (st = sl_alloc(&S->acc, 3 * (size_t)nnod)))
       return st;
   }
   S->cap = n;
@@ -861,6 +908,58 @@ static int advect_device(m3sph_mesh *M, double dt, const m3sph_slm_opts *o, bool
   return M3SPH_OK;
 }
 
+static void add_info(m3sph_locate_info &a, const m3sph_locate_info &b) {
+  a.npt += b.npt; a.nwalk += b.nwalk; a.nties += b.nties; a.ngap += b.ngap; a.nbrute += b.nbrute; a.nlost += b.nlost;
+}
+
+static int advect_device_rk4(m3sph_mesh *M, double dt, const m3sph_slm_opts *o, int nsub, bool use_ws,
+                             m3sph_locate_info *info) {
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  const int n = L0.nnod;
+  const unsigned gb = (unsigned)((n + 127) / 128), gb3 = (unsigned)((3 * n + 127) / 128);
+  const double h = dt / nsub;
+  const double cst[4] = {0.0, 0.5, 0.5, 1.0}, wst[4] = {1.0, 2.0, 2.0, 1.0};
+  m3sph_locate_info tot{};
+  M3_CUDA(cudaMemcpyAsync(S->Xc, M->fin.gcoord, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+  bool have_guess = use_ws;
+  for (int sub = 0; sub < nsub; ++sub) {
+    for (int st = 0; st < 4; ++st) {
+      if (sub == 0 && st == 0) {
+        M3_CUDA(cudaMemcpyAsync(S->kk, S->U, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+      } else {
+        // stage point x - c h k_prev (k_prev in kk), located and U interpolated there
+        // stage 0 of later substeps: U at the new point (c = 0)
+        k_rk_point<<<gb, 128, 0, s>>>(S->Xc, S->kk, n, cst[st] * h, o->r_cmb, o->r_surf, S->P); count_launch();
+        m3sph_locate_info li{};
+        M3_TRY(slm_locate(M, S, n, have_guess, true, true, &li));
+        add_info(tot, li);
+        M3_CUDA(cudaMemcpyAsync(S->guess, S->els, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+        have_guess = true;
+        k_interp_p2<<<gb, 128, 0, s>>>(S->view, S->els, S->lc, n, S->U, 3, 0, S->kk); count_launch();
+      }
+      k_rk_accum<<<gb3, 128, 0, s>>>(S->acc, S->kk, 3 * n, wst[st], st == 0); count_launch();
+    }
+    k_rk_update<<<gb, 128, 0, s>>>(S->Xc, S->acc, n, h, o->r_cmb, o->r_surf); count_launch();
+  }
+  // departure points -> T
+  k_cart_to_sph<<<gb, 128, 0, s>>>(S->Xc, n, S->P); count_launch();
+  m3sph_locate_info li{};
+  M3_TRY(slm_locate(M, S, n, true, true, true, &li));
+  add_info(tot, li);
+  if (o->method_interp == 1) {
+    M3_TRY(slm_cubic_gradients(M, S, S->V, o->method_wght));
+    k_cubic_interp<<<gb, 128, 0, s>>>(S->view, M->fin.gcoord, S->els, S->lc, n, S->V, S->gn, S->wn, S->gel,
+                                      o->monotonic, S->out); count_launch();
+  } else {
+    k_interp_p2<<<gb, 128, 0, s>>>(S->view, S->els, S->lc, n, S->V, 1, o->monotonic, S->out); count_launch();
+  }
+  M3_CUDA(cudaGetLastError());
+  if (info) *info = tot;
+  return M3SPH_OK;
+}
+
 extern "C" int m3sph_advect_slm(m3sph_mesh *M, const double *Ux, const double *Uy, const double *Uz, double *T,
                                 double dt, const m3sph_slm_opts *o, int32_t *els_BT, int32_t *els_INTERP,
                                 m3sph_locate_info *info) {
@@ -870,8 +969,8 @@ extern "C" int m3sph_advect_slm(m3sph_mesh *M, const double *Ux, const double *U
     set_error("m3sph_advect_slm: bad arguments");
     return M3SPH_ERR_BAD_INPUT;
   }
-  if (o->method_BT != 1) {
-    set_error("m3sph_advect_slm: only PC2 backtracking (method_BT = 1) is implemented");
+  if (o->method_BT != 1 && o->method_BT != 2) {
+    set_error("m3sph_advect_slm: method_BT must be 1 (PC2) or 2 (RK4, 3 substeps)");
     return M3SPH_ERR_BAD_INPUT;
   }
   SlmState *S = slm_state(M);
@@ -896,7 +995,11 @@ extern "C" int m3sph_advect_slm(m3sph_mesh *M, const double *Ux, const double *U
       M3_CUDA(cudaMemcpyAsync(S->guess, g.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     }
   }
-  M3_TRY(advect_device(M, dt, o, use_ws, info));
+  if (o->method_BT == 2) {
+    M3_TRY(advect_device_rk4(M, dt, o, 3, use_ws, info));
+  } else {
+    M3_TRY(advect_device(M, dt, o, use_ws, info));
+  }
   std::vector<int> e(n);
   M3_CUDA(cudaMemcpyAsync(T, S->out, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaMemcpyAsync(e.data(), S->els, sizeof(int) * n, cudaMemcpyDeviceToHost, s));

@@ -432,6 +432,7 @@ extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
   clear_graphs(M);
   if (M->wk && M->wk_free) M->wk_free(M->wk);
   if (M->slm && M->slm_free) M->slm_free(M->slm);
+  if (M->ml && M->ml_free) M->ml_free(M->ml);
   if (M->stream) cudaStreamDestroy(M->stream);
   delete M;
   return M3SPH_OK;
@@ -546,6 +547,17 @@ extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "mesh upload"));
   st = slm_build(M, f0);
   if (st) return fail(st);
+  {
+    double rmin = 1e300, rmax = 0.0;
+    for (int n = 0; n < nnod; ++n) {
+      const double r = f0.GCOORD_SPH[3 * (size_t)n + 2];
+      rmin = std::min(rmin, r);
+      rmax = std::max(rmax, r);
+    }
+    M->r_min = rmin;
+    M->r_max = rmax;
+  }
+  if ((st = ml_build(M)) || (st = ml_init_kernels())) return fail(st);
   *out = M;
   return M3SPH_OK;
 }
@@ -563,8 +575,8 @@ extern "C" int m3sph_mesh_ncolors(const m3sph_mesh *M, int32_t img, int32_t *nc)
 namespace {
 struct Work {
   // per level T vectors for the V-cycle
-  std::vector<double *> r64, d64, kd64;
-  std::vector<float *> r32, d32, kd32;
+  std::vector<double *> r64, d64, kd64, t64;
+  std::vector<float *> r32, d32, kd32, t32;
   double *cwork64 = nullptr;
   float *cwork32 = nullptr;
   // outer vectors (level 0, fp64)
@@ -583,12 +595,13 @@ static int alloc_work(m3sph_mesh *M) {
   M->wk = W;
   M->wk_free = [](void *p) { delete reinterpret_cast<Work *>(p); };
   const int nmg = M->nmg;
-  W->r64.resize(nmg); W->d64.resize(nmg); W->kd64.resize(nmg);
-  W->r32.resize(nmg); W->d32.resize(nmg); W->kd32.resize(nmg);
+  W->r64.resize(nmg); W->d64.resize(nmg); W->kd64.resize(nmg); W->t64.resize(nmg);
+  W->r32.resize(nmg); W->d32.resize(nmg); W->kd32.resize(nmg); W->t32.resize(nmg);
   for (int i = 0; i < nmg; ++i) {
     const size_t n = M->lev[i].ndof;
     M3_TRY(dalloc(&W->r64[i], n)); M3_TRY(dalloc(&W->d64[i], n)); M3_TRY(dalloc(&W->kd64[i], n));
     M3_TRY(dalloc(&W->r32[i], n)); M3_TRY(dalloc(&W->d32[i], n)); M3_TRY(dalloc(&W->kd32[i], n));
+    M3_TRY(dalloc(&W->t64[i], n)); M3_TRY(dalloc(&W->t32[i], n));
   }
   const size_t nc = M->lev[nmg - 1].ndof;
   M3_TRY(dalloc(&W->cwork64, 2 * nc));
@@ -603,6 +616,7 @@ static int alloc_work(m3sph_mesh *M) {
   auto reg = [&](void *p) { M->work.push_back(p); };
   for (int i = 0; i < nmg; ++i) {
     reg(W->r64[i]); reg(W->d64[i]); reg(W->kd64[i]); reg(W->r32[i]); reg(W->d32[i]); reg(W->kd32[i]);
+    reg(W->t64[i]); reg(W->t32[i]);
   }
   for (void *p : {(void *)W->cwork64, (void *)W->cwork32, (void *)W->r, (void *)W->d, (void *)W->q, (void *)W->Kq,
                   (void *)W->tmp, (void *)W->U, (void *)W->z, (void *)W->y, (void *)W->Rhs, (void *)W->pr,
@@ -764,6 +778,7 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   }
   (void)nfree;
   M->phys = *phys;
+  M3_TRY(ml_features(M, Visc));
   M3_CUDA(cudaStreamSynchronize(s));
   dfree(d_fix);
   dfree(d_vals);
@@ -828,22 +843,35 @@ template <> const double *levDi<double>(const Level &L) { return L.Dinv64; }
 template <> const float *levDi<float>(const Level &L) { return L.Dinv32; }
 
 template <typename T>
-static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std::vector<T *> &kd, const T *Ainv) {
+static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std::vector<T *> &kd,
+                    std::vector<T *> &tmp, const T *Ainv) {
   cudaStream_t s = M->stream;
   const int nm = M->nmg;
   if (nm == 1) {
     M3_TRY(dense_gemv<T>(Ainv, M->coarse.n, r[0], M->lev[0].freemask, d[0], s));
     return M3SPH_OK;
   }
+  const bool ml = M->smoother_active;
   for (int j = 0; j < nm - 1; ++j) {
     const Level &L = M->lev[j];
     const double *w = j == 0 ? WD0 : WDc;
     const size_t n = L.ndof;
-    M3_TRY(jac_first<T>((T)w[0], r[j], levDi<T>(L), d[j], n, s));
-    M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
-    for (int k = 1; k < 3; ++k) {
-      M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
+    if (ml && j < 2) {
+      // learned sweep, weighted Jacobi sweep, learned sweep
+      M3_CUDA(cudaMemsetAsync(d[j], 0, sizeof(T) * n, s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], nullptr, levDi<T>(L), tmp[j], d[j]));
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      M3_TRY(jac<T>((T)w[1], r[j], kd[j], levDi<T>(L), d[j], n, s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+    } else {
+      M3_TRY(jac_first<T>((T)w[0], r[j], levDi<T>(L), d[j], n, s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      for (int k = 1; k < 3; ++k) {
+        M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
+        M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      }
     }
     M3_TRY(restrict_<T>(L, M->lev[j + 1], r[j], kd[j], r[j + 1], s));
   }
@@ -853,9 +881,18 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     const double *w = j == 0 ? WU0 : WUc;
     const size_t n = L.ndof;
     M3_TRY(prolong<T>(L, M->lev[j + 1], d[j + 1], d[j], d[j], s));
-    for (int k = 0; k < 3; ++k) {
+    if (ml && j < 2) {
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
-      M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      M3_TRY(jac<T>((T)w[1], r[j], kd[j], levDi<T>(L), d[j], n, s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
+    } else {
+      for (int k = 0; k < 3; ++k) {
+        M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+        M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
+      }
     }
   }
   return M3SPH_OK;
@@ -870,10 +907,10 @@ static int vcycle(m3sph_mesh *M, const double *r, double *dout) {
     std::vector<double *> rr = W->r64, dd = W->d64;
     rr[0] = const_cast<double *>(r);
     dd[0] = dout;
-    return vcycle_T<double>(M, rr, dd, W->kd64, M->coarse.A64);
+    return vcycle_T<double>(M, rr, dd, W->kd64, W->t64, M->coarse.A64);
   }
   M3_TRY(d2f(r, W->r32[0], n0, s));
-  M3_TRY(vcycle_T<float>(M, W->r32, W->d32, W->kd32, M->coarse.A32));
+  M3_TRY(vcycle_T<float>(M, W->r32, W->d32, W->kd32, W->t32, M->coarse.A32));
   M3_TRY(f2d(W->d32[0], dout, n0, s));
   return M3SPH_OK;
 }
@@ -922,8 +959,9 @@ static int cg_iteration(m3sph_mesh *M, double *x) {
 
 // the iteration captured once per solution-vector pointer as a CUDA graph and replayed
 static int iteration_graph(m3sph_mesh *M, double *x, cudaGraphExec_t *out) {
+  double *key = M->smoother_active ? x + 1 : x;   // separate graphs with / without the learned smoother
   for (auto &g : M->graphs)
-    if (g.first == x) {
+    if (g.first == key) {
       *out = g.second;
       return M3SPH_OK;
     }
@@ -943,7 +981,7 @@ static int iteration_graph(m3sph_mesh *M, double *x, cudaGraphExec_t *out) {
   ce = cudaGraphInstantiate(&exec, graph, 0);
   cudaGraphDestroy(graph);
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
-  M->graphs.push_back({x, exec});
+  M->graphs.push_back({key, exec});
   *out = exec;
   return M3SPH_OK;
 }
@@ -985,12 +1023,21 @@ static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs
     }
     st.nvc++;
     M3_TRY(read_scal(M, 3, rr));
+    const double rrms_prev = rrms;
     rrms = std::sqrt(rr) / sq;
     if (std::isnan(rrms)) {
       set_error("NaN in MG-PCG residual");
       return M3SPH_ERR_NAN;
     }
     if (rrms < tol) break;
+    // learned-smoother fallback: a contraction factor above 0.95 (or growth) switches the rest of
+    // the solve to the Jacobi smoother
+    if (M->smoother_active && it > 1 && rrms > 0.95 * rrms_prev) {
+      M->smoother_active = false;
+      M->smoother_fallbacks++;
+      exec = nullptr;
+      if (M->use_graphs) M3_TRY(iteration_graph(M, x, &exec));
+    }
   }
   st.it = std::min(it, itmax);
   st.rrms = rrms;
@@ -1102,6 +1149,8 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   Level &L0 = M->lev[0];
   const size_t n = L0.ndof;
   const int np = L0.nvnod;
+  M->smoother_active = opts->smoother == 1 && ml_ready(M);
+  M->smoother_fallbacks = 0;
   double rtol_Pat = opts->rtol_Pat > 0 ? opts->rtol_Pat : 1e-4;
   double rtol_U = opts->rtol_U > 0 ? opts->rtol_U : 5e-3;
   const int itmax_Pat = opts->itmax_Pat > 0 ? opts->itmax_Pat : 120;
@@ -1212,6 +1261,8 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   inf.nitU += cs.it;
   inf.itPat = std::min(itPat, itmax_Pat);
   inf.norm_rP = norm_rP;
+  inf.smoother_fallbacks = M->smoother_fallbacks;
+  M->smoother_active = false;
   inf.nvcycle = cs.nvc;
   double rel = 0.0;
   M3_TRY(coupled_residual(M, U, Pd, rel));
@@ -1577,4 +1628,118 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
   }
   clear_graphs(M);
   return M3SPH_OK;
+}
+
+// ======================================================================================
+// learned smoother: data collection, training, weights
+// ======================================================================================
+__global__ void k_rand_rhs(double *b, const uint8_t *mask, size_t n, unsigned long long seed) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  b[i] = mask[i] ? 2.0 * u - 1.0 : 0.0;
+}
+__global__ void k_diff(const double *a, const double *b, double *out, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
+}
+
+extern "C" int m3sph_ml_reserve(m3sph_mesh *M, int64_t capacity) {
+  M3_TRY(need_op(M));
+  return ml_reserve(M, capacity);
+}
+
+extern "C" int m3sph_ml_collect(m3sph_mesh *M, uint64_t seed, int32_t n_iterates, int32_t stride, int64_t *count) {
+  M3_TRY(need_op(M));
+  if (n_iterates < 1 || stride < 1) {
+    set_error("m3sph_ml_collect: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  const size_t n = L0.ndof;
+  const bool act = M->smoother_active;
+  M->smoother_active = false;
+  k_rand_rhs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W->y, L0.freemask, n, seed); count_launch();
+  // converged reference solution of K x = b with the plain multigrid
+  M3_CUDA(cudaMemsetAsync(W->z, 0, sizeof(double) * n, s));
+  CGStats cs;
+  M3_TRY(mgpcg(M, W->y, W->z, 1e-10, false, 400, cs));
+  // plain-multigrid iterates from zero: pairs (residual, error)
+  M3_CUDA(cudaMemsetAsync(W->U, 0, sizeof(double) * n, s));
+  for (int k = 0; k < n_iterates; ++k) {
+    M3_TRY(outer_apply(M, W->U, W->r));
+    M3_TRY(sub_mask(W->y, W->r, L0.freemask, n, s));
+    k_diff<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W->z, W->U, W->tmp, n); count_launch();
+    M3_TRY(ml_add_samples(M, W->r, W->tmp, stride, (int)((seed + k) % (uint64_t)stride)));
+    CGStats c1;
+    M3_TRY(mgpcg(M, W->y, W->U, 1e-300, true, 1, c1));
+  }
+  M3_CUDA(cudaStreamSynchronize(s));
+  M->smoother_active = act;
+  if (count) *count = ml_count(M);
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_ml_train_epoch(m3sph_mesh *M, int32_t batch, float lr, uint64_t seed, double *mse) {
+  M3_TRY(need_op(M));
+  if (batch < 64 || batch % 64) {
+    set_error("m3sph_ml_train_epoch: batch must be a positive multiple of 64");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  double m = 0.0;
+  M3_TRY(ml_epoch(M, batch, lr, seed, &m));
+  clear_graphs(M);
+  if (mse) *mse = m;
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_ml_nparam(int32_t *n) {
+  if (!n) return M3SPH_ERR_BAD_INPUT;
+  *n = ml_nparam();
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_ml_set_params(m3sph_mesh *M, const float *params, int32_t trained) {
+  if (!M || !params) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  M3_TRY(ml_set_params(M, params));
+  ml_mark_trained(M, trained != 0);
+  clear_graphs(M);
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_ml_get_params(m3sph_mesh *M, float *params) {
+  if (!M || !params) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  return ml_get_params(M, params);
+}
+
+extern "C" int m3sph_ml_gradients(m3sph_mesh *M, const float *X, const float *T, int32_t n, float *grad, double *loss) {
+  if (!M || !X || !T || !grad || n < 1) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  return ml_gradients(M, X, T, n, grad, loss);
+}
+
+extern "C" int m3sph_ml_forward(m3sph_mesh *M, const float *X, int32_t n, float *Y) {
+  if (!M || !X || !Y || n < 1) {
+    set_error("bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  return ml_forward(M, X, n, Y);
 }

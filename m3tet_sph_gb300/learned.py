@@ -1,0 +1,100 @@
+"""Training driver for the learned element smoother (no counterpart in the reference).
+
+Training pairs (local residual, local error) come from plain-multigrid solves of the project's own
+operator on a shell mesh over seeded viscosity fields; the network is trained on the GPU by the
+library's forward / backward kernels (m3sph_ml_train_epoch). Weights are a flat FP32 vector
+(m3sph_ml_nparam values) that can be saved with numpy and loaded into any mesh handle.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib as L
+from . import workloads
+
+
+def nparam():
+    n = C.c_int32()
+    L.check(L.lib().m3sph_ml_nparam(C.byref(n)))
+    return n.value
+
+
+def init_params(seed=0):
+    """Xavier-uniform weights, zero biases, zero padding (W1 [128][64], b1, W2 [32][128], b2)."""
+    rng = np.random.default_rng(seed)
+    W1 = np.zeros((128, 64), np.float32)
+    W1[:, :52] = rng.uniform(-1, 1, (128, 52)) * np.sqrt(6.0 / (52 + 128))
+    W2 = np.zeros((32, 128), np.float32)
+    W2[:30] = rng.uniform(-1, 1, (30, 128)) * np.sqrt(6.0 / (128 + 30))
+    p = np.concatenate([W1.ravel(), np.zeros(128, np.float32), W2.ravel(), np.zeros(32, np.float32)])
+    assert p.size == nparam()
+    return p
+
+
+def set_params(dm, p, trained=True):
+    p = np.ascontiguousarray(p, dtype=np.float32)
+    L.check(L.lib().m3sph_ml_set_params(dm.h, L.fptr(p), int(trained)))
+
+
+def get_params(dm):
+    p = np.zeros(nparam(), np.float32)
+    L.check(L.lib().m3sph_ml_get_params(dm.h, L.fptr(p)))
+    return p
+
+
+def forward(dm, X):
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.zeros((X.shape[0], 30), np.float32)
+    L.check(L.lib().m3sph_ml_forward(dm.h, L.fptr(X), X.shape[0], L.fptr(Y)))
+    return Y
+
+
+def gradients(dm, X, T):
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    T = np.ascontiguousarray(T, dtype=np.float32)
+    g = np.zeros(nparam(), np.float32)
+    loss = C.c_double()
+    L.check(L.lib().m3sph_ml_gradients(dm.h, L.fptr(X), L.fptr(T), X.shape[0], L.fptr(g), C.byref(loss)))
+    return g, loss.value
+
+
+def collect(dm, seed, n_iterates=4, stride=1):
+    n = C.c_int64()
+    L.check(L.lib().m3sph_ml_collect(dm.h, int(seed), int(n_iterates), int(stride), C.byref(n)))
+    return n.value
+
+
+def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_000, n_iterates=4, epochs=12,
+                   batch=4096, lr=2e-3, seed=0, precision=1, log=None):
+    """Collect pairs over `n_fields` seeded viscosity fields on the mesh of workload `w`, train,
+    and leave the trained weights loaded in `dm`. Returns (params, history)."""
+    rng = np.random.default_rng(seed)
+    nel = w['levels'][0]['nel']
+    per_field = samples / n_fields
+    stride = max(1, int(np.ceil(nel * n_iterates / per_field)))
+    L.check(L.lib().m3sph_ml_reserve(dm.h, int(samples) + nel))
+    t0 = time.time()
+    for i in range(n_fields):
+        c = float(np.exp(rng.uniform(np.log(contrast_range[0]), np.log(contrast_range[1]))))
+        T = workloads.temperature(w['levels'], seed + 1000 + i)
+        visc = workloads.viscosity(w['levels'], T, c, 30.0)
+        dm.setup(visc, workloads.density(T), w['ifix'], w['vfix'], w['phys'], precision=precision)
+        count = collect(dm, seed * 7919 + i, n_iterates, stride)
+        if log:
+            log(f"field {i}: contrast {c:.3g}, samples {count}")
+    t_collect = time.time() - t0
+    set_params(dm, init_params(seed), trained=False)
+    hist = []
+    t0 = time.time()
+    for ep in range(epochs):
+        mse = C.c_double()
+        lr_ep = lr * (0.5 ** (ep // max(1, epochs // 3)))
+        L.check(L.lib().m3sph_ml_train_epoch(dm.h, int(batch), float(lr_ep), int(seed + ep), C.byref(mse)))
+        hist.append(mse.value)
+        if log:
+            log(f"epoch {ep}: mse {mse.value:.5f}")
+    t_train = time.time() - t0
+    return get_params(dm), dict(mse=hist, t_collect=t_collect, t_train=t_train, stride=stride)

@@ -324,3 +324,37 @@ def advect_pc2(mesh, U, T, dt, r_cmb, r_surf, method_interp='quadratic', monoton
     else:
         Tn = interp3d_tet(mesh['EL2NOD'], e2, lc2, T, monotonic)
     return Tn, Pd, e1, e2
+
+
+def advect_rk4(mesh, U, T, dt, r_cmb, r_surf, nsub=3, method_interp='quadratic', monotonic=True, k=48):
+    """Builder-defined RK4 backtracking over `nsub` substeps (the reference's RK4 is an error stub,
+    advect3d_slm_p_sph.m:103-104): classical RK4 on dx/dt = U(x) backwards in Cartesian
+    coordinates, every stage point moved radially into [r_cmb + tol, r_surf - tol], U by P2
+    interpolation at located points; T interpolated at the departure points."""
+    X = mesh['GCOORD']
+    loc = Locator(mesh, k)
+    r_tol = 1e-12 * (r_surf - r_cmb)
+
+    def U_at(Xp):
+        P = clamp_radius(cart2sph(Xp), r_cmb, r_surf)
+        e, lc = loc.locate(P)
+        return interp3d_tet(mesh['EL2NOD'], e, adjust_local_coords(lc), U).T
+
+    h = dt / nsub
+    Xc = X.copy()
+    for sub in range(nsub):
+        k1 = U.T if sub == 0 else U_at(Xc)
+        k2 = U_at(Xc - 0.5 * h * k1)
+        k3 = U_at(Xc - 0.5 * h * k2)
+        k4 = U_at(Xc - h * k3)
+        Xc = Xc - h / 6.0 * (k1 + 2 * k2 + 2 * k3 + k4)
+        r = np.sqrt((Xc ** 2).sum(0))
+        Xc = Xc * (np.clip(r, r_cmb + r_tol, r_surf - r_tol) / r)
+    Pd = cart2sph(Xc)
+    e2, lc2 = loc.locate(Pd)
+    lc2 = adjust_local_coords(lc2)
+    if method_interp == 'cubic':
+        Tn = interp3d_cubic(X, mesh['EL2NOD'], e2, lc2, T, monotonic)
+    else:
+        Tn = interp3d_tet(mesh['EL2NOD'], e2, lc2, T, monotonic)
+    return Tn, Pd, e2
