@@ -188,6 +188,20 @@ M3SPH_API int m3sph_interp3d_tet(m3sph_mesh *mesh, const int32_t *els, const dou
 /* Replaces interp3d_cubic_p (interp3d_cubic_p.m:80-382) for one nodal field V (nnod). */
 M3SPH_API int m3sph_interp3d_cubic(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
                                    const double *V, int32_t monotonic, int32_t method_wght, double *Vi);
+/* Allocation-free variant of m3sph_interp3d_cubic (no counterpart in the reference). For callers
+ * that cannot allocate device memory while they run: a host that owns all device memory through
+ * its own pool, a time loop with a fixed memory footprint, or a host with work in flight on other
+ * streams that a cudaMalloc / cudaFree (which may synchronise the device) would stall.
+ * els (npt, 1-based), lc (npt x 3), V (nnod) and Vi (npt) must be memory the device can access
+ * (device, managed or mapped pinned host memory), with the inputs complete before the call; the
+ * work runs on the handle's stream (m3sph_stream), which is synchronised before returning.
+ * Scratch lives in one fixed 8 MiB array per device that every call shares (7 values per element
+ * + 4 per vertex, about 120k elements of a spherical-shell mesh; larger meshes are rejected with
+ * M3SPH_ERR_BAD_INPUT). The first call on a device looks up the array's address, so make that
+ * first call before any stream capture. Calls that overlap on the GPU (two handles on two
+ * threads) race on the shared scratch. It calls no cudaMalloc / cudaFree. */
+M3SPH_API int m3sph_interp3d_cubic_noalloc(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
+                                           const double *V, int32_t monotonic, int32_t method_wght, double *Vi);
 /* Replaces advect3d_slm_p_sph (advect3d_slm_p_sph.m:1-139): Ux,Uy,Uz Cartesian nodal velocity,
  * T (nnod) advected in place over dt. els_BT / els_INTERP (nnod, 1-based, 0 = unknown) are the
  * WS_SLM search guesses, updated on return (predictor and departure elements). */

@@ -91,6 +91,7 @@ SIGNATURES = {
     "m3sph_tsearch_sph": ([P, DP, C.c_int32, IP, IP, DP, C.POINTER(LocateInfo)], C.c_int),
     "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_interp3d_cubic": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
+    "m3sph_interp3d_cubic_noalloc": ([P, P, P, C.c_int32, P, C.c_int32, C.c_int32, P], C.c_int),
     "m3sph_advect_slm": ([P, DP, DP, DP, DP, C.c_double, C.POINTER(SlmOpts), IP, IP, C.POINTER(LocateInfo)], C.c_int),
     "m3sph_ml_nparam": ([IP], C.c_int),
     "m3sph_ml_set_params": ([P, C.POINTER(C.c_float), C.c_int32], C.c_int),

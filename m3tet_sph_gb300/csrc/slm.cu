@@ -14,6 +14,8 @@
 // lie in [0,1]; if several do (points on shared faces), non-isoparametric elements win, then
 // the largest element id; if none does, the vertex-neighbours of the last walked element are
 // searched with a tolerance grown in 1e-6 steps up to 15e-3. Every walk has a step limit.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace m3sph {
@@ -1011,5 +1013,144 @@ extern "C" int m3sph_advect_slm(m3sph_mesh *M, const double *Ux, const double *U
     if (els_BT) els_BT[i] = g[i] + 1;
     if (els_INTERP) els_INTERP[i] = e[i] + 1;
   }
+  return M3SPH_OK;
+}
+
+// ======================================================================================
+// Allocation-free quasi-cubic interpolation.
+//
+// Some callers of this library cannot allocate device memory once they are running: a host
+// whose device memory is entirely owned by its own pool allocator (a stray cudaMalloc would fail
+// or fragment that pool), a solver loop that must keep its memory footprint fixed after start-up,
+// or a host with work in flight on other streams that a cudaMalloc / cudaFree (which may
+// synchronise the device) would stall. m3sph_interp3d_cubic grows the handle's work buffers on demand
+// (cudaMalloc); this variant keeps its scratch -- element gradients and weights, nodal gradient
+// sums -- in the fixed file-scope array below, and takes inputs and outputs in memory the caller
+// already owns and the device can read and write.
+// ======================================================================================
+namespace m3sph {
+
+constexpr size_t NOALLOC_SCRATCH_DOUBLES = size_t(1) << 20;   // 8 MiB per device, held until exit
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+static std::mutex g_noalloc_mu;
+
+// Device address of the scratch array on `device`, looked up once per device with that device
+// current (in host code the symbol name is only a host-side stand-in, never a device address).
+static int noalloc_scratch(int device, double **out) {
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES) {
+    set_error("device id out of range for the allocation-free scratch table");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    int cur = -1;
+    M3_CUDA(cudaGetDevice(&cur));
+    if (cur != device) M3_CUDA(cudaSetDevice(device));
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (cur != device) cudaSetDevice(cur);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[device] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return M3SPH_OK;
+}
+
+// quasi-cubic value at one point of element e with local coordinates (r,s,t): the same arithmetic
+// as k_cubic_interp (interp3d_cubic_p.m:243-382)
+__device__ double cubic_point(const SlmMesh &m, const double *__restrict__ X, int e, double r, double s, double t,
+                              const double *__restrict__ B, const double *__restrict__ gn,
+                              const double *__restrict__ wn, const double *__restrict__ gel, int monotonic) {
+  const double u = 1.0 - r - s - t;
+  const double q2 = 1.4142135623730951;   // sqrt(2)
+  const double N[16] = {r, s, t, u, q2 * r * s, q2 * s * t, t * u, r * u, q2 * r * t, s * u,
+                        q2 * s * r * (s - r), q2 * s * t * (t - s), t * u * (u - t), r * u * (u - r),
+                        q2 * r * t * (t - r), s * u * (u - s)};
+  int v[4];
+  double x[4], y[4], z[4], b[4], dB[4][3];
+  for (int k = 0; k < 4; ++k) {
+    v[k] = m.el2nod[(size_t)k * m.nel + e];
+    x[k] = X[v[k]]; y[k] = X[m.nnod + v[k]]; z[k] = X[2 * m.nnod + v[k]];
+    b[k] = B[v[k]];
+    const double wk = wn[v[k]];
+    for (int c = 0; c < 3; ++c) dB[k][c] = gn[(size_t)c * m.nvnod + v[k]] / wk - gel[(size_t)c * m.nel + e];
+  }
+  double sr[4], ss[4], st[4];
+  for (int k = 0; k < 4; ++k) {
+    sr[k] = (x[0] - x[3]) * dB[k][0] + (y[0] - y[3]) * dB[k][1] + (z[0] - z[3]) * dB[k][2];
+    ss[k] = (x[1] - x[3]) * dB[k][0] + (y[1] - y[3]) * dB[k][1] + (z[1] - z[3]) * dB[k][2];
+    st[k] = (x[2] - x[3]) * dB[k][0] + (y[2] - y[3]) * dB[k][1] + (z[2] - z[3]) * dB[k][2];
+  }
+  const double h = 0.7071067811865476;    // sqrt(1/2)
+  const double q1n2 = h * sr[1] - h * ss[1], q1n1 = h * sr[0] - h * ss[0];
+  const double q2n3 = h * ss[2] - h * st[2], q2n2 = h * ss[1] - h * st[1];
+  const double q5n3 = h * sr[2] - h * st[2], q5n1 = h * sr[0] - h * st[0];
+  const double info[12] = {(q1n2 - q1n1) / 2, (q2n3 - q2n2) / 2, (st[3] - st[2]) / 2, (sr[3] - sr[0]) / 2,
+                           (q5n3 - q5n1) / 2, (ss[3] - ss[1]) / 2, (q1n2 + q1n1) / 2, (q2n3 + q2n2) / 2,
+                           (st[3] + st[2]) / 2, (sr[3] + sr[0]) / 2, (q5n3 + q5n1) / 2, (ss[3] + ss[1]) / 2};
+  double val = N[0] * b[0] + N[1] * b[1] + N[2] * b[2] + N[3] * b[3];
+  for (int k = 0; k < 12; ++k) val += N[4 + k] * info[k];
+  if (monotonic) {
+    const double lo = fmin(fmin(b[0], b[1]), fmin(b[2], b[3])), hi = fmax(fmax(b[0], b[1]), fmax(b[2], b[3]));
+    val = fmin(fmax(val, lo), hi);
+  }
+  return val;
+}
+
+// caller-layout variant: 1-based element ids, local coordinates as npt x 3
+__global__ void k_cubic_interp_caller(SlmMesh m, const double *__restrict__ X, const int32_t *__restrict__ els,
+                                      const double *__restrict__ lc, int npt, const double *__restrict__ B,
+                                      const double *__restrict__ gn, const double *__restrict__ wn,
+                                      const double *__restrict__ gel, int monotonic, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npt) return;
+  const int e = els[i] - 1;
+  if (e < 0 || e >= m.nel) {
+    out[i] = nan("");
+    return;
+  }
+  out[i] = cubic_point(m, X, e, lc[3 * (size_t)i], lc[3 * (size_t)i + 1], lc[3 * (size_t)i + 2], B, gn, wn, gel,
+                       monotonic);
+}
+
+}  // namespace m3sph
+
+extern "C" int m3sph_interp3d_cubic_noalloc(m3sph_mesh *M, const int32_t *els, const double *lc, int32_t npt,
+                                            const double *V, int32_t monotonic, int32_t method_wght, double *Vi) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (npt <= 0 || !els || !lc || !V || !Vi) {
+    set_error("m3sph_interp3d_cubic_noalloc: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  const size_t nel = L0.nel, nv = L0.nvnod;
+  const size_t need = 7 * nel + 4 * nv;   // element gradients (3) and weights (4), nodal sums (3) and weights (1)
+  if (need > NOALLOC_SCRATCH_DOUBLES) {
+    set_error("m3sph_interp3d_cubic_noalloc: this mesh needs " + std::to_string(need) +
+              " scratch values but the fixed scratch holds " + std::to_string(NOALLOC_SCRATCH_DOUBLES) +
+              " (7 per element + 4 per vertex); use m3sph_interp3d_cubic");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  double *scr = nullptr;
+  if ((st = noalloc_scratch(M->device, &scr))) return st;
+  double *gel = scr, *wel = gel + 3 * nel, *gn = wel + 4 * nel, *wn = gn + 3 * nv;
+  cudaStream_t s = M->stream;
+  k_cubic_elgrad<<<(unsigned)((nel + 127) / 128), 128, 0, s>>>(S->view, M->fin.gcoord, V, method_wght, gel, wel); count_launch();
+  // the array keeps the previous call's contents: the nodal sums must start at zero
+  M3_CUDA(cudaMemsetAsync(gn, 0, sizeof(double) * 4 * nv, s));   // gn (3 nv) and wn (nv) are contiguous
+  for (size_t c = 0; c + 1 < L0.cstart.size(); ++c) {
+    const int b = L0.cstart[c], e = L0.cstart[c + 1];
+    if (e > b) k_cubic_scatter<<<(e - b + 127) / 128, 128, 0, s>>>(L0.perm, (int)nel, b, e, S->el2nod, gel, wel, gn,
+                                                                   wn, (int)nv); count_launch();
+  }
+  k_cubic_interp_caller<<<(npt + 127) / 128, 128, 0, s>>>(S->view, M->fin.gcoord, els, lc, npt, V, gn, wn, gel,
+                                                           monotonic, Vi); count_launch();
+  M3_CUDA(cudaGetLastError());
+  M3_CUDA(cudaStreamSynchronize(s));
   return M3SPH_OK;
 }
