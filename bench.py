@@ -180,10 +180,10 @@ def run_gb300(args, rank, ws, td):
     U = np.empty(ndof)
     P = np.zeros(lv0["EL2NOD"][:, :4].max() + 1)
     te = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(max(1, args.e2e_steps)):
         setup(1)
         U, P, einfo = dm.solve(P0=np.zeros_like(P), **SOLVER_KW)
-    t_e2e = allmax(td, (time.perf_counter() - te) / args.e2e_steps)
+    t_e2e = allmax(td, (time.perf_counter() - te) / max(1, args.e2e_steps))
     h2d = (w["visc"].nbytes + w["dens"].nbytes + 4 * len(w["ifix"]) + w["vfix"].nbytes + P.nbytes)
     d2h = U.nbytes + P.nbytes
     dm.close()
@@ -221,6 +221,31 @@ def run_gb300(args, rank, ws, td):
     }
     if rank == 0:
         print(json.dumps(out))
+
+
+def run_operator_only(args, rank):
+    """Operator-only run for profiler captures: set up the mixed-precision operator once, then time
+    --op-reps applications of one level operator (precision 0 FP64, 1 FP32, 2 double-float)."""
+    from m3tet_sph_gb300 import build as B
+    B.build()
+    from m3tet_sph_gb300 import stokes, workloads
+    w = workloads.make_workload(args.workload, seed=args.seed)
+    lv0 = w["levels"][0]
+    dm = stokes.DeviceMesh(w["levels"])
+    dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
+    for kv in args.set_option:
+        k, v = kv.split("=")
+        dm.set_option(k, int(v))
+    ms = dm.apply_timing(args.op_level, args.op_precision, args.op_reps)
+    nc = dm.ncolors(args.op_level)
+    dm.close()
+    s = 8 if args.op_precision in (0, 2) else 4
+    b = apply_bytes(lv0["nel"], 3 * lv0["nnod"], s) if args.op_level == 0 else None
+    if rank == 0:
+        print(json.dumps({"workload": args.workload, "options": args.set_option, "nel": lv0["nel"], "colours": nc,
+                          "level": args.op_level,
+                          "precision": args.op_precision, "ms_per_apply": ms,
+                          "gbs": None if b is None else b / (ms * 1e-3) / 1e9}))
 
 
 def cpu_baseline(w, gpu_info, args):
@@ -302,10 +327,19 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-sample-els", type=int, default=20000)
     ap.add_argument("--cpu-iters", type=int, default=3)
-    ap.add_argument("--ref-iters", type=int, default=600)
+    ap.add_argument("--ref-iters", type=int, default=988,
+                    help="MG-PCG iterations the reference arm charges per solve (nitU + nitZ of the "
+                         "plain-FP64 GPU solve of the 8M-DOF shell)")
+    ap.add_argument("--op-only", action="store_true", help="time one level operator only (profiling)")
+    ap.add_argument("--op-level", type=int, default=0)
+    ap.add_argument("--op-precision", type=int, default=1)
+    ap.add_argument("--op-reps", type=int, default=20)
+    ap.add_argument("--set-option", action="append", default=[], help="library option name=value (--op-only)")
     args = ap.parse_args()
     rank, ws, td = dist_init()
-    if args.impl == "reference":
+    if args.op_only:
+        run_operator_only(args, rank)
+    elif args.impl == "reference":
         run_reference(args, rank, ws, td)
     else:
         run_gb300(args, rank, ws, td)

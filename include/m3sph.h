@@ -228,6 +228,9 @@ M3SPH_API int m3sph_force_vector(m3sph_mesh *mesh, double *Fb);
 M3SPH_API int m3sph_element_matrices(m3sph_mesh *mesh, double *K, double *G, double *M);
 /* y = KK{img} x on level img (0-based, img>=1: Galerkin coarse operator), vectors 3*nnod(img) */
 M3SPH_API int m3sph_level_apply(m3sph_mesh *mesh, int32_t img, const double *x, double *y);
+/* The FP32 operator of level img as used inside the V-cycle (streamed element apply on the finest
+ * level, assembled blocks on coarse levels); needs a set-up with precision 1. */
+M3SPH_API int m3sph_level_apply32(m3sph_mesh *mesh, int32_t img, const float *x, float *y);
 /* Ic2f{img} (intermesh_transfer_matrix): prolong x_c (3*nnod(img+1)) -> x_f (3*nnod(img)) and
  * restrict r_f -> r_c with Ic2f' (free-dof masked as in restrict_stiffmat.m:94-96). */
 M3SPH_API int m3sph_prolong(m3sph_mesh *mesh, int32_t img, const double *xc, double *xf);

@@ -81,6 +81,7 @@ SIGNATURES = {
     "m3sph_div_apply": ([P, DP, DP], C.c_int),
     "m3sph_force_vector": ([P, DP], C.c_int),
     "m3sph_element_matrices": ([P, DP, DP, DP], C.c_int),
+    "m3sph_level_apply32": ([P, C.c_int32, P, P], C.c_int),
     "m3sph_level_apply": ([P, C.c_int32, DP, DP], C.c_int),
     "m3sph_prolong": ([P, C.c_int32, DP, DP], C.c_int),
     "m3sph_restrict": ([P, C.c_int32, DP, DP], C.c_int),

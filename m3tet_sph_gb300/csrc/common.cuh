@@ -35,6 +35,17 @@ __host__ __device__ __forceinline__ size_t kidx(int k, size_t e, size_t nel) {
   constexpr int V = KVec<T>::V;
   return ((size_t)(k / V) * nel + e) * V + (k % V);
 }
+// packed entry k -> (row r, column c) of the lower triangle, column-major (k = 0: (0,0), 1: (1,0), ...)
+__host__ __device__ constexpr int unpack_c(int k) {
+  int c = 0;
+  while (k >= 30 - c) { k -= 30 - c; ++c; }
+  return c;
+}
+__host__ __device__ constexpr int unpack_r(int k) {
+  int c = 0;
+  while (k >= 30 - c) { k -= 30 - c; ++c; }
+  return c + k;
+}
 template <typename T> constexpr int kpad() { return ((NPACK + KVec<T>::V - 1) / KVec<T>::V) * KVec<T>::V; }
 
 void set_error(const std::string &msg);
@@ -94,6 +105,14 @@ struct Level {
   int *bsr_cptr = nullptr, *bsr_contrib = nullptr;   // per block: contributions e*100 + a*10 + b
   double *B64 = nullptr;                         // [nnzb][9]
   float *B32 = nullptr;
+  // streamed apply (finest level): phase 1 streams the element matrices in chunks of 32 stored
+  // elements and writes element outputs Ye; phase 2 sums them per node in a fixed order
+  int nchunk = 0, sa_grid = 0;
+  int *chunk_conn = nullptr;          // [nchunk][10][32] node ids of the chunk's elements (0: unused lane)
+  float *ye32 = nullptr;              // [nel][30] element outputs
+  int *g_ptr = nullptr;               // [nnod + 1] node -> incident (element, local node) entries
+  int *g_idx = nullptr;               // [10 nel] offsets e * 30 + 3 * local node into Ye, element order
+  int *sa_err = nullptr;              // bounded waits of the streamed apply that gave up (bit mask)
   // host copies needed at set-up
   std::vector<int> h_el2nod_orig;     // [nel][10] original order, 0-based
 };

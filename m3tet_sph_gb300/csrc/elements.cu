@@ -454,16 +454,6 @@ int ebe_apply_df(const Level &L, const float *Kh, const float *Kl, const double 
 // one contiguous 512-byte segment), partial results are summed in shared memory and scattered.
 // Packed entry k -> (row, col) is resolved at compile time.
 // ----------------------------------------------------------------------------------------
-__host__ __device__ constexpr int unpack_c(int k) {
-  int c = 0;
-  while (k >= 30 - c) { k -= 30 - c; ++c; }
-  return c;
-}
-__host__ __device__ constexpr int unpack_r(int k) {
-  int c = 0;
-  while (k >= 30 - c) { k -= 30 - c; ++c; }
-  return c + k;
-}
 
 struct OpF32 {   // FP32 V-cycle operator
   using acc_t = float;

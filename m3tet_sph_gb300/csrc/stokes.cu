@@ -14,6 +14,7 @@
 #include <cstring>
 #include <atomic>
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -27,6 +28,9 @@ int ebe_apply_df(const Level &L, const float *Kh, const float *Kl, const double 
 int ebe_apply_split_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s);
 int ebe_apply_split_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
 int ebe_apply_split_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
+int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s);
+int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s);
+int stream_check(const Level &L, cudaStream_t s);
 int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
 template <typename T> int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s);
 int grad_apply(const Level &L, const double *G, const double *q, double *y, cudaStream_t s);
@@ -296,6 +300,7 @@ static int build_level(m3sph_mesh *M, int img, const m3sph_level &in, Level &L) 
   M3_TRY(dalloc(&L.Dinv64, L.ndof));
   M3_TRY(dalloc(&L.Dinv32, L.ndof));
   if (img > 0) M3_TRY(build_bsr(M, L, perm));
+  if (img == 0) M3_TRY(stream_build(L, perm, s));
   M3_CUDA(cudaStreamSynchronize(s));
   return M3SPH_OK;
 }
@@ -406,7 +411,7 @@ static void free_level(Level &L) {
                   (void *)L.K32, (void *)L.KL32, (void *)L.Dinv64, (void *)L.Dinv32, (void *)L.child, (void *)L.child_vloc,
                   (void *)L.P_ptr, (void *)L.P_col, (void *)L.P_w, (void *)L.R_ptr, (void *)L.R_col, (void *)L.R_w,
                   (void *)L.bsr_ptr, (void *)L.bsr_col, (void *)L.bsr_cptr, (void *)L.bsr_contrib, (void *)L.B64,
-                  (void *)L.B32})
+                  (void *)L.B32, (void *)L.chunk_conn, (void *)L.ye32, (void *)L.g_ptr, (void *)L.g_idx, (void *)L.sa_err})
     dfree(p);
   L = Level();
 }
@@ -831,9 +836,17 @@ static int split_apply_T(const Level &L, const float *K, const float *x, float *
 static int split_apply_T(const Level &L, const double *K, const double *x, double *y, cudaStream_t s) {
   return ebe_apply_split_f64(L, K, x, y, s);
 }
+static bool g_stream_apply = true;
+static int stream_apply_T(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
+  return stream_apply_f32(L, K, x, y, s);
+}
+static int stream_apply_T(const Level &, const double *, const double *, double *, cudaStream_t) {
+  return M3SPH_ERR_BAD_INPUT;
+}
 template <typename T>
 static int level_op(const Level &L, int img, const T *x, T *y, cudaStream_t s) {
   if (img > 0 && levB<T>(L)) return bsr_apply<T>(L, levB<T>(L), x, y, s);
+  if (std::is_same<T, float>::value && g_stream_apply && L.nchunk) return stream_apply_T(L, levK<T>(L), x, y, s);
   if (g_split_apply) return split_apply_T(L, levK<T>(L), x, y, s);
   return ebe_apply<T>(L, levK<T>(L), x, y, s);
 }
@@ -1267,6 +1280,7 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   double rel = 0.0;
   M3_TRY(coupled_residual(M, U, Pd, rel));
   inf.rel_residual = rel;
+  M3_TRY(stream_check(L0, s));
   return M3SPH_OK;
 }
 
@@ -1492,6 +1506,27 @@ extern "C" int m3sph_level_apply(m3sph_mesh *M, int32_t img, const double *x, do
   return M3SPH_OK;
 }
 
+extern "C" int m3sph_level_apply32(m3sph_mesh *M, int32_t img, const float *x, float *y) {
+  M3_TRY(need_op(M));
+  if (img < 0 || img >= M->nmg) {
+    set_error("level out of range");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Level &L = M->lev[img];
+  if (!L.K32 && !L.B32) {
+    set_error("no FP32 operator on this level (set up with precision 1)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  const size_t n = L.ndof;
+  M3_CUDA(cudaMemcpyAsync(W->r32[img], x, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  M3_TRY(level_op<float>(L, img, W->r32[img], W->kd32[img], s));
+  M3_CUDA(cudaMemcpyAsync(y, W->kd32[img], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  M3_TRY(stream_check(L, s));
+  return M3SPH_OK;
+}
+
 extern "C" int m3sph_prolong(m3sph_mesh *M, int32_t img, const double *xc, double *xf) {
   M3_TRY(need_op(M));
   if (img < 0 || img + 1 >= M->nmg) {
@@ -1604,6 +1639,7 @@ extern "C" int m3sph_apply_timing(m3sph_mesh *M, int32_t img, int32_t precision,
   float ms = 0.f;
   M3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
   *ms_per_apply = ms / nrep;
+  M3_TRY(stream_check(L, s));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return M3SPH_OK;
@@ -1615,7 +1651,9 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
     return M3SPH_ERR_BAD_INPUT;
   }
   const std::string n(name);
-  if (n == "split_apply") {
+  if (n == "stream_apply") {
+    g_stream_apply = value != 0;
+  } else if (n == "split_apply") {
     M->split_apply = value != 0;
     g_split_apply = value != 0;
   } else if (n == "graphs") {

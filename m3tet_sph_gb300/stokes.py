@@ -123,6 +123,13 @@ class DeviceMesh:
         L.check(L.lib().m3sph_level_apply(self.h, img, L.dptr(np.ascontiguousarray(x, dtype=np.float64)), L.dptr(y)))
         return y
 
+    def level_apply32(self, img, x):
+        """FP32 level operator (the V-cycle's); x in the level's rotated, dof-interleaved frame."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty_like(x)
+        L.check(L.lib().m3sph_level_apply32(self.h, img, L.fptr(x), L.fptr(y)))
+        return y
+
     def prolong(self, img, xc):
         y = np.empty(3 * self.levels[img]['GCOORD'].shape[1])
         L.check(L.lib().m3sph_prolong(self.h, img, L.dptr(np.ascontiguousarray(xc, dtype=np.float64)), L.dptr(y)))

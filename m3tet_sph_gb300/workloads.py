@@ -138,6 +138,9 @@ def make_workload(name, seed=0, nmg=None, level=None, nlayer=None):
     elif name == 'mid':
         # 1/8 of the 8M-DOF shell (level 4, 16 layers): the profiling case (> L2, a few GB on device)
         L, n, g, contrast, jump, bc = 4, 16, 4, 1e4, 30.0, 'plates'
+    elif name == 'prof':
+        # profiler case: 491,520 elements (about 12k per colour), ~4.5 GB on the device
+        L, n, g, contrast, jump, bc = 5, 8, 4, 1e4, 30.0, 'plates'
     elif name == 'tiny':
         L, n, g, contrast, jump, bc = 2, 4, 2, 1.0, 1.0, 'free_slip'
     elif name == 'tiny_plates':

@@ -189,3 +189,53 @@ def test_mixed_operators_parity(case):
         assert np.linalg.norm(yc - yc_ref) < 1e-5 * np.linalg.norm(yc_ref)
     finally:
         dm2.close()
+
+
+def _stream_vs_split(dm2, x):
+    """(streamed apply twice, per-colour split apply) of the FP32 finest-level operator."""
+    try:
+        ys = [dm2.level_apply32(0, x) for _ in range(2)]
+        dm2.set_option("stream_apply", 0)
+        y_split = dm2.level_apply32(0, x)
+    finally:
+        dm2.set_option("stream_apply", 1)
+    return ys, y_split
+
+
+def test_streamed_fp32_apply(case):
+    """The streamed finest-level FP32 apply (TMA ring + fixed-order node sums) is deterministic and
+    matches the per-colour split kernel and the FP64 operator to FP32 rounding."""
+    w, S, dm = case
+    from m3tet_sph_gb300 import stokes
+    dm2 = stokes.DeviceMesh(w['levels'])
+    try:
+        dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
+        rng = np.random.default_rng(11)
+        x = np.zeros(S.nU, np.float32)
+        x[S.ifree] = rng.standard_normal(len(S.ifree))
+        y_ref = np.zeros(S.nU)
+        y_ref[S.ifree] = S.K1 @ x[S.ifree].astype(np.float64)
+        ys, y_split = _stream_vs_split(dm2, x)
+        assert np.array_equal(ys[0], ys[1])
+        assert np.linalg.norm(ys[0] - y_split) < 1e-6 * np.linalg.norm(y_split)
+        assert np.linalg.norm(ys[0] - y_ref) < 1e-5 * np.linalg.norm(y_ref)
+    finally:
+        dm2.close()
+
+
+def test_streamed_fp32_apply_many_chunks(built_lib):
+    """Same checks on the 15,360-element shell (several chunks per CTA)."""
+    from m3tet_sph_gb300 import stokes, workloads
+    w = workloads.make_workload('c1')
+    dm2 = stokes.DeviceMesh(w['levels'])
+    try:
+        dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
+        rng = np.random.default_rng(12)
+        x = rng.standard_normal(3 * w['levels'][0]['nnod']).astype(np.float32)
+        y64 = dm2.level_apply(0, x.astype(np.float64))
+        ys, y_split = _stream_vs_split(dm2, x)
+        assert np.array_equal(ys[0], ys[1])
+        assert np.linalg.norm(ys[0] - y_split) < 1e-6 * np.linalg.norm(y_split)
+        assert np.linalg.norm(ys[0] - y64) < 1e-5 * np.linalg.norm(y64)
+    finally:
+        dm2.close()
