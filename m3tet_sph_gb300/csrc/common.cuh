@@ -46,6 +46,20 @@ __host__ __device__ constexpr int unpack_r(int k) {
   while (k >= 30 - c) { k -= 30 - c; ++c; }
   return c + k;
 }
+// y_hi + y_lo += (v_hi + v_lo)(x_hi + x_lo) in double-float: the product's rounding error by FMA,
+// the sum's by Knuth's two-sum (used by the FP64-accurate outer operator built from FP32 parts)
+__device__ __forceinline__ void df_mac(float vh, float vl, float xh, float xl, float &sh, float &sl) {
+  const float p = vh * xh;
+  float e = fmaf(vh, xh, -p);
+  e = fmaf(vh, xl, e);
+  e = fmaf(vl, xh, e);
+  const float s = sh + p;
+  const float bb = s - sh;
+  const float err = (sh - (s - bb)) + (p - bb);
+  sh = s;
+  sl += err + e;
+}
+
 template <typename T> constexpr int kpad() { return ((NPACK + KVec<T>::V - 1) / KVec<T>::V) * KVec<T>::V; }
 
 void set_error(const std::string &msg);
@@ -110,6 +124,9 @@ struct Level {
   int nchunk = 0, sa_grid = 0;
   int *chunk_conn = nullptr;          // [nchunk][10][32] node ids of the chunk's elements (0: unused lane)
   float *ye32 = nullptr;              // [nel][30] element outputs
+  int nchunk8 = 0;                    // FP64-accurate operators: chunks of 8 elements
+  int *chunk_conn8 = nullptr;         // [nchunk8][10][8]
+  double *ye64 = nullptr;             // [nel][30]
   int *g_ptr = nullptr;               // [nnod + 1] node -> incident (element, local node) entries
   int *g_idx = nullptr;               // [10 nel] offsets e * 30 + 3 * local node into Ye, element order
   int *sa_err = nullptr;              // bounded waits of the streamed apply that gave up (bit mask)

@@ -380,17 +380,6 @@ __global__ void __launch_bounds__(128) k_ebe_apply(const T *__restrict__ K, cons
 // operator of the V-cycle), x split the same way at the gather; each product is formed exactly
 // (FMA error term) and accumulated in double-float (Knuth two-sum). ~10 FP32 operations per
 // multiply-add instead of one FP64 FMA, which GB300 issues at 1/62 of its FP32 rate.
-__device__ __forceinline__ void df_mac(float vh, float vl, float xh, float xl, float &sh, float &sl) {
-  const float p = vh * xh;
-  float e = fmaf(vh, xh, -p);
-  e = fmaf(vh, xl, e);
-  e = fmaf(vl, xh, e);
-  const float s = sh + p;
-  const float bb = s - sh;
-  const float err = (sh - (s - bb)) + (p - bb);
-  sh = s;
-  sl += err + e;
-}
 
 __global__ void __launch_bounds__(128) k_ebe_apply_df(const float *__restrict__ Kh, const float *__restrict__ Kl,
                                                       const int *__restrict__ el2nod, int nel, int e_begin, int e_end,

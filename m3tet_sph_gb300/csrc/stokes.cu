@@ -30,7 +30,10 @@ int ebe_apply_split_f64(const Level &L, const double *K, const double *x, double
 int ebe_apply_split_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
 int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s);
 int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s);
+int stream_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
+int stream_apply_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
 int stream_check(const Level &L, cudaStream_t s);
+int stream_set_outer_warps(int n);
 int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
 template <typename T> int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s);
 int grad_apply(const Level &L, const double *G, const double *q, double *y, cudaStream_t s);
@@ -411,7 +414,8 @@ static void free_level(Level &L) {
                   (void *)L.K32, (void *)L.KL32, (void *)L.Dinv64, (void *)L.Dinv32, (void *)L.child, (void *)L.child_vloc,
                   (void *)L.P_ptr, (void *)L.P_col, (void *)L.P_w, (void *)L.R_ptr, (void *)L.R_col, (void *)L.R_w,
                   (void *)L.bsr_ptr, (void *)L.bsr_col, (void *)L.bsr_cptr, (void *)L.bsr_contrib, (void *)L.B64,
-                  (void *)L.B32, (void *)L.chunk_conn, (void *)L.ye32, (void *)L.g_ptr, (void *)L.g_idx, (void *)L.sa_err})
+                  (void *)L.B32, (void *)L.chunk_conn, (void *)L.ye32, (void *)L.g_ptr, (void *)L.g_idx, (void *)L.sa_err,
+                  (void *)L.chunk_conn8, (void *)L.ye64})
     dfree(p);
   L = Level();
 }
@@ -806,11 +810,19 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
 
 // FP64-accurate finest-level operator for the outer iterations: native FP64 on the plain path,
 // double-float FP32 arithmetic on the mixed path
+// streamed finest-level operators (TMA ring + fixed-order node sums) for the FP32 V-cycle operator
+// and, optionally, for the FP64-accurate outer operators; off: per-colour kernels
+static bool g_stream_apply = true;
+static bool g_stream_outer = true;
+
 static int outer_apply(m3sph_mesh *M, const double *x, double *y) {
   Level &L0 = M->lev[0];
-  if (M->precision == 1 && M->df_outer)
+  if (M->precision == 1 && M->df_outer) {
+    if (g_stream_outer && L0.nchunk) return stream_apply_df(L0, L0.K32, L0.KL32, x, y, M->stream);
     return M->split_apply ? ebe_apply_split_df(L0, L0.K32, L0.KL32, x, y, M->stream)
                           : ebe_apply_df(L0, L0.K32, L0.KL32, x, y, M->stream);
+  }
+  if (g_stream_outer && L0.nchunk) return stream_apply_f64(L0, L0.K64, x, y, M->stream);
   return M->split_apply ? ebe_apply_split_f64(L0, L0.K64, x, y, M->stream)
                         : ebe_apply<double>(L0, L0.K64, x, y, M->stream);
 }
@@ -836,17 +848,17 @@ static int split_apply_T(const Level &L, const float *K, const float *x, float *
 static int split_apply_T(const Level &L, const double *K, const double *x, double *y, cudaStream_t s) {
   return ebe_apply_split_f64(L, K, x, y, s);
 }
-static bool g_stream_apply = true;
 static int stream_apply_T(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
   return stream_apply_f32(L, K, x, y, s);
 }
-static int stream_apply_T(const Level &, const double *, const double *, double *, cudaStream_t) {
-  return M3SPH_ERR_BAD_INPUT;
+static int stream_apply_T(const Level &L, const double *K, const double *x, double *y, cudaStream_t s) {
+  return stream_apply_f64(L, K, x, y, s);
 }
 template <typename T>
 static int level_op(const Level &L, int img, const T *x, T *y, cudaStream_t s) {
   if (img > 0 && levB<T>(L)) return bsr_apply<T>(L, levB<T>(L), x, y, s);
-  if (std::is_same<T, float>::value && g_stream_apply && L.nchunk) return stream_apply_T(L, levK<T>(L), x, y, s);
+  if ((std::is_same<T, float>::value ? g_stream_apply : g_stream_outer) && L.nchunk && levK<T>(L))
+    return stream_apply_T(L, levK<T>(L), x, y, s);
   if (g_split_apply) return split_apply_T(L, levK<T>(L), x, y, s);
   return ebe_apply<T>(L, levK<T>(L), x, y, s);
 }
@@ -1410,7 +1422,7 @@ extern "C" int m3sph_stokes_apply(m3sph_mesh *M, const double *x, double *y) {
   M3_CUDA(cudaMemcpyAsync(W->tmp, x, sizeof(double) * L0.ndof, cudaMemcpyHostToDevice, s));
   M3_TRY(outer_apply(M, W->tmp, W->y));
   M3_CUDA(cudaMemcpyAsync(y, W->y, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
-  M3_CUDA(cudaStreamSynchronize(s));
+  M3_TRY(stream_check(L0, s));
   return M3SPH_OK;
 }
 
@@ -1653,6 +1665,10 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
   const std::string n(name);
   if (n == "stream_apply") {
     g_stream_apply = value != 0;
+  } else if (n == "stream_outer") {
+    g_stream_outer = value != 0;
+  } else if (n == "stream_outer_warps") {
+    M3_TRY(stream_set_outer_warps(value));
   } else if (n == "split_apply") {
     M->split_apply = value != 0;
     g_split_apply = value != 0;

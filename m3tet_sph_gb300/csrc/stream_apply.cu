@@ -279,19 +279,218 @@ __global__ void k_node_gather_f32(const int *__restrict__ ptr, const int *__rest
 }
 
 // ---------------------------------------------------------------------------------------
+// FP64-accurate operators, row-per-lane form: a stage holds 8 elements (one 128-byte TMA row per
+// packed row, 128-byte swizzle so the 16-byte piece of element e in row q sits at e ^ (q & 7)).
+// Each consumer warp owns whole stages; lane r < 30 forms output row r of each element,
+// y_r = sum_c K_rc x_c, reading K_rc from the packed lower triangle (k = pack(max, min)), with
+// x_c broadcast from shared memory. The code per element is 30 unrolled multiply-adds, so it stays
+// in the instruction cache; two elements are interleaved for instruction-level parallelism.
+// ---------------------------------------------------------------------------------------
+namespace sr {
+constexpr int E = 8;
+constexpr int NST = 7;
+constexpr int ARR = 15360;                    // array stride inside a stage (multiple of 1024)
+constexpr int KSTRIDE = 30720;                // stage stride
+constexpr int CBYTES = 10 * E * 4;
+template <int NCW> struct Map {
+  static constexpr int THREADS = 32 * (NCW + 1);
+  static constexpr int OFF_K = 0;
+  static constexpr int OFF_CONN = OFF_K + NST * KSTRIDE;
+  static constexpr int OFF_HDR = OFF_CONN + NST * CBYTES;
+  static constexpr int OFF_XS = OFF_HDR + 128;
+  static constexpr int OFF_BAR = OFF_XS + NCW * E * 30 * 8;
+  static constexpr int SMEM = OFF_BAR + 2 * NST * 8;
+  static constexpr int SMEM_ALLOC = SMEM + 1024;
+  static_assert(SMEM_ALLOC <= 232448, "shared memory budget");
+};
+}  // namespace sr
+
+struct RlDF {   // double-float: K_hi, K_lo as FP32 (117 float4 rows), x split into FP32 hi + lo
+  static constexpr int NARR = 2, ROWS = 117, V = 4;
+  static constexpr int ARR_BYTES = ROWS * 128;
+  struct Acc {
+    float h, l;
+  };
+  __device__ __forceinline__ static int base(int k) {
+    const int q = k >> 2;
+    return (q * 32 + (k & 3)) ^ ((q & 7) << 2);
+  }
+  __device__ __forceinline__ static int eshift(int e) { return e << 2; }
+  __device__ __forceinline__ static void mac(const unsigned char *st, int off, float2 xv, Acc &a) {
+    const float vh = reinterpret_cast<const float *>(st)[off];
+    const float vl = reinterpret_cast<const float *>(st + sr::ARR)[off];
+    df_mac(vh, vl, xv.x, xv.y, a.h, a.l);
+  }
+  __device__ __forceinline__ static float2 xsplit(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+  }
+  __device__ __forceinline__ static double finish(const Acc &a) { return (double)a.h + (double)a.l; }
+};
+struct RlF64 {  // FP64: K as 233 double2 rows
+  static constexpr int NARR = 1, ROWS = 233, V = 2;
+  static constexpr int ARR_BYTES = ROWS * 128;
+  struct Acc {
+    double h;
+  };
+  __device__ __forceinline__ static int base(int k) {
+    const int q = k >> 1;
+    return (q * 16 + (k & 1)) ^ ((q & 7) << 1);
+  }
+  __device__ __forceinline__ static int eshift(int e) { return e << 1; }
+  __device__ __forceinline__ static void mac(const unsigned char *st, int off, double xv, Acc &a) {
+    a.h = fma(reinterpret_cast<const double *>(st)[off], xv, a.h);
+  }
+  __device__ __forceinline__ static double xsplit(double v) { return v; }
+  __device__ __forceinline__ static double finish(const Acc &a) { return a.h; }
+};
+static_assert(RlDF::ARR_BYTES <= sr::ARR && RlF64::ARR_BYTES <= sr::KSTRIDE, "row-lane stage layout");
+static_assert(sizeof(decltype(RlDF::xsplit(0.0))) == 8 && sizeof(decltype(RlF64::xsplit(0.0))) == 8,
+              "x entries are 8 bytes in the per-warp buffer");
+
+template <class Op, int NCW>
+__global__ void __launch_bounds__(32 * (NCW + 1), 1)
+    k_stream_rowlane(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const int *__restrict__ conn, int nchunk, int nel, int *__restrict__ ticket,
+                     int *__restrict__ err, const double *__restrict__ x, double *__restrict__ ye) {
+  using namespace sr;
+  using Mp = Map<NCW>;
+  using XV = decltype(Op::xsplit(0.0));
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t bar0 = smem_u32(sm + Mp::OFF_BAR);
+  auto full = [&](int s) { return bar0 + 8u * s; };
+  auto empty = [&](int s) { return bar0 + 8u * (NST + s); };
+  int4 *hdr = reinterpret_cast<int4 *>(sm + Mp::OFF_HDR);
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  if (warp == NCW) {
+    // ---------------- producer ----------------
+    if (lane != 0) return;
+    const uint64_t pol = evict_first_policy();
+    int it = 0;
+    bool ok = true;
+    for (;; ++it) {
+      const int s = it % NST;
+      if (it >= NST && !mbar_wait(empty(s), ((it / NST) & 1) ^ 1)) {
+        ok = false;
+        break;
+      }
+      const int t = atomicAdd(ticket, 1);
+      if (t >= nchunk) break;
+      const int e0 = t * E;
+      hdr[s] = make_int4(e0, min(E, nel - e0), t, 0);
+      mbar_arrive_tx(full(s), CBYTES + Op::NARR * Op::ARR_BYTES);
+      bulk_load(smem_u32(sm + Mp::OFF_CONN + s * CBYTES), conn + (size_t)t * (10 * E), CBYTES, full(s));
+      const uint32_t dst = smem_u32(sm + Mp::OFF_K + s * KSTRIDE);
+      tma_load_2d(dst, &tmA, Op::V * e0, 0, full(s), pol);
+      if (Op::NARR == 2) tma_load_2d(dst + ARR, &tmB, Op::V * e0, 0, full(s), pol);
+    }
+    for (int j = 0; ok && j < NCW; ++j, ++it) {
+      const int s = it % NST;
+      if (it >= NST && !mbar_wait(empty(s), ((it / NST) & 1) ^ 1)) {
+        ok = false;
+        break;
+      }
+      hdr[s] = make_int4(0, -1, 0, 0);
+      mbar_arrive(full(s));
+    }
+    if (!ok) {
+      atomicOr(err, 1);
+      for (int j = 1; j <= NST && it - j >= 0; ++j) {
+        const int i2 = it - j;
+        mbar_wait(full(i2 % NST), (i2 / NST) & 1);
+      }
+    }
+    return;
+  }
+
+  // ---------------- consumers: one warp per stage ----------------
+  const int r = lane < 30 ? lane : 29;
+  int base[30];
+#pragma unroll
+  for (int c = 0; c < 30; ++c) base[c] = Op::base(r >= c ? pack_idx(r, c) : pack_idx(c, r));
+  XV *xs = reinterpret_cast<XV *>(sm + Mp::OFF_XS + warp * E * 30 * 8);
+  for (int it = warp;; it += NCW) {
+    const int s = it % NST;
+    const uint32_t par = (it / NST) & 1;
+    if (!__all_sync(0xffffffffu, mbar_wait(full(s), par))) {
+      if (lane == 0) atomicOr(err, 2);
+      break;
+    }
+    const int4 h = hdr[s];
+    if (h.y < 0) break;
+    const int *cs = reinterpret_cast<const int *>(sm + Mp::OFF_CONN + s * CBYTES);
+    if (lane < 30) {
+      double xv[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) xv[e] = e < h.y ? x[3 * cs[(lane / 3) * E + e] + lane % 3] : 0.0;
+#pragma unroll
+      for (int e = 0; e < E; ++e) xs[e * 30 + lane] = Op::xsplit(xv[e]);
+    }
+    __syncwarp();
+    const unsigned char *st = sm + Mp::OFF_K + s * KSTRIDE;
+    double *yo = ye + (size_t)h.x * 30;
+    for (int e = 0; e < h.y; e += 2) {
+      typename Op::Acc a0{}, a1{};
+      const int s0 = Op::eshift(e), s1 = Op::eshift(e + 1);
+      const XV *x0 = xs + e * 30, *x1 = x0 + 30;
+#pragma unroll
+      for (int c = 0; c < 30; ++c) {
+        Op::mac(st, base[c] ^ s0, x0[c], a0);
+        Op::mac(st, base[c] ^ s1, x1[c], a1);
+      }
+      if (lane < 30) {
+        yo[e * 30 + lane] = Op::finish(a0);
+        if (e + 1 < h.y) yo[(e + 1) * 30 + lane] = Op::finish(a1);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(empty(s));
+  }
+}
+
+__global__ void k_node_gather_f64(const int *__restrict__ ptr, const int *__restrict__ idx, int nnod,
+                                  const double *__restrict__ ye, double *__restrict__ y) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnod) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  const int b = ptr[n], e = ptr[n + 1];
+  for (int j = b; j < e; ++j) {
+    const double *p = ye + idx[j];
+    s0 += p[0];
+    s1 += p[1];
+    s2 += p[2];
+  }
+  y[3 * (size_t)n] = s0;
+  y[3 * (size_t)n + 1] = s1;
+  y[3 * (size_t)n + 2] = s2;
+}
+
+// ---------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------
-__global__ void k_chunk_conn(const int *__restrict__ el2nod, int nel, int nchunk, int *__restrict__ conn) {
+__global__ void k_chunk_conn(const int *__restrict__ el2nod, int nel, int nchunk, int E, int *__restrict__ conn) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= (size_t)nchunk * 10 * sa::E) return;
-  const int ch = (int)(i / (10 * sa::E)), r = (int)(i % (10 * sa::E)), n = r / sa::E, el = r % sa::E;
-  const int e = ch * sa::E + el;
+  if (i >= (size_t)nchunk * 10 * E) return;
+  const int ch = (int)(i / (10 * E)), r = (int)(i % (10 * E)), n = r / E, el = r % E;
+  const int e = ch * E + el;
   conn[i] = e < nel ? el2nod[(size_t)n * nel + e] : 0;
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static std::once_flag g_encode_once;
 static cudaError_t g_encode_status = cudaSuccess;
+
+template <class Op> static int rowlane_attrs();
 
 int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s) {
   std::call_once(g_encode_once, [] {
@@ -304,6 +503,7 @@ int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s) {
   if (g_encode_status != cudaSuccess || !g_encode) return cuda_fail(g_encode_status, "cuTensorMapEncodeTiled lookup");
   const int nel = L.nel, nnod = L.nnod;
   L.nchunk = (nel + sa::E - 1) / sa::E;
+  L.nchunk8 = (nel + sr::E - 1) / sr::E;
   // node -> (element, local node) table in stored element order
   std::vector<int> ptr(nnod + 1, 0), idx((size_t)nel * 10);
   for (int p = 0; p < nel; ++p)
@@ -314,17 +514,23 @@ int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s) {
     for (int n = 0; n < 10; ++n) idx[fill[L.h_el2nod_orig[(size_t)perm[p] * 10 + n]]++] = p * 30 + 3 * n;
   M3_CUDA(cudaMalloc(&L.chunk_conn, sizeof(int) * (size_t)L.nchunk * 10 * sa::E));
   M3_CUDA(cudaMalloc(&L.ye32, sizeof(float) * (size_t)nel * 30));
+  M3_CUDA(cudaMalloc(&L.chunk_conn8, sizeof(int) * (size_t)L.nchunk8 * 10 * sr::E));
+  M3_CUDA(cudaMalloc(&L.ye64, sizeof(double) * (size_t)nel * 30));
   M3_CUDA(cudaMalloc(&L.g_ptr, sizeof(int) * ptr.size()));
   M3_CUDA(cudaMalloc(&L.g_idx, sizeof(int) * idx.size()));
   M3_CUDA(cudaMalloc(&L.sa_err, sizeof(int) * 2));   // [0] error bits, [1] chunk ticket
   M3_CUDA(cudaMemcpyAsync(L.g_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, s));
   M3_CUDA(cudaMemcpyAsync(L.g_idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, s));
   M3_CUDA(cudaMemsetAsync(L.sa_err, 0, sizeof(int) * 2, s));
-  const size_t n = (size_t)L.nchunk * 10 * sa::E;
-  k_chunk_conn<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(L.el2nod, nel, L.nchunk, L.chunk_conn);
+  const size_t n = (size_t)L.nchunk * 10 * sa::E, n8 = (size_t)L.nchunk8 * 10 * sr::E;
+  k_chunk_conn<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(L.el2nod, nel, L.nchunk, sa::E, L.chunk_conn);
+  count_launch();
+  k_chunk_conn<<<(unsigned)((n8 + 255) / 256), 256, 0, s>>>(L.el2nod, nel, L.nchunk8, sr::E, L.chunk_conn8);
   count_launch();
   M3_CUDA(cudaGetLastError());
   M3_CUDA(cudaFuncSetAttribute(k_stream_elem_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, sa::SMEM_ALLOC));
+  M3_TRY(rowlane_attrs<RlDF>());
+  M3_TRY(rowlane_attrs<RlF64>());
   int dev = 0, nsm = 0;
   M3_CUDA(cudaGetDevice(&dev));
   M3_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -334,31 +540,41 @@ int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s) {
   return M3SPH_OK;
 }
 
-// 2D view of a packed FP32 operator [117 rows][4 nel floats]; box = 32 elements x 117 rows
-static int encode_k32(const Level &L, const float *K, CUtensorMap *map) {
-  const cuuint64_t dims[2] = {(cuuint64_t)L.nel * 4, (cuuint64_t)sa::ROWS};
+// 2D view of a packed operator [rows][V nel] of FP32 (V = 4) or FP64 (V = 2) values; a box covers
+// E elements x all rows
+static int encode_k(const Level &L, const void *K, bool f64, int rows, int E, CUtensorMap *map, bool swz = false) {
+  const int V = f64 ? 2 : 4;
+  const cuuint64_t dims[2] = {(cuuint64_t)L.nel * V, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)L.nel * 16};
-  const cuuint32_t box[2] = {4 * sa::E, sa::ROWS};
+  const cuuint32_t box[2] = {(cuuint32_t)(V * E), (cuuint32_t)rows};
   const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(K), dims, strides, box, estr,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  const CUresult r = g_encode(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                              const_cast<void *>(K), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return M3SPH_ERR_CUDA;
   }
   return M3SPH_OK;
 }
+static int encode_k32(const Level &L, const float *K, CUtensorMap *map) { return encode_k(L, K, false, sa::ROWS, sa::E, map); }
 
-int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
+static int stream_ready(const Level &L, const void *K) {
   if (!L.nchunk || !g_encode) {
     set_error("streamed apply not built for this level");
     return M3SPH_ERR_BAD_INPUT;
   }
-  if ((reinterpret_cast<uintptr_t>(K) & 15) != 0) {
-    set_error("streamed apply: element matrices not 16-byte aligned");
+  if (!K || (reinterpret_cast<uintptr_t>(K) & 15) != 0) {
+    set_error("streamed apply: element matrices missing or not 16-byte aligned");
     return M3SPH_ERR_BAD_INPUT;
   }
+  return M3SPH_OK;
+}
+
+int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
+  M3_TRY(stream_ready(L, K));
   CUtensorMap map;
   M3_TRY(encode_k32(L, K, &map));
   M3_CUDA(cudaMemsetAsync(L.sa_err + 1, 0, sizeof(int), s));
@@ -369,6 +585,71 @@ int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, c
   count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
+}
+
+// consumer warps per CTA of the row-per-lane kernels (4..6)
+static int g_rowlane_ncw = 6;
+int stream_set_outer_warps(int n) {
+  if (n < 4 || n > 6) {
+    set_error("stream_outer_warps must be 4, 5 or 6");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  g_rowlane_ncw = n;
+  return M3SPH_OK;
+}
+
+template <class Op, int NCW>
+static int rowlane_attr() {
+  M3_CUDA(cudaFuncSetAttribute(k_stream_rowlane<Op, NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               sr::Map<NCW>::SMEM_ALLOC));
+  return M3SPH_OK;
+}
+template <class Op>
+static int rowlane_attrs() {
+  M3_TRY((rowlane_attr<Op, 4>()));
+  M3_TRY((rowlane_attr<Op, 5>()));
+  M3_TRY((rowlane_attr<Op, 6>()));
+  return M3SPH_OK;
+}
+
+template <class Op, int NCW>
+static void rowlane_launch(const Level &L, const CUtensorMap &ma, const CUtensorMap &mb, const double *x, cudaStream_t s) {
+  k_stream_rowlane<Op, NCW><<<L.sa_grid, sr::Map<NCW>::THREADS, sr::Map<NCW>::SMEM_ALLOC, s>>>(
+      ma, mb, L.chunk_conn8, L.nchunk8, L.nel, L.sa_err + 1, L.sa_err, x, L.ye64);
+}
+
+template <class Op>
+static int rowlane_apply(const Level &L, const CUtensorMap &ma, const CUtensorMap &mb, const double *x, double *y,
+                         cudaStream_t s) {
+  M3_CUDA(cudaMemsetAsync(L.sa_err + 1, 0, sizeof(int), s));
+  switch (g_rowlane_ncw) {
+    case 5: rowlane_launch<Op, 5>(L, ma, mb, x, s); break;
+    case 6: rowlane_launch<Op, 6>(L, ma, mb, x, s); break;
+    default: rowlane_launch<Op, 4>(L, ma, mb, x, s); break;
+  }
+  count_launch();
+  k_node_gather_f64<<<(L.nnod + 255) / 256, 256, 0, s>>>(L.g_ptr, L.g_idx, L.nnod, L.ye64, y);
+  count_launch();
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+// y = (K_hi + K_lo) x with FP64 accuracy (double-float arithmetic)
+int stream_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s) {
+  M3_TRY(stream_ready(L, Kh));
+  M3_TRY(stream_ready(L, Kl));
+  CUtensorMap ma, mb;
+  M3_TRY(encode_k(L, Kh, false, RlDF::ROWS, sr::E, &ma, true));
+  M3_TRY(encode_k(L, Kl, false, RlDF::ROWS, sr::E, &mb, true));
+  return rowlane_apply<RlDF>(L, ma, mb, x, y, s);
+}
+
+// y = K x in FP64 from the FP64 element matrices
+int stream_apply_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s) {
+  M3_TRY(stream_ready(L, K));
+  CUtensorMap ma;
+  M3_TRY(encode_k(L, K, true, RlF64::ROWS, sr::E, &ma, true));
+  return rowlane_apply<RlF64>(L, ma, ma, x, y, s);
 }
 
 // reads (and clears) the error word of the streamed apply

@@ -232,7 +232,19 @@ def test_streamed_fp32_apply_many_chunks(built_lib):
         dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
         rng = np.random.default_rng(12)
         x = rng.standard_normal(3 * w['levels'][0]['nnod']).astype(np.float32)
-        y64 = dm2.level_apply(0, x.astype(np.float64))
+        y64s = dm2.level_apply(0, x.astype(np.float64))
+        assert np.array_equal(y64s, dm2.level_apply(0, x.astype(np.float64)))
+        ydfs = dm2.apply(x.astype(np.float64))
+        assert np.array_equal(ydfs, dm2.apply(x.astype(np.float64)))
+        try:
+            dm2.set_option("stream_outer", 0)
+            y64 = dm2.level_apply(0, x.astype(np.float64))
+            ydf = dm2.apply(x.astype(np.float64))
+        finally:
+            dm2.set_option("stream_outer", 1)
+        assert np.linalg.norm(y64s - y64) < 1e-14 * np.linalg.norm(y64)
+        assert np.linalg.norm(ydfs - ydf) < 1e-14 * np.linalg.norm(ydf)
+        assert np.linalg.norm(ydf - y64) < 1e-13 * np.linalg.norm(y64)
         ys, y_split = _stream_vs_split(dm2, x)
         assert np.array_equal(ys[0], ys[1])
         assert np.linalg.norm(ys[0] - y_split) < 1e-6 * np.linalg.norm(y_split)
