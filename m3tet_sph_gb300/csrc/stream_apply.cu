@@ -22,21 +22,25 @@
 namespace m3sph {
 namespace sa {
 constexpr int E = 32;                         // elements per chunk
-constexpr int NST = 3;                        // pipeline stages
+constexpr int NST = 3;                        // matrix stages
+constexpr int NCX = 3;                        // connectivity + gathered-x slots
 constexpr int NGRP = 2;                       // consumer groups of 4 warps
-constexpr int THREADS = NGRP * 128 + 32;      // + one producer warp
+constexpr int NGW = 2;                        // gather warps
+constexpr int THREADS = NGRP * 128 + NGW * 32 + 32;   // + one producer warp
 constexpr int ROWS = 117;                     // float4 rows of a packed FP32 element matrix
 constexpr int KBYTES = ROWS * E * 16;         // 59,904 B per stage
 constexpr int KSTRIDE = 60416;                // stage stride (multiple of 1024)
 constexpr int CBYTES = 10 * E * 4;            // connectivity of a chunk
+constexpr int XBYTES = 30 * E * 4;            // gathered x of a chunk
 constexpr int SY_LD = 33;
 constexpr int OFF_K = 0;
-constexpr int OFF_CONN = OFF_K + NST * KSTRIDE;
-constexpr int OFF_HDR = OFF_CONN + NST * CBYTES;
-constexpr int OFF_XS = OFF_HDR + 64;
-constexpr int OFF_SY = OFF_XS + NGRP * 30 * E * 4;
+constexpr int OFF_CX = OFF_K + NST * KSTRIDE;              // slot: connectivity, then x
+constexpr int OFF_HDR = OFF_CX + NCX * (CBYTES + XBYTES);
+constexpr int OFF_KTAG = OFF_HDR + 64;          // use tags of the matrix stages
+constexpr int OFF_SY = OFF_KTAG + 64;
 constexpr int OFF_BAR = OFF_SY + NGRP * 4 * 30 * SY_LD * 4;
-constexpr int SMEM = OFF_BAR + 3 * NST * 8;
+constexpr int NBAR = 2 * NST + 3 * NCX;
+constexpr int SMEM = OFF_BAR + NBAR * 8;
 constexpr int SMEM_ALLOC = SMEM + 1024;       // room to align the base to 1024 B
 constexpr unsigned long long TIMEOUT_NS = 1000000000ull;
 static_assert(SMEM_ALLOC <= 232448, "shared memory budget");
@@ -84,6 +88,19 @@ __device__ __forceinline__ uint64_t evict_first_policy() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
   return p;
+}
+// Wait for use u of a ring barrier when several waiters take turns on the ring: a waiter may run
+// a full ring ahead, and then the phase parity alone cannot tell use u from the still-pending use
+// u - depth. The producer writes the tag u before arming the barrier for use u, which it only does
+// after use u - depth has completed; so the tag is read first and the parity trusted after.
+__device__ __forceinline__ bool ring_wait(uint32_t bar, uint32_t parity, const volatile int *tag, int u) {
+  if (*tag == u && mbar_test(bar, parity)) return true;
+  const unsigned long long t0 = gtime();
+  for (;;) {
+    for (int i = 0; i < 32; ++i)
+      if (*tag == u && mbar_test(bar, parity)) return true;
+    if (gtime() - t0 > sa::TIMEOUT_NS) return false;
+  }
 }
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar,
                                             uint64_t policy) {
@@ -152,90 +169,130 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
   unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t bar0 = smem_u32(sm + OFF_BAR);
-  auto full_conn = [&](int s) { return bar0 + 8u * s; };
-  auto full_k = [&](int s) { return bar0 + 8u * (NST + s); };
-  auto empty = [&](int s) { return bar0 + 8u * (2 * NST + s); };
-  int4 *hdr = reinterpret_cast<int4 *>(sm + OFF_HDR);
+  // matrix ring: full_k / empty_k; slot ring: conn landed / x gathered / slot free
+  auto full_k = [&](int s) { return bar0 + 8u * s; };
+  auto empty_k = [&](int s) { return bar0 + 8u * (NST + s); };
+  auto cx_conn = [&](int j) { return bar0 + 8u * (2 * NST + j); };
+  auto cx_x = [&](int j) { return bar0 + 8u * (2 * NST + NCX + j); };
+  auto cx_empty = [&](int j) { return bar0 + 8u * (2 * NST + 2 * NCX + j); };
+  auto slot_conn = [&](int j) { return reinterpret_cast<int *>(sm + OFF_CX + j * (CBYTES + XBYTES)); };
+  auto slot_x = [&](int j) { return reinterpret_cast<float *>(sm + OFF_CX + j * (CBYTES + XBYTES) + CBYTES); };
+  int4 *hdr = reinterpret_cast<int4 *>(sm + OFF_HDR);   // {first element, count, ticket, use tag}
+  int *ktag = reinterpret_cast<int *>(sm + OFF_KTAG);
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
-      mbar_init(full_conn(s), 1);
       mbar_init(full_k(s), 1);
-      mbar_init(empty(s), 4);
+      mbar_init(empty_k(s), 4);
+      ktag[s] = -1;
+    }
+    for (int j = 0; j < NCX; ++j) {
+      hdr[j] = make_int4(0, 0, 0, -1);
+      mbar_init(cx_conn(j), 1);
+      mbar_init(cx_x(j), 1);
+      mbar_init(cx_empty(j), 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
-  if (warp == NGRP * 4) {
-    // ---------------- producer ----------------
+  const int gw0 = NGRP * 4;          // first gather warp
+  const int pw = gw0 + NGW;          // producer warp
+  if (warp == pw) {
+    // ---------------- producer: connectivity one chunk ahead of the matrices ----------------
     if (lane != 0) return;
     const uint64_t pol = evict_first_policy();
-    int it = 0;
     bool ok = true;
-    for (;; ++it) {
-      const int s = it % NST;
-      if (it >= NST && !mbar_wait(empty(s), ((it / NST) & 1) ^ 1)) {
+    auto issue_k = [&](int m) -> bool {
+      const int s = m % NST;
+      if (m >= NST && !mbar_wait(empty_k(s), ((m / NST) & 1) ^ 1)) return false;
+      reinterpret_cast<volatile int *>(ktag)[s] = m;
+      mbar_arrive_tx(full_k(s), KBYTES);
+      tma_load_2d(smem_u32(sm + OFF_K + s * KSTRIDE), &tmK, 4 * hdr[m % NCX].x, 0, full_k(s), pol);
+      return true;
+    };
+    int i = 0;
+    for (;; ++i) {
+      const int j = i % NCX;
+      if (i >= NCX && !mbar_wait(cx_empty(j), ((i / NCX) & 1) ^ 1)) {
         ok = false;
         break;
       }
       const int t = atomicAdd(ticket, 1);
       if (t >= nchunk) break;
       const int e0 = t * E;
-      hdr[s] = make_int4(e0, min(E, nel - e0), t, 0);
-      mbar_arrive_tx(full_conn(s), CBYTES);
-      bulk_load(smem_u32(sm + OFF_CONN + s * CBYTES), conn + (size_t)t * (10 * E), CBYTES, full_conn(s));
-      mbar_arrive_tx(full_k(s), KBYTES);
-      tma_load_2d(smem_u32(sm + OFF_K + s * KSTRIDE), &tmK, 4 * e0, 0, full_k(s), pol);
-    }
-    // one end marker per consumer group
-    for (int j = 0; ok && j < NGRP; ++j, ++it) {
-      const int s = it % NST;
-      if (it >= NST && !mbar_wait(empty(s), ((it / NST) & 1) ^ 1)) {
+      hdr[j] = make_int4(e0, min(E, nel - e0), t, i);
+      mbar_arrive_tx(cx_conn(j), CBYTES);
+      bulk_load(smem_u32(slot_conn(j)), conn + (size_t)t * (10 * E), CBYTES, cx_conn(j));
+      if (i >= 1 && !issue_k(i - 1)) {
         ok = false;
         break;
       }
-      hdr[s] = make_int4(0, -1, 0, 0);
-      mbar_arrive(full_conn(s));
+    }
+    if (ok && i >= 1 && !issue_k(i - 1)) ok = false;
+    // end markers: one per gather warp / consumer group (chunk indices i, i + 1)
+    for (int m = i; ok && m < i + NGRP; ++m) {
+      const int j = m % NCX;
+      if (m >= NCX && !mbar_wait(cx_empty(j), ((m / NCX) & 1) ^ 1)) {
+        ok = false;
+        break;
+      }
+      hdr[j] = make_int4(0, -1, 0, m);
+      mbar_arrive(cx_conn(j));
     }
     if (!ok) {
       atomicOr(err, 1);
       // let the copies already issued land before the block can exit
-      for (int j = 1; j <= NST && it - j >= 0; ++j) {
-        const int i2 = it - j, s = i2 % NST;
-        mbar_wait(full_conn(s), (i2 / NST) & 1);
-        mbar_wait(full_k(s), (i2 / NST) & 1);
+      for (int m = i - 1; m >= 0 && m >= i - NST; --m) mbar_wait(full_k(m % NST), (m / NST) & 1);
+      for (int m = i - 1; m >= 0 && m >= i - NCX; --m) mbar_wait(cx_conn(m % NCX), (m / NCX) & 1);
+    }
+    return;
+  }
+
+  if (warp >= gw0) {
+    // ---------------- gather warps: x of the chunk's 30 dofs per element ----------------
+    for (int m = warp - gw0;; m += NGW) {
+      const int j = m % NCX;
+      if (!__all_sync(0xffffffffu, ring_wait(cx_conn(j), (m / NCX) & 1, &hdr[j].w, m))) {
+        if (lane == 0) atomicOr(err, 16);
+        break;
       }
+      const int4 c = hdr[j];
+      if (c.y >= 0) {
+        const int *cs = slot_conn(j);
+        float *xs = slot_x(j);
+        float v[30];
+#pragma unroll
+        for (int q = 0; q < 30; ++q) v[q] = lane < c.y ? x[3 * cs[(q / 3) * E + lane] + q % 3] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 30; ++q) xs[q * E + lane] = v[q];
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(cx_x(j));
+      if (c.y < 0) break;
     }
     return;
   }
 
   // ---------------- consumers ----------------
   const int g = warp >> 2, w = warp & 3, t = tid & 127;
-  float *xs = reinterpret_cast<float *>(sm + OFF_XS) + g * 30 * E;
   float *sY = reinterpret_cast<float *>(sm + OFF_SY) + g * 4 * 30 * SY_LD;
-  for (int it = g;; it += NGRP) {
-    const int s = it % NST;
-    const uint32_t par = (it / NST) & 1;
-    // (also the barrier after the previous chunk's reads of xs and sY)
-    if (!group_and(g, mbar_wait(full_conn(s), par))) {
+  for (int m = g;; m += NGRP) {
+    const int j = m % NCX, s = m % NST;
+    // (also the barrier after the previous chunk's reads of sY)
+    if (!group_and(g, ring_wait(cx_x(j), (m / NCX) & 1, &hdr[j].w, m))) {
       if (t == 0) atomicOr(err, 2);
       break;
     }
-    const int4 c = hdr[s];
+    const int4 c = hdr[j];
     if (c.y < 0) break;
-    const int *cs = reinterpret_cast<const int *>(sm + OFF_CONN + s * CBYTES);
-    for (int i = t; i < 30 * E; i += 128) {
-      const int q = i >> 5, el = i & 31;
-      xs[i] = el < c.y ? x[3 * cs[(q / 3) * E + el] + q % 3] : 0.f;
-    }
-    group_sync(g);
+    const float *xs = slot_x(j);
     float xh[30], yv[30];
 #pragma unroll
     for (int q = 0; q < 30; ++q) {
       xh[q] = xs[q * E + lane];
       yv[q] = 0.f;
     }
-    const bool kok = mbar_wait(full_k(s), par);
+    const bool kok = ring_wait(full_k(s), (m / NST) & 1, &ktag[s], m);
     const float4 *rows = reinterpret_cast<const float4 *>(sm + OFF_K + s * KSTRIDE) + lane;
     switch (w) {
       case 0: part_mac<0>(rows, xh, yv); break;
@@ -244,7 +301,7 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
       default: part_mac<3>(rows, xh, yv); break;
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(empty(s));
+    if (lane == 0) mbar_arrive(empty_k(s));
 #pragma unroll
     for (int q = 0; q < 30; ++q) sY[(w * 30 + q) * SY_LD + lane] = yv[q];
     if (!group_and(g, kok)) {
@@ -257,6 +314,8 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
       const int el = i / 30, q = i - 30 * el;
       yo[i] = sY[q * SY_LD + el] + sY[(30 + q) * SY_LD + el] + sY[(60 + q) * SY_LD + el] + sY[(90 + q) * SY_LD + el];
     }
+    group_sync(g);
+    if (t == 0) mbar_arrive(cx_empty(j));
   }
 }
 
@@ -362,11 +421,12 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
   const uint32_t bar0 = smem_u32(sm + Mp::OFF_BAR);
   auto full = [&](int s) { return bar0 + 8u * s; };
   auto empty = [&](int s) { return bar0 + 8u * (NST + s); };
-  int4 *hdr = reinterpret_cast<int4 *>(sm + Mp::OFF_HDR);
+  int4 *hdr = reinterpret_cast<int4 *>(sm + Mp::OFF_HDR);   // {first element, count, ticket, use tag}
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(full(s), 1);
       mbar_init(empty(s), 1);
+      hdr[s] = make_int4(0, 0, 0, -1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -387,7 +447,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
       const int t = atomicAdd(ticket, 1);
       if (t >= nchunk) break;
       const int e0 = t * E;
-      hdr[s] = make_int4(e0, min(E, nel - e0), t, 0);
+      hdr[s] = make_int4(e0, min(E, nel - e0), t, it);
       mbar_arrive_tx(full(s), CBYTES + Op::NARR * Op::ARR_BYTES);
       bulk_load(smem_u32(sm + Mp::OFF_CONN + s * CBYTES), conn + (size_t)t * (10 * E), CBYTES, full(s));
       const uint32_t dst = smem_u32(sm + Mp::OFF_K + s * KSTRIDE);
@@ -400,7 +460,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
         ok = false;
         break;
       }
-      hdr[s] = make_int4(0, -1, 0, 0);
+      hdr[s] = make_int4(0, -1, 0, it);
       mbar_arrive(full(s));
     }
     if (!ok) {
@@ -422,7 +482,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
   for (int it = warp;; it += NCW) {
     const int s = it % NST;
     const uint32_t par = (it / NST) & 1;
-    if (!__all_sync(0xffffffffu, mbar_wait(full(s), par))) {
+    if (!__all_sync(0xffffffffu, ring_wait(full(s), par, &hdr[s].w, it))) {
       if (lane == 0) atomicOr(err, 2);
       break;
     }
