@@ -1667,7 +1667,7 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
     g_stream_apply = value != 0;
   } else if (n == "stream_outer") {
     g_stream_outer = value != 0;
-  } else if (n == "stream_outer_warps") {
+  } else if (n == "stream_outer_variant") {
     M3_TRY(stream_set_outer_warps(value));
   } else if (n == "split_apply") {
     M->split_apply = value != 0;

@@ -16,6 +16,7 @@
 #include <cudaTypedefs.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -407,8 +408,8 @@ static_assert(RlDF::ARR_BYTES <= sr::ARR && RlF64::ARR_BYTES <= sr::KSTRIDE, "ro
 static_assert(sizeof(decltype(RlDF::xsplit(0.0))) == 8 && sizeof(decltype(RlF64::xsplit(0.0))) == 8,
               "x entries are 8 bytes in the per-warp buffer");
 
-template <class Op, int NCW>
-__global__ void __launch_bounds__(32 * (NCW + 1), 1)
+template <class Op, int NCW, int EG, int SPLIT>
+__global__ void __launch_bounds__(32 * (NCW * SPLIT + 1), 1)
     k_stream_rowlane(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const int *__restrict__ conn, int nchunk, int nel, int *__restrict__ ticket,
                      int *__restrict__ err, const double *__restrict__ x, double *__restrict__ ye) {
@@ -425,14 +426,14 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(full(s), 1);
-      mbar_init(empty(s), 1);
+      mbar_init(empty(s), SPLIT);
       hdr[s] = make_int4(0, 0, 0, -1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
-  if (warp == NCW) {
+  if (warp == NCW * SPLIT) {
     // ---------------- producer ----------------
     if (lane != 0) return;
     const uint64_t pol = evict_first_policy();
@@ -473,13 +474,16 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
     return;
   }
 
-  // ---------------- consumers: one warp per stage ----------------
+  // ---------------- consumers: SPLIT warps per stage, each with E / SPLIT elements ----------------
+  constexpr int EW = E / SPLIT;
+  constexpr int EGI = EG < EW ? EG : EW;   // elements interleaved per pass
+  const int owner = warp / SPLIT, part = warp % SPLIT, eb = part * EW;
   const int r = lane < 30 ? lane : 29;
   int base[30];
 #pragma unroll
   for (int c = 0; c < 30; ++c) base[c] = Op::base(r >= c ? pack_idx(r, c) : pack_idx(c, r));
-  XV *xs = reinterpret_cast<XV *>(sm + Mp::OFF_XS + warp * E * 30 * 8);
-  for (int it = warp;; it += NCW) {
+  XV *xs = reinterpret_cast<XV *>(sm + Mp::OFF_XS + warp * EW * 30 * 8);
+  for (int it = owner;; it += NCW) {
     const int s = it % NST;
     const uint32_t par = (it / NST) & 1;
     if (!__all_sync(0xffffffffu, ring_wait(full(s), par, &hdr[s].w, it))) {
@@ -488,29 +492,32 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1)
     }
     const int4 h = hdr[s];
     if (h.y < 0) break;
+    const int ne = min(EW, h.y - eb);   // elements of this warp (may be <= 0 in the last chunk)
     const int *cs = reinterpret_cast<const int *>(sm + Mp::OFF_CONN + s * CBYTES);
     if (lane < 30) {
-      double xv[E];
+      double xv[EW];
 #pragma unroll
-      for (int e = 0; e < E; ++e) xv[e] = e < h.y ? x[3 * cs[(lane / 3) * E + e] + lane % 3] : 0.0;
+      for (int e = 0; e < EW; ++e) xv[e] = e < ne ? x[3 * cs[(lane / 3) * E + eb + e] + lane % 3] : 0.0;
 #pragma unroll
-      for (int e = 0; e < E; ++e) xs[e * 30 + lane] = Op::xsplit(xv[e]);
+      for (int e = 0; e < EW; ++e) xs[e * 30 + lane] = Op::xsplit(xv[e]);
     }
     __syncwarp();
     const unsigned char *st = sm + Mp::OFF_K + s * KSTRIDE;
-    double *yo = ye + (size_t)h.x * 30;
-    for (int e = 0; e < h.y; e += 2) {
-      typename Op::Acc a0{}, a1{};
-      const int s0 = Op::eshift(e), s1 = Op::eshift(e + 1);
-      const XV *x0 = xs + e * 30, *x1 = x0 + 30;
+    double *yo = ye + (size_t)(h.x + eb) * 30;
+    for (int e = 0; e < ne; e += EGI) {
+      typename Op::Acc a[EGI];
+#pragma unroll
+      for (int g = 0; g < EGI; ++g) a[g] = typename Op::Acc{};
+      const XV *xe = xs + e * 30;
 #pragma unroll
       for (int c = 0; c < 30; ++c) {
-        Op::mac(st, base[c] ^ s0, x0[c], a0);
-        Op::mac(st, base[c] ^ s1, x1[c], a1);
+#pragma unroll
+        for (int g = 0; g < EGI; ++g) Op::mac(st, base[c] ^ Op::eshift(eb + e + g), xe[g * 30 + c], a[g]);
       }
       if (lane < 30) {
-        yo[e * 30 + lane] = Op::finish(a0);
-        if (e + 1 < h.y) yo[(e + 1) * 30 + lane] = Op::finish(a1);
+#pragma unroll
+        for (int g = 0; g < EGI; ++g)
+          if (e + g < ne) yo[(e + g) * 30 + lane] = Op::finish(a[g]);
       }
     }
     __syncwarp();
@@ -647,34 +654,48 @@ int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, c
   return M3SPH_OK;
 }
 
-// consumer warps per CTA of the row-per-lane kernels (4..6)
-static int g_rowlane_ncw = 6;
+// row-per-lane kernels. Double-float: `owners` warps-groups own stages in turn, SPLIT warps share a
+// stage (E / SPLIT elements each), 2 elements interleaved; FP64: 6 owners, one warp per stage.
+struct RlShape {
+  int owners, split;
+};
+static const RlShape RL_DF_SHAPES[] = {{6, 1}, {6, 2}, {5, 2}, {4, 2}, {4, 4}, {5, 4}, {6, 4}, {3, 8}};
+static int g_rowlane_variant = 4;
 int stream_set_outer_warps(int n) {
-  if (n < 4 || n > 6) {
-    set_error("stream_outer_warps must be 4, 5 or 6");
+  if (n < 0 || n >= (int)(sizeof(RL_DF_SHAPES) / sizeof(RL_DF_SHAPES[0]))) {
+    set_error("stream_outer_variant out of range");
     return M3SPH_ERR_BAD_INPUT;
   }
-  g_rowlane_ncw = n;
+  g_rowlane_variant = n;
   return M3SPH_OK;
 }
 
-template <class Op, int NCW>
+template <class Op, int NCW, int SPLIT>
 static int rowlane_attr() {
-  M3_CUDA(cudaFuncSetAttribute(k_stream_rowlane<Op, NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  M3_CUDA(cudaFuncSetAttribute(k_stream_rowlane<Op, NCW, 2, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                sr::Map<NCW>::SMEM_ALLOC));
   return M3SPH_OK;
 }
 template <class Op>
 static int rowlane_attrs() {
-  M3_TRY((rowlane_attr<Op, 4>()));
-  M3_TRY((rowlane_attr<Op, 5>()));
-  M3_TRY((rowlane_attr<Op, 6>()));
-  return M3SPH_OK;
+  if constexpr (std::is_same<Op, RlF64>::value) {
+    return rowlane_attr<Op, 6, 1>();
+  } else {
+    M3_TRY((rowlane_attr<Op, 6, 1>()));
+    M3_TRY((rowlane_attr<Op, 6, 2>()));
+    M3_TRY((rowlane_attr<Op, 5, 2>()));
+    M3_TRY((rowlane_attr<Op, 4, 2>()));
+    M3_TRY((rowlane_attr<Op, 4, 4>()));
+    M3_TRY((rowlane_attr<Op, 5, 4>()));
+    M3_TRY((rowlane_attr<Op, 6, 4>()));
+    M3_TRY((rowlane_attr<Op, 3, 8>()));
+    return M3SPH_OK;
+  }
 }
 
-template <class Op, int NCW>
+template <class Op, int NCW, int SPLIT>
 static void rowlane_launch(const Level &L, const CUtensorMap &ma, const CUtensorMap &mb, const double *x, cudaStream_t s) {
-  k_stream_rowlane<Op, NCW><<<L.sa_grid, sr::Map<NCW>::THREADS, sr::Map<NCW>::SMEM_ALLOC, s>>>(
+  k_stream_rowlane<Op, NCW, 2, SPLIT><<<L.sa_grid, 32 * (NCW * SPLIT + 1), sr::Map<NCW>::SMEM_ALLOC, s>>>(
       ma, mb, L.chunk_conn8, L.nchunk8, L.nel, L.sa_err + 1, L.sa_err, x, L.ye64);
 }
 
@@ -682,10 +703,20 @@ template <class Op>
 static int rowlane_apply(const Level &L, const CUtensorMap &ma, const CUtensorMap &mb, const double *x, double *y,
                          cudaStream_t s) {
   M3_CUDA(cudaMemsetAsync(L.sa_err + 1, 0, sizeof(int), s));
-  switch (g_rowlane_ncw) {
-    case 5: rowlane_launch<Op, 5>(L, ma, mb, x, s); break;
-    case 6: rowlane_launch<Op, 6>(L, ma, mb, x, s); break;
-    default: rowlane_launch<Op, 4>(L, ma, mb, x, s); break;
+  if constexpr (std::is_same<Op, RlF64>::value) {
+    rowlane_launch<RlF64, 6, 1>(L, ma, mb, x, s);
+  } else {
+    switch (g_rowlane_variant) {
+      case 0: rowlane_launch<Op, 6, 1>(L, ma, mb, x, s); break;
+      case 2: rowlane_launch<Op, 5, 2>(L, ma, mb, x, s); break;
+      case 3: rowlane_launch<Op, 4, 2>(L, ma, mb, x, s); break;
+      case 4: rowlane_launch<Op, 4, 4>(L, ma, mb, x, s); break;
+      case 5: rowlane_launch<Op, 5, 4>(L, ma, mb, x, s); break;
+      case 6: rowlane_launch<Op, 6, 4>(L, ma, mb, x, s); break;
+      case 7: rowlane_launch<Op, 3, 8>(L, ma, mb, x, s); break;
+      case 1: rowlane_launch<Op, 6, 2>(L, ma, mb, x, s); break;
+      default: rowlane_launch<Op, 4, 4>(L, ma, mb, x, s); break;
+    }
   }
   count_launch();
   k_node_gather_f64<<<(L.nnod + 255) / 256, 256, 0, s>>>(L.g_ptr, L.g_idx, L.nnod, L.ye64, y);
