@@ -896,27 +896,34 @@ __global__ void k_bsr_assemble(const T *__restrict__ K, int nel, int nnzb, const
       }
   }
 #pragma unroll
-  for (int q = 0; q < 9; ++q) B[(size_t)k * 9 + q] = acc[q];
+  for (int q = 0; q < 9; ++q) B[(size_t)q * nnzb + k] = acc[q];   // [9][nnzb]
 }
 
+// y = B x for a 3x3-block CSR matrix with blocks stored [9][nnzb]: one warp per block row, lane l
+// takes blocks ptr[i] + l, ptr[i] + l + 32, ... (all loads of a warp coalesced), then a shuffle sum
 template <typename T>
-__global__ void __launch_bounds__(128) k_bsr_spmv(const int *__restrict__ ptr, const int *__restrict__ col,
-                                                  const T *__restrict__ B, int nrow, const T *__restrict__ x,
-                                                  T *__restrict__ y) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_bsr_spmv(const int *__restrict__ ptr, const int *__restrict__ col,
+                                                  const T *__restrict__ B, int nrow, size_t nnzb,
+                                                  const T *__restrict__ x, T *__restrict__ y) {
+  const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= nrow) return;
   T s0 = 0, s1 = 0, s2 = 0;
-  for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+  const int kb = ptr[i], ke = ptr[i + 1];
+  for (int k = kb + lane; k < ke; k += 32) {
     const int j = col[k];
-    const T *b = B + (size_t)k * 9;
     const T x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-    s0 += b[0] * x0 + b[1] * x1 + b[2] * x2;
-    s1 += b[3] * x0 + b[4] * x1 + b[5] * x2;
-    s2 += b[6] * x0 + b[7] * x1 + b[8] * x2;
+    s0 += B[k] * x0 + B[nnzb + k] * x1 + B[2 * nnzb + k] * x2;
+    s1 += B[3 * nnzb + k] * x0 + B[4 * nnzb + k] * x1 + B[5 * nnzb + k] * x2;
+    s2 += B[6 * nnzb + k] * x0 + B[7 * nnzb + k] * x1 + B[8 * nnzb + k] * x2;
   }
-  y[3 * i] = s0;
-  y[3 * i + 1] = s1;
-  y[3 * i + 2] = s2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if (lane < 3) y[3 * (size_t)i + lane] = lane == 0 ? s0 : lane == 1 ? s1 : s2;
 }
 
 template <typename T>
@@ -927,7 +934,9 @@ int bsr_assemble(const Level &L, const T *K, T *B, cudaStream_t s) {
 }
 template <typename T>
 int bsr_apply(const Level &L, const T *B, const T *x, T *y, cudaStream_t s) {
-  k_bsr_spmv<T><<<(L.nnod + 127) / 128, 128, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, x, y); count_launch();
+  k_bsr_spmv<T><<<(unsigned)(((size_t)L.nnod * 32 + 255) / 256), 256, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod,
+                                                                             (size_t)L.nnzb, x, y);
+  count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }

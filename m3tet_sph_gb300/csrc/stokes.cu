@@ -30,6 +30,8 @@ int ebe_apply_split_f64(const Level &L, const double *K, const double *x, double
 int ebe_apply_split_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
 int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s);
 int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s);
+int stream_apply_jac_f32(const Level &L, const float *K, float w, const float *r, const float *Di, float *d,
+                         cudaStream_t s);
 int stream_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
 int stream_apply_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
 int stream_check(const Level &L, cudaStream_t s);
@@ -867,6 +869,17 @@ template <typename T> static const T *levDi(const Level &L);
 template <> const double *levDi<double>(const Level &L) { return L.Dinv64; }
 template <> const float *levDi<float>(const Level &L) { return L.Dinv32; }
 
+// kd = K d, then d += w (r - kd) / diag; fused into one pass on the streamed finest level (kd is
+// then not written)
+template <typename T>
+static int level_op_jac(const Level &L, int img, T w, const T *r, T *d, T *kd, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (img == 0 && g_stream_apply && L.nchunk && L.K32) return stream_apply_jac_f32(L, L.K32, w, r, L.Dinv32, d, s);
+  }
+  M3_TRY(level_op<T>(L, img, d, kd, s));
+  return jac<T>(w, r, kd, levDi<T>(L), d, L.ndof, s);
+}
+
 template <typename T>
 static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std::vector<T *> &kd,
                     std::vector<T *> &tmp, const T *Ainv) {
@@ -892,11 +905,8 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
     } else {
       M3_TRY(jac_first<T>((T)w[0], r[j], levDi<T>(L), d[j], n, s));
+      for (int k = 1; k < 3; ++k) M3_TRY(level_op_jac<T>(L, j, (T)w[k], r[j], d[j], kd[j], s));
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
-      for (int k = 1; k < 3; ++k) {
-        M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
-        M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
-      }
     }
     M3_TRY(restrict_<T>(L, M->lev[j + 1], r[j], kd[j], r[j + 1], s));
   }
@@ -914,10 +924,7 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
       M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
     } else {
-      for (int k = 0; k < 3; ++k) {
-        M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
-        M3_TRY(jac<T>((T)w[k], r[j], kd[j], levDi<T>(L), d[j], n, s));
-      }
+      for (int k = 0; k < 3; ++k) M3_TRY(level_op_jac<T>(L, j, (T)w[k], r[j], d[j], kd[j], s));
     }
   }
   return M3SPH_OK;

@@ -525,6 +525,27 @@ __global__ void __launch_bounds__(32 * (NCW * SPLIT + 1), 1)
   }
 }
 
+// phase 2 fused with a weighted Jacobi sweep: (K d)_n is complete once gathered, so
+// d_n += w (r_n - (K d)_n) / diag_n follows in the same pass (d_n is read only by its own node)
+__global__ void k_node_gather_jac_f32(const int *__restrict__ ptr, const int *__restrict__ idx, int nnod,
+                                      const float *__restrict__ ye, float w, const float *__restrict__ r,
+                                      const float *__restrict__ Di, float *__restrict__ d) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnod) return;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  const int b = ptr[n], e = ptr[n + 1];
+  for (int j = b; j < e; ++j) {
+    const float *p = ye + idx[j];
+    s0 += p[0];
+    s1 += p[1];
+    s2 += p[2];
+  }
+  const size_t i = 3 * (size_t)n;
+  d[i] += w * (r[i] - s0) * Di[i];
+  d[i + 1] += w * (r[i + 1] - s1) * Di[i + 1];
+  d[i + 2] += w * (r[i + 2] - s2) * Di[i + 2];
+}
+
 __global__ void k_node_gather_f64(const int *__restrict__ ptr, const int *__restrict__ idx, int nnod,
                                   const double *__restrict__ ye, double *__restrict__ y) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -720,6 +741,22 @@ static int rowlane_apply(const Level &L, const CUtensorMap &ma, const CUtensorMa
   }
   count_launch();
   k_node_gather_f64<<<(L.nnod + 255) / 256, 256, 0, s>>>(L.g_ptr, L.g_idx, L.nnod, L.ye64, y);
+  count_launch();
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+// d += w (r - K d) / diag with K d from the streamed apply (one weighted Jacobi sweep)
+int stream_apply_jac_f32(const Level &L, const float *K, float w, const float *r, const float *Di, float *d,
+                         cudaStream_t s) {
+  M3_TRY(stream_ready(L, K));
+  CUtensorMap map;
+  M3_TRY(encode_k32(L, K, &map));
+  M3_CUDA(cudaMemsetAsync(L.sa_err + 1, 0, sizeof(int), s));
+  k_stream_elem_f32<<<L.sa_grid, sa::THREADS, sa::SMEM_ALLOC, s>>>(map, L.chunk_conn, L.nchunk, L.nel, L.sa_err + 1,
+                                                                    L.sa_err, d, L.ye32);
+  count_launch();
+  k_node_gather_jac_f32<<<(L.nnod + 255) / 256, 256, 0, s>>>(L.g_ptr, L.g_idx, L.nnod, L.ye32, w, r, Di, d);
   count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
