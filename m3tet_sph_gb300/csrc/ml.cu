@@ -185,10 +185,12 @@ __global__ void k_ml_gather(int nnod, int nel, const int *__restrict__ ptr, cons
     s1 += C[(size_t)(3 * a + 1) * nel + el];
     s2 += C[(size_t)(3 * a + 2) * nel + el];
   }
+  // a non-finite correction (an unusable network) is dropped; the outer CG's rate check then
+  // switches the smoother off
   const float w = 1.0f / (float)(e - b);
-  if (mask[3 * n]) d[3 * n] += (T)(w * s0);
-  if (mask[3 * n + 1]) d[3 * n + 1] += (T)(w * s1);
-  if (mask[3 * n + 2]) d[3 * n + 2] += (T)(w * s2);
+  if (mask[3 * n] && isfinite(s0)) d[3 * n] += (T)(w * s0);
+  if (mask[3 * n + 1] && isfinite(s1)) d[3 * n + 1] += (T)(w * s1);
+  if (mask[3 * n + 2] && isfinite(s2)) d[3 * n + 2] += (T)(w * s2);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -546,9 +548,12 @@ int ml_init_kernels() {
 bool ml_ready(m3sph_mesh *M) { return M->ml && mls(M)->trained; }
 
 // ---- training data: features of r and targets e_loc / s for every element of level 0 ----
+// Training pair of element e: features of the residual, and as target the element's error values scaled
+// like the network output (1 / local residual norm), zero on fixed dofs and clamped against outliers.
+constexpr float TARGET_CLIP = 20.f;
 __global__ void k_ml_samples(FeatLevel L, const double *__restrict__ r, const double *__restrict__ Dinv,
-                             const double *__restrict__ err, int stride, int offset, long base, long cap,
-                             __nv_bfloat16 *__restrict__ X, float *__restrict__ Tg) {
+                             const double *__restrict__ err, const uint8_t *__restrict__ mask, int stride, int offset,
+                             long base, long cap, __nv_bfloat16 *__restrict__ Xo, float *__restrict__ Tg) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int e = offset + i * stride;
   if (e >= L.nel) return;
@@ -556,11 +561,14 @@ __global__ void k_ml_samples(FeatLevel L, const double *__restrict__ r, const do
   if (row >= cap) return;
   __nv_bfloat16 xr[INP];
   const float s = element_features<double>(L, e, r, Dinv, xr);
-  for (int q = 0; q < INP; ++q) X[row * INP + q] = xr[q];
+  for (int q = 0; q < INP; ++q) Xo[row * INP + q] = xr[q];
   const float is = s > 0.f ? 1.0f / s : 0.f;
   for (int n = 0; n < 10; ++n) {
     const int nod = L.el2nod[(size_t)n * L.nel + e];
-    for (int c = 0; c < 3; ++c) Tg[row * OUTP + 3 * n + c] = (float)err[3 * nod + c] * is;
+    for (int c = 0; c < 3; ++c) {
+      const float t = mask[3 * (size_t)nod + c] ? (float)err[3 * (size_t)nod + c] * is : 0.f;
+      Tg[row * OUTP + 3 * n + c] = fminf(fmaxf(t, -TARGET_CLIP), TARGET_CLIP);
+    }
   }
   Tg[row * OUTP + 30] = 0.f;
   Tg[row * OUTP + 31] = 0.f;
@@ -573,8 +581,9 @@ int ml_add_samples(m3sph_mesh *M, const double *r, const double *err, int stride
   const long room = S->cap - S->count;
   if (room <= 0) return M3SPH_OK;
   FeatLevel f{L0.nel, L0.el2nod, S->lev[0].lvisc, S->lev[0].geo};
-  k_ml_samples<<<(n + 127) / 128, 128, 0, M->stream>>>(f, r, L0.Dinv64, err, stride, offset, S->count, S->cap, S->X,
-                                                        S->T); count_launch();
+  k_ml_samples<<<(n + 127) / 128, 128, 0, M->stream>>>(f, r, L0.Dinv64, err, L0.freemask, stride, offset, S->count,
+                                                        S->cap, S->X, S->T);
+  count_launch();
   M3_CUDA(cudaGetLastError());
   S->count = std::min<long>(S->cap, S->count + n);
   return M3SPH_OK;

@@ -1726,20 +1726,15 @@ extern "C" int m3sph_ml_collect(m3sph_mesh *M, uint64_t seed, int32_t n_iterates
   const size_t n = L0.ndof;
   const bool act = M->smoother_active;
   M->smoother_active = false;
-  k_rand_rhs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W->y, L0.freemask, n, seed); count_launch();
-  // converged reference solution of K x = b with the plain multigrid
-  M3_CUDA(cudaMemsetAsync(W->z, 0, sizeof(double) * n, s));
-  CGStats cs;
-  M3_TRY(mgpcg(M, W->y, W->z, 1e-10, false, 400, cs));
-  // plain-multigrid iterates from zero: pairs (residual, error)
-  M3_CUDA(cudaMemsetAsync(W->U, 0, sizeof(double) * n, s));
+  // pairs (r = K e, e) for white-noise errors e on the free dofs: the energy of such an error is spread
+  // over all modes, so most of it is determined by the local residual -- the network learns a local
+  // approximate inverse of the operator, which is what a smoother applies
   for (int k = 0; k < n_iterates; ++k) {
-    M3_TRY(outer_apply(M, W->U, W->r));
-    M3_TRY(sub_mask(W->y, W->r, L0.freemask, n, s));
-    k_diff<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W->z, W->U, W->tmp, n); count_launch();
+    k_rand_rhs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W->tmp, L0.freemask, n, seed * 1000003ull + k);
+    count_launch();
+    M3_TRY(outer_apply(M, W->tmp, W->r));
+    M3_TRY(apply_mask(W->r, L0.freemask, n, s));
     M3_TRY(ml_add_samples(M, W->r, W->tmp, stride, (int)((seed + k) % (uint64_t)stride)));
-    CGStats c1;
-    M3_TRY(mgpcg(M, W->y, W->U, 1e-300, true, 1, c1));
   }
   M3_CUDA(cudaStreamSynchronize(s));
   M->smoother_active = act;

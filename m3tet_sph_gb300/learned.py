@@ -74,7 +74,8 @@ def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_
     rng = np.random.default_rng(seed)
     nel = w['levels'][0]['nel']
     per_field = samples / n_fields
-    stride = max(1, int(np.ceil(nel * n_iterates / per_field)))
+    stride = max(1, int(nel * n_iterates // per_field))
+    dm.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=precision)
     L.check(L.lib().m3sph_ml_reserve(dm.h, int(samples) + nel))
     t0 = time.time()
     for i in range(n_fields):
@@ -98,3 +99,56 @@ def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_
             log(f"epoch {ep}: mse {mse.value:.5f}")
     t_train = time.time() - t0
     return get_params(dm), dict(mse=hist, t_collect=t_collect, t_train=t_train, stride=stride)
+
+
+def evaluate(dm, w, params=None, solver_kw=None, repeats=1):
+    """Solve once with the Jacobi smoother and once with the learned smoother on the mesh and fields
+    of workload `w` (FP32 V-cycle): iteration counts, times and the difference of the answers."""
+    kw = dict(rtol_Pat=1e-7, rtol_U=5e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=1e-8)
+    kw.update(solver_kw or {})
+    dm.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
+    if params is not None:
+        set_params(dm, params, trained=True)
+    out, sols = {}, {}
+    for name, sm in (('jacobi', 0), ('learned', 1)):
+        best = None
+        for _ in range(repeats):
+            info = dm.step_device(smoother=sm, **kw)
+            best = info if best is None or info['t_iter_ms'] < best['t_iter_ms'] else best
+        sols[name] = dm.solution()[0]
+        out[name] = dict(its=best['nitU'] + best['nitZ'], itPat=best['itPat'], t_iter_ms=best['t_iter_ms'],
+                         rel_residual=best['rel_residual'], fallbacks=best['smoother_fallbacks'])
+    out['dU'] = float(np.linalg.norm(sols['learned'] - sols['jacobi']) / np.linalg.norm(sols['jacobi']))
+    return out
+
+
+def main(argv=None):
+    import argparse
+    import json
+    from . import stokes
+    ap = argparse.ArgumentParser(description="train / evaluate the learned element smoother")
+    ap.add_argument("cmd", choices=["train", "evaluate"])
+    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--weights", required=True, help=".npy file written by train, read by evaluate")
+    ap.add_argument("--fields", type=int, default=20)
+    ap.add_argument("--samples", type=int, default=2_000_000)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    w = workloads.make_workload(a.workload, seed=a.seed)
+    dm = stokes.DeviceMesh(w['levels'])
+    try:
+        if a.cmd == "train":
+            p, h = train_smoother(dm, w, n_fields=a.fields, samples=a.samples, epochs=a.epochs, seed=a.seed,
+                                  log=lambda m: print(m, flush=True))
+            np.save(a.weights, p)
+            print(json.dumps({"mse": h["mse"], "t_collect_s": h["t_collect"], "t_train_s": h["t_train"],
+                              "stride": h["stride"]}))
+        else:
+            print(json.dumps({"workload": a.workload, **evaluate(dm, w, np.load(a.weights))}))
+    finally:
+        dm.close()
+
+
+if __name__ == "__main__":
+    main()
