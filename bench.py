@@ -8,8 +8,11 @@ operator, Galerkin hierarchy and coarse inverse from the resident inputs and run
 solve from P = 0 until the coupled FP64 residual is below 1e-8.
 
 Arms:
-  default (--impl gb300): FP32 V-cycle inside FP64 outer CG / Patera on the GPU (libm3sph.so).
-      The plain-FP64 GPU path (FP64 V-cycle) is timed on the same inputs for the comparison.
+  default (--impl gb300): FP32 V-cycle (weighted-Jacobi smoothing) inside FP64 outer CG / Patera on
+      the GPU (libm3sph.so); `value` is its solve time. The plain-FP64 GPU path (FP64 V-cycle) and the
+      same FP32 solve with the learned element smoother (weights trained on the 130k-DOF shell) are
+      timed on the same inputs for the comparison; semi-Lagrangian rates are measured on the 130k-DOF
+      shell (RK4 + cubic step, 16M-point location sweep).
   --impl reference: the FP64 CPU oracle (numpy/scipy restatement of the reference algorithm) on
       the host cores, on a bounded sample of the same workload, extrapolated to one solve.
 
@@ -113,6 +116,17 @@ def peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes per element of one streamed FP32 apply (both kernels), from the ncu capture of the
+# 491,520-element shell: (948.40 + 16.31 + 84.35 + 3.60) MB / 491,520
+TRAFFIC_PER_ELEMENT_F32 = (948.40e6 + 16.31e6 + 84.35e6 + 3.60e6) / 491520
+
+
+def apply_bytes_df(nel, ndof):
+    """Algorithmic bytes of one double-float outer apply: two FP32 packed matrices per element,
+    connectivity, x read and y written in FP64."""
+    return nel * (2 * 465 * 4 + 40) + 2 * 8 * ndof
+
+
 def apply_bytes(nel, ndof, s):
     """Algorithmic bytes of one element-by-element operator application: packed element
     matrices (465 values), connectivity (10 int32), x read and y written once."""
@@ -171,11 +185,27 @@ def run_gb300(args, rank, ws, td):
     ms = allmax(td, ms)
     clocks = clk.summary(dev)
     last = infos[-1]
-    # ---- operator roofline (FP32 EBE apply, dominant kernel of the V-cycle) ----
+    # ---- operator roofline: the finest-level FP32 apply (phase 1 k_stream_elem_f32 + phase 2
+    # k_node_gather_f32), the dominant unit of the V-cycle; and the double-float outer apply ----
     ms_apply32 = dm.apply_timing(0, 1, 10)
+    ms_apply_df = dm.apply_timing(0, 2, 10)
     hbm, peak_kind = peaks()
     b32 = apply_bytes(nel, ndof, 4)
     achieved = b32 / (ms_apply32 * 1e-3) / 1e9
+    # ---- learned element smoother (weights trained on the 130k-DOF shell), same solve ----
+    learned = None
+    wfile = ROOT / "m3tet_sph_gb300" / "smoother_c1.npy"
+    if not args.skip_learned and wfile.exists():
+        from m3tet_sph_gb300 import learned as LS
+        LS.set_params(dm, np.load(wfile), trained=True)
+        torch.cuda.synchronize()
+        tl = time.perf_counter()
+        li = dm.step_device(smoother=1, **SOLVER_KW)
+        torch.cuda.synchronize()
+        learned = {"s_per_solve": time.perf_counter() - tl, "nitU": li["nitU"], "nitZ": li["nitZ"],
+                   "itPat": li["itPat"], "rel_residual": li["rel_residual"],
+                   "smoother_fallbacks": li["smoother_fallbacks"],
+                   "weights": "trained on the 130,662-DOF shell, 20 viscosity fields (contrast 1e2-1e5), ~2M pairs"}
     # ---- end-to-end through the public API with host buffers ----
     U = np.empty(ndof)
     P = np.zeros(lv0["EL2NOD"][:, :4].max() + 1)
@@ -208,10 +238,18 @@ def run_gb300(args, rank, ws, td):
             "itPat": plain["info"]["itPat"], "nitU": plain["info"]["nitU"], "nitZ": plain["info"]["nitZ"],
             "t_setup_ms": plain["info"]["t_setup_ms"], "fp64_apply_ms": fp64_apply_ms,
             "speedup_mixed_vs_plain": plain["s_per_solve"] / (ms / 1e3)},
-        "roofline": {"bound": "hbm", "kernel": "k_ebe_apply<float> (all colours)", "achieved": achieved,
-                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
-                     "traffic": None, "bytes_per_apply": b32, "ms_per_apply": ms_apply32,
+        "roofline": {"bound": "hbm", "kernel": "finest-level FP32 apply: k_stream_elem_f32 + k_node_gather_f32",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
+                     "traffic": TRAFFIC_PER_ELEMENT_F32 * nel,
+                     "traffic_source": "ncu dram__bytes_read+write of both kernels on the 491,520-element shell, "
+                                       "scaled by element count",
+                     "bytes_per_apply": b32, "ms_per_apply": ms_apply32,
+                     "dof_per_s": ndof / (ms_apply32 * 1e-3),
+                     "outer_df_apply_ms": ms_apply_df,
+                     "outer_df_apply_gbs": apply_bytes_df(nel, ndof) / (ms_apply_df * 1e-3) / 1e9,
+                     "fp64_apply_ms": fp64_apply_ms if plain else None,
                      "fp64_apply_gbs": apply_bytes(nel, ndof, 8) / (fp64_apply_ms * 1e-3) / 1e9 if plain else None},
+        "learned_smoother": learned,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "rel_residual": einfo["rel_residual"]},
         "gpu_launches": int(launches),
@@ -219,8 +257,59 @@ def run_gb300(args, rank, ws, td):
         "cpu_baseline": cpu,
         "mesh_build_s": t_mesh,
     }
+    if rank == 0 and not args.skip_sl:
+        out["advection"] = sl_rates(args)
     if rank == 0:
         print(json.dumps(out))
+
+
+def shell_points(n, seed, r0=3480.0, r1=6371.0):
+    """(theta, phi, r) of n seeded points: directions uniform on the sphere, r uniform in volume."""
+    from m3tet_sph_gb300 import mesh as M
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=(3, n))
+    v /= np.linalg.norm(v, axis=0)
+    r = (r0 ** 3 + rng.uniform(size=n) * (r1 ** 3 - r0 ** 3)) ** (1.0 / 3.0)
+    r = np.clip(r, r0 + 1e-9 * (r1 - r0), r1 - 1e-9 * (r1 - r0))
+    return M.cart2sph(v * r)
+
+
+def sl_rates(args):
+    """Semi-Lagrangian rates on the 130k-DOF shell (public API, host buffers, copies included): one
+    advection step of T (RK4 over 3 substeps, curved-element location, cubic interpolation) in the
+    Stokes velocity at the CFL dt, and a seeded point-location sweep inside the shell."""
+    from m3tet_sph_gb300 import advection as A, stokes, workloads
+    w = workloads.make_workload("c1", seed=args.seed)
+    f = w["levels"][0]
+    dm = stokes.DeviceMesh(w["levels"])
+    try:
+        dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
+        U, _, _ = dm.solve(**SOLVER_KW)
+        Ux, Uy, Uz = U[0::3], U[1::3], U[2::3]
+        X, EL = f["GCOORD"], f["EL2NOD"]
+        hmin = min(np.linalg.norm(X[:, EL[:, a]] - X[:, EL[:, b]], axis=0).min()
+                   for a, b in ((0, 1), (1, 2), (2, 3), (3, 0), (0, 2), (1, 3)))
+        umax = np.sqrt(Ux ** 2 + Uy ** 2 + Uz ** 2).max()
+        dt = 0.5 * hmin / umax                                     # CFL number 0.5
+        MESH = dict(levels=w["levels"], device_mesh=dm, r_cmb=workloads.R_CMB, r_surf=workloads.R_SURF)
+        opts = dict(method_BT="RK4", method_interp="cubic")
+        A.advect3d_slm_p_sph(MESH, None, Ux, Uy, Uz, w["T"], dt, opts)
+        t = time.perf_counter()
+        _, WS = A.advect3d_slm_p_sph(MESH, None, Ux, Uy, Uz, w["T"], dt, opts)
+        t_sl = time.perf_counter() - t
+        pts = shell_points(args.sweep_points, args.seed + 3)
+        A.tsearch2_sph(dm, pts[:, :100000])
+        t = time.perf_counter()
+        _, _, info = A.tsearch2_sph(dm, pts)
+        t_loc = time.perf_counter() - t
+    finally:
+        dm.close()
+    n = f["nnod"]
+    return {"sl_step": {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {n} P2 nodes", "dt": dt,
+                        "method": "RK4 (3 substeps) + cubic", "s": t_sl, "departure_points_per_s": n / t_sl,
+                        "locate": WS["locate_info"]},
+            "location_sweep": {"points": args.sweep_points, "s": t_loc, "points_per_s": args.sweep_points / t_loc,
+                               "locate": info}}
 
 
 def run_operator_only(args, rank):
@@ -330,6 +419,9 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=988,
                     help="MG-PCG iterations the reference arm charges per solve (nitU + nitZ of the "
                          "plain-FP64 GPU solve of the 8M-DOF shell)")
+    ap.add_argument("--skip-learned", action="store_true")
+    ap.add_argument("--skip-sl", action="store_true")
+    ap.add_argument("--sweep-points", type=int, default=16_000_000)
     ap.add_argument("--op-only", action="store_true", help="time one level operator only (profiling)")
     ap.add_argument("--op-level", type=int, default=0)
     ap.add_argument("--op-precision", type=int, default=1)
