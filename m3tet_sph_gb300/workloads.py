@@ -156,4 +156,4 @@ def make_workload(name, seed=0, nmg=None, level=None, nlayer=None):
     dens = density(T)
     ifix, vfix = boundary_conditions(levels[0], bc, seed)
     return dict(name=name, levels=levels, visc=visc, dens=dens, T=T, ifix=ifix, vfix=vfix, phys=physics(),
-                level=L, nlayer=n, nmg=g)
+                level=L, nlayer=n, nmg=g, contrast=contrast)
