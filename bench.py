@@ -154,7 +154,7 @@ def run_gb300(args, rank, ws, td):
     plain = None
     if not args.skip_plain:
         setup(0)
-        for _ in range(max(1, args.plain_warmup)):
+        for _ in range(args.plain_warmup):
             info64 = dm.step_device(**SOLVER_KW)
         barrier(td)
         torch.cuda.synchronize()
