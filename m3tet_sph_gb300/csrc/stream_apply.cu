@@ -24,7 +24,7 @@ namespace m3sph {
 namespace sa {
 constexpr int E = 32;                         // elements per chunk
 constexpr int NST = 3;                        // matrix stages
-constexpr int NCX = 3;                        // connectivity + gathered-x slots
+constexpr int NCX = 6;                        // connectivity + gathered-x slots
 constexpr int NGRP = 2;                       // consumer groups of 4 warps
 constexpr int NGW = 2;                        // gather warps
 constexpr int THREADS = NGRP * 128 + NGW * 32 + 32;   // + one producer warp
@@ -37,15 +37,17 @@ constexpr int SY_LD = 33;
 constexpr int OFF_K = 0;
 constexpr int OFF_CX = OFF_K + NST * KSTRIDE;              // slot: connectivity, then x
 constexpr int OFF_HDR = OFF_CX + NCX * (CBYTES + XBYTES);
-constexpr int OFF_KTAG = OFF_HDR + 64;          // use tags of the matrix stages
-constexpr int OFF_SY = OFF_KTAG + 64;
-constexpr int OFF_BAR = OFF_SY + NGRP * 4 * 30 * SY_LD * 4;
+constexpr int HDR_BYTES = ((16 * NCX + 63) / 64) * 64;   // one int4 header per slot
+constexpr int OFF_KTAG = OFF_HDR + HDR_BYTES;  // use tags of the matrix stages
+constexpr int OFF_BAR = OFF_KTAG + 64;        // (the partial sums of a chunk reuse its matrix stage)
 constexpr int NBAR = 2 * NST + 3 * NCX;
 constexpr int SMEM = OFF_BAR + NBAR * 8;
 constexpr int SMEM_ALLOC = SMEM + 1024;       // room to align the base to 1024 B
 constexpr unsigned long long TIMEOUT_NS = 1000000000ull;
 static_assert(SMEM_ALLOC <= 232448, "shared memory budget");
 static_assert(KBYTES <= KSTRIDE && KSTRIDE % 1024 == 0, "stage layout");
+static_assert(4 * 30 * SY_LD * 4 <= KBYTES, "partial sums fit in a matrix stage");
+static_assert(16 * NCX <= HDR_BYTES && 4 * NST <= 64, "header and tag areas");
 }  // namespace sa
 
 namespace {
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(full_k(s), 1);
-      mbar_init(empty_k(s), 4);
+      mbar_init(empty_k(s), 1);
       ktag[s] = -1;
     }
     for (int j = 0; j < NCX; ++j) {
@@ -276,10 +278,8 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
 
   // ---------------- consumers ----------------
   const int g = warp >> 2, w = warp & 3, t = tid & 127;
-  float *sY = reinterpret_cast<float *>(sm + OFF_SY) + g * 4 * 30 * SY_LD;
   for (int m = g;; m += NGRP) {
     const int j = m % NCX, s = m % NST;
-    // (also the barrier after the previous chunk's reads of sY)
     if (!group_and(g, ring_wait(cx_x(j), (m / NCX) & 1, &hdr[j].w, m))) {
       if (t == 0) atomicOr(err, 2);
       break;
@@ -294,29 +294,35 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
       yv[q] = 0.f;
     }
     const bool kok = ring_wait(full_k(s), (m / NST) & 1, &ktag[s], m);
-    const float4 *rows = reinterpret_cast<const float4 *>(sm + OFF_K + s * KSTRIDE) + lane;
+    unsigned char *stage = sm + OFF_K + s * KSTRIDE;
+    const float4 *rows = reinterpret_cast<const float4 *>(stage) + lane;
     switch (w) {
       case 0: part_mac<0>(rows, xh, yv); break;
       case 1: part_mac<1>(rows, xh, yv); break;
       case 2: part_mac<2>(rows, xh, yv); break;
       default: part_mac<3>(rows, xh, yv); break;
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(empty_k(s));
-#pragma unroll
-    for (int q = 0; q < 30; ++q) sY[(w * 30 + q) * SY_LD + lane] = yv[q];
+    // every warp has its x in registers and is done with the matrix rows
     if (!group_and(g, kok)) {
       if (t == 0) atomicOr(err, 4);
       break;
     }
+    if (t == 0) mbar_arrive(cx_empty(j));
+    // the four partial sums go into the consumed stage; it is released after the outputs are written
+    float *sY = reinterpret_cast<float *>(stage);
+#pragma unroll
+    for (int q = 0; q < 30; ++q) sY[(w * 30 + q) * SY_LD + lane] = yv[q];
+    group_sync(g);
     // element outputs, 30 consecutive values per element (contiguous over the chunk)
     float *yo = ye + (size_t)c.x * 30;
     for (int i = t; i < 30 * c.y; i += 128) {
       const int el = i / 30, q = i - 30 * el;
       yo[i] = sY[q * SY_LD + el] + sY[(30 + q) * SY_LD + el] + sY[(60 + q) * SY_LD + el] + sY[(90 + q) * SY_LD + el];
     }
+    // order this thread's generic writes to the stage before the next TMA write into it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     group_sync(g);
-    if (t == 0) mbar_arrive(cx_empty(j));
+    if (t == 0) mbar_arrive(empty_k(s));
   }
 }
 
