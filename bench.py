@@ -117,8 +117,8 @@ def peaks():
 
 
 # DRAM bytes per element of one streamed FP32 apply (both kernels), from the ncu capture of the
-# 491,520-element shell: (948.40 + 16.31 + 84.35 + 3.60) MB / 491,520
-TRAFFIC_PER_ELEMENT_F32 = (948.40e6 + 16.31e6 + 84.35e6 + 3.60e6) / 491520
+# 491,520-element shell: (948.77 + 20.58 + 84.51 + 3.46) MB / 491,520
+TRAFFIC_PER_ELEMENT_F32 = (948.77e6 + 20.58e6 + 84.51e6 + 3.46e6) / 491520
 
 
 def apply_bytes_df(nel, ndof):
