@@ -163,6 +163,7 @@ def run_gb300(args, rank, ws, td):
         torch.cuda.synchronize()
         t_plain = allmax(td, (time.perf_counter() - t) / args.plain_steps)
         plain = dict(s_per_solve=t_plain, info=infos64[-1])
+        U64, P64 = dm.solution()
         fp64_apply_ms = dm.apply_timing(0, 0, 5)
     # ---- mixed path (the product): timed region ----
     setup(1)
@@ -182,6 +183,12 @@ def run_gb300(args, rank, ws, td):
         ev1.synchronize()
     launches = _lib.launch_count() - n0
     ms = ev0.elapsed_time(ev1) / args.steps
+    accuracy = None
+    if plain is not None:
+        Um, Pm = dm.solution()
+        Pc, Pc64 = Pm - Pm.mean(), P64 - P64.mean()
+        accuracy = {"dU_rel_l2_vs_plain_fp64": float(np.linalg.norm(Um - U64) / np.linalg.norm(U64)),
+                    "dP_rel_l2_vs_plain_fp64": float(np.linalg.norm(Pc - Pc64) / np.linalg.norm(Pc64))}
     ms = allmax(td, ms)
     clocks = clk.summary(dev)
     last = infos[-1]
@@ -252,6 +259,7 @@ def run_gb300(args, rank, ws, td):
                      "fp64_apply_ms": fp64_apply_ms if plain else None,
                      "fp64_apply_gbs": apply_bytes(nel, ndof, 8) / (fp64_apply_ms * 1e-3) / 1e9 if plain else None},
         "learned_smoother": learned,
+        "accuracy": accuracy,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "rel_residual": einfo["rel_residual"]},
         "gpu_launches": int(launches),
