@@ -237,14 +237,18 @@ template int jac<float>(float, const float *, const float *, const float *, floa
 // transfer: restriction rc = Ic2f' (r0 - Kd) (gather over coarse rows), prolongation
 // d_f += Ic2f d_c (gather over fine rows); both masked to free dofs
 // ---------------------------------------------------------------------------------------
+// one warp per coarse row: lane l takes fine entries ptr[i] + l, + 32, ... (coarse rows gather ~40
+// fine nodes), then a shuffle sum
 template <typename T>
-__global__ void k_restrict(const int *__restrict__ ptr, const int *__restrict__ col, const float *__restrict__ w,
-                           int nrow, const T *__restrict__ a, const T *__restrict__ b, const uint8_t *__restrict__ mask,
-                           T *__restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_restrict(const int *__restrict__ ptr, const int *__restrict__ col,
+                                                  const float *__restrict__ w, int nrow, const T *__restrict__ a,
+                                                  const T *__restrict__ b, const uint8_t *__restrict__ mask,
+                                                  T *__restrict__ out) {
+  const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= nrow) return;
   T s0 = 0, s1 = 0, s2 = 0;
-  for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+  for (int k = ptr[i] + lane; k < ptr[i + 1]; k += 32) {
     const int j = col[k];
     const T wk = (T)w[k];
     if (b) {
@@ -257,9 +261,16 @@ __global__ void k_restrict(const int *__restrict__ ptr, const int *__restrict__ 
       s2 += wk * a[3 * j + 2];
     }
   }
-  out[3 * i] = mask[3 * i] ? s0 : T(0);
-  out[3 * i + 1] = mask[3 * i + 1] ? s1 : T(0);
-  out[3 * i + 2] = mask[3 * i + 2] ? s2 : T(0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if (lane < 3) {
+    const T v = lane == 0 ? s0 : lane == 1 ? s1 : s2;
+    out[3 * (size_t)i + lane] = mask[3 * (size_t)i + lane] ? v : T(0);
+  }
 }
 // out = add + P xc (masked); add may alias out
 template <typename T>
@@ -283,7 +294,9 @@ __global__ void k_prolong(const int *__restrict__ ptr, const int *__restrict__ c
 }
 template <typename T>
 int restrict_(const Level &F, const Level &C, const T *a, const T *b, T *out, cudaStream_t s) {
-  k_restrict<T><<<(C.nnod + 255) / 256, 256, 0, s>>>(F.R_ptr, F.R_col, F.R_w, C.nnod, a, b, C.freemask, out); count_launch();
+  k_restrict<T><<<(unsigned)(((size_t)C.nnod * 32 + 255) / 256), 256, 0, s>>>(F.R_ptr, F.R_col, F.R_w, C.nnod, a, b,
+                                                                             C.freemask, out);
+  count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
