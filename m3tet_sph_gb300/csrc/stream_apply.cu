@@ -334,10 +334,14 @@ __global__ void k_node_gather_f32(const int *__restrict__ ptr, const int *__rest
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
   const int b = ptr[n], e = ptr[n + 1];
   for (int j = b; j < e; ++j) {
-    const float *p = ye + idx[j];
-    s0 += p[0];
-    s1 += p[1];
-    s2 += p[2];
+    // the triple starts at 30 e + 3 n: 8-byte aligned for even n; one 8-byte and one 4-byte load
+    // at per-thread offsets (no branch)
+    const int o = idx[j], odd = o & 1;
+    const float2 v2 = *reinterpret_cast<const float2 *>(ye + o + odd);
+    const float v1 = ye[o + 2 * (1 - odd)];
+    s0 += odd ? v1 : v2.x;
+    s1 += odd ? v2.x : v2.y;
+    s2 += odd ? v2.y : v1;
   }
   y[3 * (size_t)n] = s0;
   y[3 * (size_t)n + 1] = s1;
@@ -541,10 +545,14 @@ __global__ void k_node_gather_jac_f32(const int *__restrict__ ptr, const int *__
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
   const int b = ptr[n], e = ptr[n + 1];
   for (int j = b; j < e; ++j) {
-    const float *p = ye + idx[j];
-    s0 += p[0];
-    s1 += p[1];
-    s2 += p[2];
+    // the triple starts at 30 e + 3 n: 8-byte aligned for even n; one 8-byte and one 4-byte load
+    // at per-thread offsets (no branch)
+    const int o = idx[j], odd = o & 1;
+    const float2 v2 = *reinterpret_cast<const float2 *>(ye + o + odd);
+    const float v1 = ye[o + 2 * (1 - odd)];
+    s0 += odd ? v1 : v2.x;
+    s1 += odd ? v2.x : v2.y;
+    s2 += odd ? v2.y : v1;
   }
   const size_t i = 3 * (size_t)n;
   d[i] += w * (r[i] - s0) * Di[i];
@@ -559,10 +567,12 @@ __global__ void k_node_gather_f64(const int *__restrict__ ptr, const int *__rest
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   const int b = ptr[n], e = ptr[n + 1];
   for (int j = b; j < e; ++j) {
-    const double *p = ye + idx[j];
-    s0 += p[0];
-    s1 += p[1];
-    s2 += p[2];
+    const int o = idx[j], odd = o & 1;   // 16-byte aligned pair for even n, as in the FP32 gather
+    const double2 v2 = *reinterpret_cast<const double2 *>(ye + o + odd);
+    const double v1 = ye[o + 2 * (1 - odd)];
+    s0 += odd ? v1 : v2.x;
+    s1 += odd ? v2.x : v2.y;
+    s2 += odd ? v2.y : v1;
   }
   y[3 * (size_t)n] = s0;
   y[3 * (size_t)n + 1] = s1;
