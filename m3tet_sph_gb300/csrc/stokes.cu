@@ -776,8 +776,8 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   if (nfix) k_scatter_vals<<<(nfix + 255) / 256, 256, 0, s>>>(M->Ufix, d_fix, d_vals, nfix); count_launch();
   M3_CUDA(cudaMemcpyAsync(M->fin.visc, Visc, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
   M3_CUDA(cudaMemcpyAsync(M->fin.dens, Dens, sizeof(double) * L0.nnod, cudaMemcpyHostToDevice, s));
-  int nfree = 0;
   {
+    // free-dof counts per level
     std::vector<uint8_t> fm(L0.ndof, 1);
     for (int i : fx) fm[i] = 0;
     for (int i = 0; i < M->nmg; ++i) {
@@ -785,9 +785,7 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
       for (int d = 0; d < M->lev[i].ndof; ++d) c += fm[d];
       M->lev[i].nfree = c;
     }
-    nfree = M->lev[0].nfree;
   }
-  (void)nfree;
   M->phys = *phys;
   M3_TRY(ml_features(M, Visc));
   M3_CUDA(cudaStreamSynchronize(s));
