@@ -892,7 +892,12 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     const Level &L = M->lev[j];
     const double *w = j == 0 ? WD0 : WDc;
     const size_t n = L.ndof;
-    if (ml && j < 2) {
+    if (ml && j < 2 && M->ml_schedule == 1) {
+      // one learned sweep from zero, then the residual for the restriction
+      M3_CUDA(cudaMemsetAsync(d[j], 0, sizeof(T) * n, s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], nullptr, levDi<T>(L), tmp[j], d[j]));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+    } else if (ml && j < 2) {
       // learned sweep, weighted Jacobi sweep, learned sweep
       M3_CUDA(cudaMemsetAsync(d[j], 0, sizeof(T) * n, s));
       M3_TRY(ml_sweep<T>(M, j, r[j], nullptr, levDi<T>(L), tmp[j], d[j]));
@@ -914,7 +919,10 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     const double *w = j == 0 ? WU0 : WUc;
     const size_t n = L.ndof;
     M3_TRY(prolong<T>(L, M->lev[j + 1], d[j + 1], d[j], d[j], s));
-    if (ml && j < 2) {
+    if (ml && j < 2 && M->ml_schedule == 1) {
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
+    } else if (ml && j < 2) {
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
       M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
@@ -1670,6 +1678,12 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
   const std::string n(name);
   if (n == "stream_apply") {
     g_stream_apply = value != 0;
+  } else if (n == "ml_schedule") {
+    if (value < 0 || value > 1) {
+      set_error("ml_schedule must be 0 or 1");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    M->ml_schedule = value;
   } else if (n == "stream_outer") {
     g_stream_outer = value != 0;
   } else if (n == "stream_outer_variant") {

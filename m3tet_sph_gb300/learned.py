@@ -101,7 +101,7 @@ def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_
     return get_params(dm), dict(mse=hist, t_collect=t_collect, t_train=t_train, stride=stride)
 
 
-def evaluate(dm, w, params=None, solver_kw=None, repeats=1):
+def evaluate(dm, w, params=None, solver_kw=None, repeats=1, schedule=0):
     """Solve once with the Jacobi smoother and once with the learned smoother on the mesh and fields
     of workload `w` (FP32 V-cycle): iteration counts, times and the difference of the answers."""
     kw = dict(rtol_Pat=1e-7, rtol_U=5e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=1e-8)
@@ -109,7 +109,8 @@ def evaluate(dm, w, params=None, solver_kw=None, repeats=1):
     dm.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
     if params is not None:
         set_params(dm, params, trained=True)
-    out, sols = {}, {}
+    dm.set_option("ml_schedule", schedule)
+    out, sols = {"schedule": schedule}, {}
     for name, sm in (('jacobi', 0), ('learned', 1)):
         best = None
         for _ in range(repeats):
@@ -134,6 +135,7 @@ def main(argv=None):
     ap.add_argument("--samples", type=int, default=2_000_000)
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--schedule", type=int, default=0, help="0: learned-Jacobi-learned per side, 1: one learned sweep")
     a = ap.parse_args(argv)
     w = workloads.make_workload(a.workload, seed=a.seed)
     dm = stokes.DeviceMesh(w['levels'])
@@ -145,7 +147,7 @@ def main(argv=None):
             print(json.dumps({"mse": h["mse"], "t_collect_s": h["t_collect"], "t_train_s": h["t_train"],
                               "stride": h["stride"]}))
         else:
-            print(json.dumps({"workload": a.workload, **evaluate(dm, w, np.load(a.weights))}))
+            print(json.dumps({"workload": a.workload, **evaluate(dm, w, np.load(a.weights), schedule=a.schedule)}))
     finally:
         dm.close()
 
