@@ -167,14 +167,20 @@ M3SPH_API int m3sph_ml_train_epoch(m3sph_mesh *mesh, int32_t batch, float lr, ui
 M3SPH_API int m3sph_ml_gradients(m3sph_mesh *mesh, const float *X, const float *T, int32_t n, float *grad, double *loss);
 M3SPH_API int m3sph_ml_forward(m3sph_mesh *mesh, const float *X, int32_t n, float *Y);
 
-/* Kernel-variant switches for measurement and tests: "split_apply" (4-warp split element
- * kernels, default 1), "graphs" (CUDA-graph replay of MG-PCG iterations, default 1),
- * "df_outer" (double-float outer operator on the mixed path, default 1). */
+/* Kernel-variant switches for measurement and tests (per process, results equal to rounding):
+ * "stream_apply" (streamed finest-level FP32 operator, default 1; 0: one launch per colour),
+ * "stream_outer" (streamed double-float / FP64 finest-level operators, default 1),
+ * "stream_outer_variant" (warp layout of the double-float kernel, 0-7, default 4),
+ * "split_apply" (4-warp per-colour kernels when streaming is off, default 1), "graphs" (CUDA-graph
+ * replay of MG-PCG iterations, default 1), "df_outer" (double-float outer operator on the mixed
+ * path, default 1), "ml_schedule" (learned smoothing: 0 learned-Jacobi-learned, 1 one learned
+ * sweep per side; per handle). */
 M3SPH_API int m3sph_set_option(m3sph_mesh *mesh, const char *name, int32_t value);
 /* Cumulative number of CUDA kernels this library has launched (all handles). */
 M3SPH_API int m3sph_launch_count(unsigned long long *count);
-/* Operator benchmark: nrep device-resident applications of the level-`img` element operator in
- * FP64 (precision 0) or FP32 (1); returns the mean time per full application (all colours). */
+/* Operator benchmark: nrep device-resident applications of the level-`img` operator in FP64
+ * (precision 0), FP32 (1) or, on the finest level, double-float (2); returns the mean time per
+ * full application. */
 M3SPH_API int m3sph_apply_timing(m3sph_mesh *mesh, int32_t img, int32_t precision, int32_t nrep, double *ms_per_apply);
 
 /* Replaces tsearch2_sph + local_coords_3d_sph (tsearch2_sph.m:1-424, local_coords_3d_sph.m:28-147):
