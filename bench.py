@@ -292,21 +292,27 @@ def sl_rates(args):
     w = workloads.make_workload("c1", seed=args.seed)
     f = w["levels"][0]
     dm = stokes.DeviceMesh(w["levels"])
+    step = None
     try:
-        dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
-        U, _, _ = dm.solve(**SOLVER_KW)
-        Ux, Uy, Uz = U[0::3], U[1::3], U[2::3]
-        X, EL = f["GCOORD"], f["EL2NOD"]
-        hmin = min(np.linalg.norm(X[:, EL[:, a]] - X[:, EL[:, b]], axis=0).min()
-                   for a, b in ((0, 1), (1, 2), (2, 3), (3, 0), (0, 2), (1, 3)))
-        umax = np.sqrt(Ux ** 2 + Uy ** 2 + Uz ** 2).max()
-        dt = 0.5 * hmin / umax                                     # CFL number 0.5
-        MESH = dict(levels=w["levels"], device_mesh=dm, r_cmb=workloads.R_CMB, r_surf=workloads.R_SURF)
-        opts = dict(method_BT="RK4", method_interp="cubic")
-        A.advect3d_slm_p_sph(MESH, None, Ux, Uy, Uz, w["T"], dt, opts)
-        t = time.perf_counter()
-        _, WS = A.advect3d_slm_p_sph(MESH, None, Ux, Uy, Uz, w["T"], dt, opts)
-        t_sl = time.perf_counter() - t
+        if not args.sweep_only:
+            dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
+            U, _, _ = dm.solve(**SOLVER_KW)
+            Ux, Uy, Uz = U[0::3], U[1::3], U[2::3]
+            X, EL = f["GCOORD"], f["EL2NOD"]
+            hmin = min(np.linalg.norm(X[:, EL[:, a]] - X[:, EL[:, b]], axis=0).min()
+                       for a, b in ((0, 1), (1, 2), (2, 3), (3, 0), (0, 2), (1, 3)))
+            umax = np.sqrt(Ux ** 2 + Uy ** 2 + Uz ** 2).max()
+            dt = 0.5 * hmin / umax                                     # CFL number 0.5
+            MESH = dict(levels=w["levels"], device_mesh=dm, r_cmb=workloads.R_CMB, r_surf=workloads.R_SURF)
+            opts = dict(method_BT="RK4", method_interp="cubic")
+            A.advect3d_slm_p_sph(MESH, None, Ux, Uy, Uz, w["T"], dt, opts)
+            t = time.perf_counter()
+            _, WS = A.advect3d_slm_p_sph(MESH, None, Ux, Uy, Uz, w["T"], dt, opts)
+            t_sl = time.perf_counter() - t
+            n = f["nnod"]
+            step = {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {n} P2 nodes", "dt": dt,
+                    "method": "RK4 (3 substeps) + cubic", "s": t_sl, "departure_points_per_s": n / t_sl,
+                    "locate": WS["locate_info"]}
         pts = shell_points(args.sweep_points, args.seed + 3)
         A.tsearch2_sph(dm, pts[:, :100000])
         t = time.perf_counter()
@@ -314,10 +320,7 @@ def sl_rates(args):
         t_loc = time.perf_counter() - t
     finally:
         dm.close()
-    n = f["nnod"]
-    return {"sl_step": {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {n} P2 nodes", "dt": dt,
-                        "method": "RK4 (3 substeps) + cubic", "s": t_sl, "departure_points_per_s": n / t_sl,
-                        "locate": WS["locate_info"]},
+    return {"sl_step": step,
             "location_sweep": {"points": args.sweep_points, "s": t_loc, "points_per_s": args.sweep_points / t_loc,
                                "locate": info}}
 
@@ -431,6 +434,8 @@ def main():
                          "plain-FP64 GPU solve of the 8M-DOF shell)")
     ap.add_argument("--skip-learned", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--sl-only", action="store_true", help="semi-Lagrangian rates only (profiling)")
+    ap.add_argument("--sweep-only", action="store_true", help="with --sl-only: the location sweep alone")
     ap.add_argument("--skip-sl", action="store_true")
     ap.add_argument("--sweep-points", type=int, default=16_000_000)
     ap.add_argument("--op-only", action="store_true", help="time one level operator only (profiling)")
@@ -440,7 +445,12 @@ def main():
     ap.add_argument("--set-option", action="append", default=[], help="library option name=value (--op-only)")
     args = ap.parse_args()
     rank, ws, td = dist_init()
-    if args.op_only:
+    if args.sl_only:
+        if rank == 0:
+            from m3tet_sph_gb300 import build as B
+            B.build()
+            print(json.dumps(sl_rates(args)))
+    elif args.op_only:
         run_operator_only(args, rank)
     elif args.impl == "reference":
         run_reference(args, rank, ws, td)

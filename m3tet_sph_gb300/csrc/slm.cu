@@ -33,7 +33,25 @@ struct SlmMesh {
   const double *SX;      // [3][nnod]  X-90 frame of all nodes
   const int *v2e_ptr;    // [nvnod+1]
   const int *v2e;        // vertex -> elements
+  // start grid for walks without a guess: cells equal in cos(theta), phi and r
+  const int *grid;       // [gnr][gnt][gnp] element id
+  int gnt, gnp, gnr;
+  double grmin, grmax;
 };
+
+__host__ __device__ inline int grid_cell(int gnt, int gnp, int gnr, double grmin, double grmax, double ct, double ph,
+                                         double r) {
+  const double two_pi = 6.283185307179586;
+  int it = (int)((1.0 - ct) * 0.5 * gnt);
+  double p = fmod(ph, two_pi);
+  if (p < 0) p += two_pi;
+  int ip = (int)(p / two_pi * gnp);
+  int ir = (int)((r - grmin) / (grmax - grmin) * gnr);
+  it = it < 0 ? 0 : (it >= gnt ? gnt - 1 : it);
+  ip = ip < 0 ? 0 : (ip >= gnp ? gnp - 1 : ip);
+  ir = ir < 0 ? 0 : (ir >= gnr ? gnr - 1 : ir);
+  return (ir * gnt + it) * gnp + ip;
+}
 
 __device__ __forceinline__ void sph2cart_d(double th, double ph, double r, double &x, double &y, double &z) {
   double st, ct, sp, cp;
@@ -202,6 +220,8 @@ __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const
   point_frames(P[i], P[npt + i], P[2 * npt + i], f);
   int e = guess ? guess[i] : -1;
   if ((e < 0 || e >= m.nel) && node_guess) e = node_guess[i];
+  if ((e < 0 || e >= m.nel) && m.grid)
+    e = m.grid[grid_cell(m.gnt, m.gnp, m.gnr, m.grmin, m.grmax, cos(P[i]), P[npt + i], P[2 * npt + i])];
   if (e < 0 || e >= m.nel) e = 0;
   int prev = -1, found = -1;
   double lc[3] = {0, 0, 0};
@@ -548,7 +568,7 @@ __global__ void k_cart_to_sph(const double *__restrict__ Xc, int n, double *__re
 // ======================================================================================
 struct SlmState {
   bool built = false;
-  int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr;
+  int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr, *grid = nullptr;
   uint8_t *cls = nullptr;
   double *S0 = nullptr, *SZ = nullptr, *SX = nullptr;
   // work
@@ -590,7 +610,7 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
                     (void *)S->V, (void *)S->out, (void *)S->upu, (void *)S->rpu, (void *)S->U, (void *)S->gel,
                     (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->Xc, (void *)S->kk, (void *)S->acc,
                     (void *)S->els, (void *)S->guess,
-                    (void *)S->todo, (void *)S->status})
+                    (void *)S->todo, (void *)S->status, (void *)S->grid})
       if (q) cudaFree(q);
     delete S;
   };
@@ -655,16 +675,61 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
       }
     }
   }
+  // start grid: each cell holds the largest id of the elements whose vertex centroid falls in it;
+  // empty cells take the first filled face neighbour (fixed order, repeated passes)
+  double grmin = 1e300, grmax = -1e300;
+  for (int v = 0; v < nv; ++v) {
+    grmin = std::min(grmin, S0[2 * (size_t)nv + v]);
+    grmax = std::max(grmax, S0[2 * (size_t)nv + v]);
+  }
+  if (!(grmax > grmin)) grmax = grmin + 1.0;
+  const double target = std::max(1.0, nel / 4.0);
+  const int gnr = std::min(64, std::max(2, (int)std::lround(std::cbrt(target) / 4.0)));
+  const int gnt = std::max(2, (int)std::lround(std::sqrt(target / gnr / 2.0)));
+  const int gnp = 2 * gnt;
+  std::vector<int> grid((size_t)gnt * gnp * gnr, -1);
+  for (int e = 0; e < nel; ++e) {
+    double c[3] = {0, 0, 0};
+    for (int i = 0; i < 4; ++i)
+      for (int k = 0; k < 3; ++k) c[k] += 0.25 * f0.GCOORD[3 * (size_t)el[(size_t)e * 10 + i] + k];
+    const double r = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    const int cell = grid_cell(gnt, gnp, gnr, grmin, grmax, r > 0 ? c[2] / r : 1.0, std::atan2(c[1], c[0]), r);
+    grid[cell] = std::max(grid[cell], e);
+  }
+  for (bool again = true; again;) {
+    again = false;
+    std::vector<int> g2 = grid;
+    for (int ir = 0; ir < gnr; ++ir)
+      for (int it = 0; it < gnt; ++it)
+        for (int ip = 0; ip < gnp; ++ip) {
+          const size_t c = ((size_t)ir * gnt + it) * gnp + ip;
+          if (grid[c] >= 0) continue;
+          const int nb[6][3] = {{ir, it, (ip + 1) % gnp}, {ir, it, (ip + gnp - 1) % gnp}, {ir, it + 1, ip},
+                                {ir, it - 1, ip},         {ir + 1, it, ip},                 {ir - 1, it, ip}};
+          for (const auto &q : nb)
+            if (q[0] >= 0 && q[0] < gnr && q[1] >= 0 && q[1] < gnt) {
+              const int v = grid[((size_t)q[0] * gnt + q[1]) * gnp + q[2]];
+              if (v >= 0) {
+                g2[c] = v;
+                break;
+              }
+            }
+          if (g2[c] < 0) again = true;
+        }
+    grid.swap(g2);
+  }
   std::vector<uint8_t> cls(f0.elclass, f0.elclass + nel);
   int st;
   if ((st = sl_upload(&S->el2nod, soa.data(), soa.size(), s)) || (st = sl_upload(&S->nbr, nbr.data(), nbr.size(), s)) ||
       (st = sl_upload(&S->v2e_ptr, ptr.data(), ptr.size(), s)) || (st = sl_upload(&S->v2e, adj.data(), adj.size(), s)) ||
       (st = sl_upload(&S->node_guess, first.data(), first.size(), s)) ||
       (st = sl_upload(&S->cls, cls.data(), cls.size(), s)) || (st = sl_upload(&S->S0, S0.data(), S0.size(), s)) ||
-      (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)))
+      (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)) ||
+      (st = sl_upload(&S->grid, grid.data(), grid.size(), s)))
     return st;
   M3_CUDA(cudaStreamSynchronize(s));
-  S->view = SlmMesh{nel, nnod, nv, S->el2nod, S->nbr, S->cls, S->S0, S->SZ, S->SX, S->v2e_ptr, S->v2e};
+  S->view = SlmMesh{nel, nnod, nv, S->el2nod, S->nbr, S->cls, S->S0, S->SZ, S->SX, S->v2e_ptr, S->v2e,
+                    S->grid, gnt, gnp, gnr, grmin, grmax};
   S->built = true;
   return M3SPH_OK;
 }
