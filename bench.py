@@ -289,7 +289,7 @@ def sl_rates(args):
     advection step of T (RK4 over 3 substeps, curved-element location, cubic interpolation) in the
     Stokes velocity at the CFL dt, and a seeded point-location sweep inside the shell."""
     from m3tet_sph_gb300 import advection as A, stokes, workloads
-    w = workloads.make_workload("c1", seed=args.seed)
+    w = workloads.make_workload(args.sl_workload, seed=args.seed)
     f = w["levels"][0]
     dm = stokes.DeviceMesh(w["levels"])
     step = None
@@ -436,6 +436,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--sl-only", action="store_true", help="semi-Lagrangian rates only (profiling)")
     ap.add_argument("--sweep-only", action="store_true", help="with --sl-only: the location sweep alone")
+    ap.add_argument("--sl-workload", default="c1", help="mesh of the semi-Lagrangian measurements")
     ap.add_argument("--skip-sl", action="store_true")
     ap.add_argument("--sweep-points", type=int, default=16_000_000)
     ap.add_argument("--op-only", action="store_true", help="time one level operator only (profiling)")
