@@ -117,8 +117,8 @@ def peaks():
 
 
 # DRAM bytes per element of one streamed FP32 apply (both kernels), from the ncu capture of the
-# 491,520-element shell: (948.77 + 20.58 + 84.51 + 3.46) MB / 491,520
-TRAFFIC_PER_ELEMENT_F32 = (948.77e6 + 20.58e6 + 84.51e6 + 3.46e6) / 491520
+# 491,520-element shell: (948.76 + 20.05 + 83.85 + 4.28) MB / 491,520
+TRAFFIC_PER_ELEMENT_F32 = (948.76e6 + 20.05e6 + 83.85e6 + 4.28e6) / 491520
 
 
 def apply_bytes_df(nel, ndof):
