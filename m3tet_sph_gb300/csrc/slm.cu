@@ -21,6 +21,7 @@
 namespace m3sph {
 
 constexpr int WALK_MAX_STEPS = 512;
+constexpr float WALK32_MARGIN = 1e-4f;   // FP32 barycentric margin before the FP64 walk takes over
 constexpr double TIE_EPS = 1e-10;
 
 struct SlmMesh {
@@ -33,6 +34,7 @@ struct SlmMesh {
   const double *SX;      // [3][nnod]  X-90 frame of all nodes
   const int *v2e_ptr;    // [nvnod+1]
   const int *v2e;        // vertex -> elements
+  const float *S0f, *SZf, *SXf;   // FP32 copies of S0, SZ, SX (the FP32 part of the walk)
   // start grid for walks without a guess: cells equal in cos(theta), phi and r
   const int *grid;       // [gnr][gnt][gnp] element id
   int gnt, gnp, gnr;
@@ -68,9 +70,10 @@ __device__ __forceinline__ void c2s(double x, double y, double z, double &th, do
   if (ph < 0.0) ph += 2.0 * M_PI;
 }
 
-struct PointFrames {
-  double p0[3], pz[3], px[3];
+template <typename R> struct PointFramesT {
+  R p0[3], pz[3], px[3];
 };
+using PointFrames = PointFramesT<double>;
 
 __device__ __forceinline__ void point_frames(double th, double ph, double r, PointFrames &f) {
   f.p0[0] = th; f.p0[1] = ph; f.p0[2] = r;
@@ -81,9 +84,10 @@ __device__ __forceinline__ void point_frames(double th, double ph, double r, Poi
 }
 
 // barycentric determinant ratio of local_coords_3d_sph.m:94-147 for vertex a (b,c,d the others)
-__device__ __forceinline__ double dratio(const double (&t)[4], const double (&p)[4], const double (&q)[4], int b,
-                                         int c, int d, double tp, double pp, double rp, int a) {
-  auto D = [&](double ta, double pa, double ra) {
+template <typename R>
+__device__ __forceinline__ R dratio(const R (&t)[4], const R (&p)[4], const R (&q)[4], int b, int c, int d, R tp, R pp,
+                                    R rp, int a) {
+  auto D = [&](R ta, R pa, R ra) {
     return (t[b] - ta) * (p[c] - pa) * (q[d] - ra) + (t[c] - ta) * (p[d] - pa) * (q[b] - ra) +
            (t[d] - ta) * (p[b] - pa) * (q[c] - ra) - (q[b] - ra) * (p[c] - pa) * (t[d] - ta) -
            (q[c] - ra) * (p[d] - pa) * (t[b] - ta) - (q[d] - ra) * (p[b] - pa) * (t[c] - ta);
@@ -91,74 +95,80 @@ __device__ __forceinline__ double dratio(const double (&t)[4], const double (&p)
   return D(tp, pp, rp) / D(t[a], p[a], q[a]);
 }
 
-__device__ __forceinline__ void lc_straight(const double (&t)[4], const double (&p)[4], const double (&q)[4],
-                                            const double *pt, double *lc) {
-  lc[0] = dratio(t, p, q, 1, 2, 3, pt[0], pt[1], pt[2], 0);
-  lc[1] = dratio(t, p, q, 0, 2, 3, pt[0], pt[1], pt[2], 1);
-  lc[2] = dratio(t, p, q, 0, 1, 3, pt[0], pt[1], pt[2], 2);
+template <typename R>
+__device__ __forceinline__ void lc_straight(const R (&t)[4], const R (&p)[4], const R (&q)[4], const R *pt, R *lc) {
+  lc[0] = dratio<R>(t, p, q, 1, 2, 3, pt[0], pt[1], pt[2], 0);
+  lc[1] = dratio<R>(t, p, q, 0, 2, 3, pt[0], pt[1], pt[2], 1);
+  lc[2] = dratio<R>(t, p, q, 0, 1, 3, pt[0], pt[1], pt[2], 2);
 }
 
-// own-frame local coordinates of point f in element e; returns Newton step size for iso elements
-__device__ double local_coords(const SlmMesh &m, int e, const PointFrames &f, double *lc) {
+// own-frame local coordinates of point f in element e from the frame coordinates S0/SZ/SX (FP64 or
+// their FP32 copies); returns the Newton step size for iso elements
+template <typename R>
+__device__ R local_coords_t(const SlmMesh &m, const R *S0, const R *SZ, const R *SX, int e, const PointFramesT<R> &f,
+                            R *lc) {
   const int cls = m.cls[e];
-  double t[4], p[4], q[4];
+  R t[4], p[4], q[4];
   int v[4];
   for (int i = 0; i < 4; ++i) v[i] = m.el2nod[(size_t)i * m.nel + e];
   if (cls == M3SPH_OUT_CONE_NO_CROSS_2PI) {
-    for (int i = 0; i < 4; ++i) { t[i] = m.S0[v[i]]; p[i] = m.S0[m.nvnod + v[i]]; q[i] = m.S0[2 * m.nvnod + v[i]]; }
-    lc_straight(t, p, q, f.p0, lc);
-    return 0.0;
+    for (int i = 0; i < 4; ++i) { t[i] = S0[v[i]]; p[i] = S0[m.nvnod + v[i]]; q[i] = S0[2 * m.nvnod + v[i]]; }
+    lc_straight<R>(t, p, q, f.p0, lc);
+    return R(0);
   }
   if (cls == M3SPH_OUT_CONE_CROSS_2PI) {
-    for (int i = 0; i < 4; ++i) { t[i] = m.SZ[v[i]]; p[i] = m.SZ[m.nvnod + v[i]]; q[i] = m.SZ[2 * m.nvnod + v[i]]; }
-    lc_straight(t, p, q, f.pz, lc);
-    return 0.0;
+    for (int i = 0; i < 4; ++i) { t[i] = SZ[v[i]]; p[i] = SZ[m.nvnod + v[i]]; q[i] = SZ[2 * m.nvnod + v[i]]; }
+    lc_straight<R>(t, p, q, f.pz, lc);
+    return R(0);
   }
-  for (int i = 0; i < 4; ++i) { t[i] = m.SX[v[i]]; p[i] = m.SX[m.nnod + v[i]]; q[i] = m.SX[2 * m.nnod + v[i]]; }
-  lc_straight(t, p, q, f.px, lc);
-  if (cls != M3SPH_IN_CONE_ISO) return 0.0;
+  for (int i = 0; i < 4; ++i) { t[i] = SX[v[i]]; p[i] = SX[m.nnod + v[i]]; q[i] = SX[2 * m.nnod + v[i]]; }
+  lc_straight<R>(t, p, q, f.px, lc);
+  if (cls != M3SPH_IN_CONE_ISO) return R(0);
   // Newton on the 10-node map (local_coords_curved_3d_sph.m:45-168): up to 6 steps, tol 1e-8
-  double G[3][10];
+  R G[3][10];
   for (int n = 0; n < 10; ++n) {
     const int nod = m.el2nod[(size_t)n * m.nel + e];
-    for (int k = 0; k < 3; ++k) G[k][n] = m.SX[(size_t)k * m.nnod + nod];
+    for (int k = 0; k < 3; ++k) G[k][n] = SX[(size_t)k * m.nnod + nod];
   }
-  double step = 0.0;
+  R step = R(0);
   for (int it = 0; it < 6; ++it) {
-    const double r = lc[0], s = lc[1], tt = lc[2], u = 1.0 - r - s - tt;
-    const double N[10] = {r * (2 * r - 1), s * (2 * s - 1), tt * (2 * tt - 1), u * (2 * u - 1), 4 * r * s,
-                          4 * s * tt, 4 * tt * u, 4 * r * u, 4 * r * tt, 4 * s * u};
-    const double dN[10][3] = {{4 * r - 1, 0, 0}, {0, 4 * s - 1, 0}, {0, 0, 4 * tt - 1},
-                              {1 - 4 * u, 1 - 4 * u, 1 - 4 * u}, {4 * s, 4 * r, 0}, {0, 4 * tt, 4 * s},
-                              {-4 * tt, -4 * tt, 4 * (u - tt)}, {4 * (u - r), -4 * r, -4 * r},
-                              {4 * tt, 0, 4 * r}, {-4 * s, 4 * (u - s), -4 * s}};
-    double d[3], J[3][3];
+    const R r = lc[0], s = lc[1], tt = lc[2], u = R(1) - r - s - tt;
+    const R N[10] = {r * (2 * r - 1), s * (2 * s - 1), tt * (2 * tt - 1), u * (2 * u - 1), 4 * r * s,
+                     4 * s * tt, 4 * tt * u, 4 * r * u, 4 * r * tt, 4 * s * u};
+    const R dN[10][3] = {{4 * r - 1, 0, 0}, {0, 4 * s - 1, 0}, {0, 0, 4 * tt - 1},
+                         {1 - 4 * u, 1 - 4 * u, 1 - 4 * u}, {4 * s, 4 * r, 0}, {0, 4 * tt, 4 * s},
+                         {-4 * tt, -4 * tt, 4 * (u - tt)}, {4 * (u - r), -4 * r, -4 * r},
+                         {4 * tt, 0, 4 * r}, {-4 * s, 4 * (u - s), -4 * s}};
+    R d[3], J[3][3];
     for (int k = 0; k < 3; ++k) {
-      double s0 = 0.0;
+      R s0 = R(0);
       for (int n = 0; n < 10; ++n) s0 += G[k][n] * N[n];
       d[k] = f.px[k] - s0;
       for (int j = 0; j < 3; ++j) {
-        double sj = 0.0;
+        R sj = R(0);
         for (int n = 0; n < 10; ++n) sj += G[k][n] * dN[n][j];
         J[k][j] = sj;
       }
     }
-    if (sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < 1e-8) break;
-    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-    const double id = 1.0 / det;
-    const double ds0 = id * ((J[1][1] * J[2][2] - J[1][2] * J[2][1]) * d[0] + (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * d[1] +
-                             (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * d[2]);
-    const double ds1 = id * ((J[1][2] * J[2][0] - J[1][0] * J[2][2]) * d[0] + (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * d[1] +
-                             (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * d[2]);
-    const double ds2 = id * ((J[1][0] * J[2][1] - J[1][1] * J[2][0]) * d[0] + (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * d[1] +
-                             (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * d[2]);
+    if (sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < R(1e-8)) break;
+    const R det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                  J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    const R id = R(1) / det;
+    const R ds0 = id * ((J[1][1] * J[2][2] - J[1][2] * J[2][1]) * d[0] + (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * d[1] +
+                        (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * d[2]);
+    const R ds1 = id * ((J[1][2] * J[2][0] - J[1][0] * J[2][2]) * d[0] + (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * d[1] +
+                        (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * d[2]);
+    const R ds2 = id * ((J[1][0] * J[2][1] - J[1][1] * J[2][0]) * d[0] + (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * d[1] +
+                        (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * d[2]);
     lc[0] += ds0;
     lc[1] += ds1;
     lc[2] += ds2;
     step = fabs(ds0) + fabs(ds1) + fabs(ds2);
   }
   return step;
+}
+__device__ __forceinline__ double local_coords(const SlmMesh &m, int e, const PointFrames &f, double *lc) {
+  return local_coords_t<double>(m, m.S0, m.SZ, m.SX, e, f, lc);
 }
 
 __device__ __forceinline__ void bary_minmax(const double *lc, double &mn, double &mx, int &argmn) {
@@ -224,6 +234,42 @@ __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const
     e = m.grid[grid_cell(m.gnt, m.gnp, m.gnr, m.grmin, m.grmax, cos(P[i]), P[npt + i], P[2 * npt + i])];
   if (e < 0 || e >= m.nel) e = 0;
   int prev = -1, found = -1;
+  // walk in FP32 (the FP64 pipe issues at 1/64 of the FP32 rate) until the FP32 barycentrics place
+  // the point inside within a margin well above their rounding; the FP64 walk below then decides
+  int steps32 = 0;
+  {
+    PointFramesT<float> g;
+    for (int k = 0; k < 3; ++k) {
+      g.p0[k] = (float)f.p0[k];
+      g.pz[k] = (float)f.pz[k];
+      g.px[k] = (float)f.px[k];
+    }
+    for (; steps32 < WALK_MAX_STEPS; ++steps32) {
+      float l[3];
+      local_coords_t<float>(m, m.S0f, m.SZf, m.SXf, e, g, l);
+      const float b[4] = {l[0], l[1], l[2], 1.0f - l[0] - l[1] - l[2]};
+      int am = 0;
+      float mn = b[0];
+      for (int k = 1; k < 4; ++k)
+        if (b[k] < mn) { mn = b[k]; am = k; }
+      if (!(mn < -WALK32_MARGIN)) break;   // inside (or NaN): hand over to FP64
+      int nb = m.nbr[(size_t)am * m.nel + e];
+      if (nb == prev || nb < 0) {
+        int alt = -1;
+        float amin = 1e30f;
+        for (int k = 0; k < 4; ++k) {
+          if (k == am || !(b[k] < 0.0f)) continue;
+          const int c = m.nbr[(size_t)k * m.nel + e];
+          if (c >= 0 && c != prev && b[k] < amin) { amin = b[k]; alt = c; }
+        }
+        if (alt < 0) break;
+        nb = alt;
+      }
+      prev = e;
+      e = nb;
+    }
+  }
+  prev = -1;
   double lc[3] = {0, 0, 0};
   uint8_t st = 0;
   for (int step = 0; step < WALK_MAX_STEPS; ++step) {
@@ -569,6 +615,7 @@ __global__ void k_cart_to_sph(const double *__restrict__ Xc, int n, double *__re
 struct SlmState {
   bool built = false;
   int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr, *grid = nullptr;
+  float *S0f = nullptr, *SZf = nullptr, *SXf = nullptr;
   uint8_t *cls = nullptr;
   double *S0 = nullptr, *SZ = nullptr, *SX = nullptr;
   // work
@@ -610,7 +657,8 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
                     (void *)S->V, (void *)S->out, (void *)S->upu, (void *)S->rpu, (void *)S->U, (void *)S->gel,
                     (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->Xc, (void *)S->kk, (void *)S->acc,
                     (void *)S->els, (void *)S->guess,
-                    (void *)S->todo, (void *)S->status, (void *)S->grid})
+                    (void *)S->todo, (void *)S->status, (void *)S->grid, (void *)S->S0f, (void *)S->SZf,
+                    (void *)S->SXf})
       if (q) cudaFree(q);
     delete S;
   };
@@ -727,9 +775,13 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
       (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)) ||
       (st = sl_upload(&S->grid, grid.data(), grid.size(), s)))
     return st;
+  const std::vector<float> S0f(S0.begin(), S0.end()), SZf(SZ.begin(), SZ.end()), SXf(SX.begin(), SX.end());
+  if ((st = sl_upload(&S->S0f, S0f.data(), S0f.size(), s)) || (st = sl_upload(&S->SZf, SZf.data(), SZf.size(), s)) ||
+      (st = sl_upload(&S->SXf, SXf.data(), SXf.size(), s)))
+    return st;
   M3_CUDA(cudaStreamSynchronize(s));
   S->view = SlmMesh{nel, nnod, nv, S->el2nod, S->nbr, S->cls, S->S0, S->SZ, S->SX, S->v2e_ptr, S->v2e,
-                    S->grid, gnt, gnp, gnr, grmin, grmax};
+                    S->S0f, S->SZf, S->SXf, S->grid, gnt, gnp, gnr, grmin, grmax};
   S->built = true;
   return M3SPH_OK;
 }
