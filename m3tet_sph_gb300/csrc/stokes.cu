@@ -36,6 +36,7 @@ int stream_apply_df(const Level &L, const float *Kh, const float *Kl, const doub
 int stream_apply_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
 int stream_check(const Level &L, cudaStream_t s);
 int stream_set_outer_warps(int n);
+int stream_set_f32_variant(int v);
 int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
 template <typename T> int level_inverse_diag(Level &L, const T *K, double *work, cudaStream_t s);
 int grad_apply(const Level &L, const double *G, const double *q, double *y, cudaStream_t s);
@@ -1684,6 +1685,8 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
       return M3SPH_ERR_BAD_INPUT;
     }
     M->ml_schedule = value;
+  } else if (n == "stream_f32_variant") {
+    M3_TRY(stream_set_f32_variant(value));
   } else if (n == "stream_outer") {
     g_stream_outer = value != 0;
   } else if (n == "stream_outer_variant") {

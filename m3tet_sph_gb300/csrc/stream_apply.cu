@@ -24,10 +24,7 @@ namespace m3sph {
 namespace sa {
 constexpr int E = 32;                         // elements per chunk
 constexpr int NST = 3;                        // matrix stages
-constexpr int NCX = 6;                        // connectivity + gathered-x slots
 constexpr int NGRP = 2;                       // consumer groups of 4 warps
-constexpr int NGW = 2;                        // gather warps
-constexpr int THREADS = NGRP * 128 + NGW * 32 + 32;   // + one producer warp
 constexpr int ROWS = 117;                     // float4 rows of a packed FP32 element matrix
 constexpr int KBYTES = ROWS * E * 16;         // 59,904 B per stage
 constexpr int KSTRIDE = 60416;                // stage stride (multiple of 1024)
@@ -36,18 +33,22 @@ constexpr int XBYTES = 30 * E * 4;            // gathered x of a chunk
 constexpr int SY_LD = 33;
 constexpr int OFF_K = 0;
 constexpr int OFF_CX = OFF_K + NST * KSTRIDE;              // slot: connectivity, then x
-constexpr int OFF_HDR = OFF_CX + NCX * (CBYTES + XBYTES);
-constexpr int HDR_BYTES = ((16 * NCX + 63) / 64) * 64;   // one int4 header per slot
-constexpr int OFF_KTAG = OFF_HDR + HDR_BYTES;  // use tags of the matrix stages
-constexpr int OFF_BAR = OFF_KTAG + 64;        // (the partial sums of a chunk reuse its matrix stage)
-constexpr int NBAR = 2 * NST + 3 * NCX;
-constexpr int SMEM = OFF_BAR + NBAR * 8;
-constexpr int SMEM_ALLOC = SMEM + 1024;       // room to align the base to 1024 B
 constexpr unsigned long long TIMEOUT_NS = 1000000000ull;
-static_assert(SMEM_ALLOC <= 232448, "shared memory budget");
 static_assert(KBYTES <= KSTRIDE && KSTRIDE % 1024 == 0, "stage layout");
 static_assert(4 * 30 * SY_LD * 4 <= KBYTES, "partial sums fit in a matrix stage");
-static_assert(16 * NCX <= HDR_BYTES && 4 * NST <= 64, "header and tag areas");
+// layout for NCX connectivity + gathered-x slots and NGW gather warps
+template <int NCX, int NGW> struct Lay {
+  static constexpr int THREADS = NGRP * 128 + NGW * 32 + 32;   // + one producer warp
+  static constexpr int OFF_HDR = OFF_CX + NCX * (CBYTES + XBYTES);
+  static constexpr int HDR_BYTES = ((16 * NCX + 63) / 64) * 64;   // one int4 header per slot
+  static constexpr int OFF_KTAG = OFF_HDR + HDR_BYTES;            // use tags of the matrix stages
+  static constexpr int OFF_BAR = OFF_KTAG + 64;   // (the partial sums of a chunk reuse its matrix stage)
+  static constexpr int NBAR = 2 * NST + 3 * NCX;
+  static constexpr int SMEM = OFF_BAR + NBAR * 8;
+  static constexpr int SMEM_ALLOC = SMEM + 1024;    // room to align the base to 1024 B
+  static_assert(SMEM_ALLOC <= 232448, "shared memory budget");
+  static_assert(16 * NCX <= HDR_BYTES && 4 * NST <= 64, "header and tag areas");
+};
 }  // namespace sa
 
 namespace {
@@ -163,15 +164,17 @@ __device__ __forceinline__ void part_mac(const float4 *rows, const float (&x)[30
 
 }  // namespace
 
-__global__ void __launch_bounds__(sa::THREADS, 1)
+template <int NCX, int NGW>
+__global__ void __launch_bounds__(sa::Lay<NCX, NGW>::THREADS, 1)
     k_stream_elem_f32(const __grid_constant__ CUtensorMap tmK, const int *__restrict__ conn, int nchunk, int nel,
                       int *__restrict__ ticket, int *__restrict__ err, const float *__restrict__ x,
                       float *__restrict__ ye) {
   using namespace sa;
+  using Ly = Lay<NCX, NGW>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t bar0 = smem_u32(sm + OFF_BAR);
+  const uint32_t bar0 = smem_u32(sm + Ly::OFF_BAR);
   // matrix ring: full_k / empty_k; slot ring: conn landed / x gathered / slot free
   auto full_k = [&](int s) { return bar0 + 8u * s; };
   auto empty_k = [&](int s) { return bar0 + 8u * (NST + s); };
@@ -180,8 +183,8 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
   auto cx_empty = [&](int j) { return bar0 + 8u * (2 * NST + 2 * NCX + j); };
   auto slot_conn = [&](int j) { return reinterpret_cast<int *>(sm + OFF_CX + j * (CBYTES + XBYTES)); };
   auto slot_x = [&](int j) { return reinterpret_cast<float *>(sm + OFF_CX + j * (CBYTES + XBYTES) + CBYTES); };
-  int4 *hdr = reinterpret_cast<int4 *>(sm + OFF_HDR);   // {first element, count, ticket, use tag}
-  int *ktag = reinterpret_cast<int *>(sm + OFF_KTAG);
+  int4 *hdr = reinterpret_cast<int4 *>(sm + Ly::OFF_HDR);   // {first element, count, ticket, use tag}
+  int *ktag = reinterpret_cast<int *>(sm + Ly::OFF_KTAG);
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(full_k(s), 1);
@@ -232,8 +235,10 @@ __global__ void __launch_bounds__(sa::THREADS, 1)
       }
     }
     if (ok && i >= 1 && !issue_k(i - 1)) ok = false;
-    // end markers: one per gather warp / consumer group (chunk indices i, i + 1)
-    for (int m = i; ok && m < i + NGRP; ++m) {
+    // end markers at chunk indices i .. i + max(NGRP, NGW) - 1: consecutive indices reach every
+    // gather warp and every consumer group
+    constexpr int NEND = NGRP > NGW ? NGRP : NGW;
+    for (int m = i; ok && m < i + NEND; ++m) {
       const int j = m % NCX;
       if (m >= NCX && !mbar_wait(cx_empty(j), ((m / NCX) & 1) ^ 1)) {
         ok = false;
@@ -595,6 +600,7 @@ static std::once_flag g_encode_once;
 static cudaError_t g_encode_status = cudaSuccess;
 
 template <class Op> static int rowlane_attrs();
+static int f32_attrs();
 
 int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s) {
   std::call_once(g_encode_once, [] {
@@ -632,7 +638,7 @@ int stream_build(Level &L, const std::vector<int> &perm, cudaStream_t s) {
   k_chunk_conn<<<(unsigned)((n8 + 255) / 256), 256, 0, s>>>(L.el2nod, nel, L.nchunk8, sr::E, L.chunk_conn8);
   count_launch();
   M3_CUDA(cudaGetLastError());
-  M3_CUDA(cudaFuncSetAttribute(k_stream_elem_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, sa::SMEM_ALLOC));
+  M3_TRY(f32_attrs());
   M3_TRY(rowlane_attrs<RlDF>());
   M3_TRY(rowlane_attrs<RlF64>());
   int dev = 0, nsm = 0;
@@ -677,13 +683,49 @@ static int stream_ready(const Level &L, const void *K) {
   return M3SPH_OK;
 }
 
+// FP32 streamed kernel variants: (connectivity/x slots, gather warps)
+static int g_f32_variant = 0;
+template <int NCX, int NGW>
+static int f32_attr() {
+  M3_CUDA(cudaFuncSetAttribute(k_stream_elem_f32<NCX, NGW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               sa::Lay<NCX, NGW>::SMEM_ALLOC));
+  return M3SPH_OK;
+}
+static int f32_attrs() {
+  M3_TRY((f32_attr<6, 2>()));
+  M3_TRY((f32_attr<8, 2>()));
+  M3_TRY((f32_attr<6, 3>()));
+  M3_TRY((f32_attr<8, 3>()));
+  return M3SPH_OK;
+}
+int stream_set_f32_variant(int v) {
+  if (v < 0 || v > 3) {
+    set_error("stream_f32_variant must be 0..3");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  g_f32_variant = v;
+  return M3SPH_OK;
+}
+template <int NCX, int NGW>
+static void f32_launch(const Level &L, const CUtensorMap &map, const float *x, cudaStream_t s) {
+  k_stream_elem_f32<NCX, NGW><<<L.sa_grid, sa::Lay<NCX, NGW>::THREADS, sa::Lay<NCX, NGW>::SMEM_ALLOC, s>>>(
+      map, L.chunk_conn, L.nchunk, L.nel, L.sa_err + 1, L.sa_err, x, L.ye32);
+}
+static void f32_phase1(const Level &L, const CUtensorMap &map, const float *x, cudaStream_t s) {
+  switch (g_f32_variant) {
+    case 1: f32_launch<8, 2>(L, map, x, s); break;
+    case 2: f32_launch<6, 3>(L, map, x, s); break;
+    case 3: f32_launch<8, 3>(L, map, x, s); break;
+    default: f32_launch<6, 2>(L, map, x, s); break;
+  }
+}
+
 int stream_apply_f32(const Level &L, const float *K, const float *x, float *y, cudaStream_t s) {
   M3_TRY(stream_ready(L, K));
   CUtensorMap map;
   M3_TRY(encode_k32(L, K, &map));
   M3_CUDA(cudaMemsetAsync(L.sa_err + 1, 0, sizeof(int), s));
-  k_stream_elem_f32<<<L.sa_grid, sa::THREADS, sa::SMEM_ALLOC, s>>>(map, L.chunk_conn, L.nchunk, L.nel, L.sa_err + 1,
-                                                                    L.sa_err, x, L.ye32);
+  f32_phase1(L, map, x, s);
   count_launch();
   k_node_gather_f32<<<(L.nnod + 255) / 256, 256, 0, s>>>(L.g_ptr, L.g_idx, L.nnod, L.ye32, y);
   count_launch();
@@ -769,8 +811,7 @@ int stream_apply_jac_f32(const Level &L, const float *K, float w, const float *r
   CUtensorMap map;
   M3_TRY(encode_k32(L, K, &map));
   M3_CUDA(cudaMemsetAsync(L.sa_err + 1, 0, sizeof(int), s));
-  k_stream_elem_f32<<<L.sa_grid, sa::THREADS, sa::SMEM_ALLOC, s>>>(map, L.chunk_conn, L.nchunk, L.nel, L.sa_err + 1,
-                                                                    L.sa_err, d, L.ye32);
+  f32_phase1(L, map, d, s);
   count_launch();
   k_node_gather_jac_f32<<<(L.nnod + 255) / 256, 256, 0, s>>>(L.g_ptr, L.g_idx, L.nnod, L.ye32, w, r, Di, d);
   count_launch();

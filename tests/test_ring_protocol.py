@@ -102,7 +102,7 @@ def run_f32(nchunk, seed, tags=True, NST=3, NCX=6, NGRP=2, NGW=2):
             yield 's'
         if i >= 1:
             yield from issue_k(i - 1)
-        for m in range(i, i + NGRP):
+        for m in range(i, i + max(NGRP, NGW)):
             j = m % NCX
             if m >= NCX:
                 while not cx_empty[j].test(((m // NCX) & 1) ^ 1):
@@ -208,6 +208,13 @@ SIZES = [1, 2, 3, 5, 7, 13, 40, 150]
 @pytest.mark.parametrize("run", [run_f32, run_rowlane])
 def test_tagged_rings_never_deadlock_or_mix_chunks(run):
     bad = [(n, seed) for n in SIZES for seed in range(60) if not run(n, seed, tags=True)]
+    assert not bad, bad[:5]
+
+
+@pytest.mark.parametrize("ncx,ngw", [(8, 2), (6, 3), (8, 3)])
+def test_f32_slot_and_gather_variants(ncx, ngw):
+    """The slot-ring depths and gather-warp counts selectable by stream_f32_variant."""
+    bad = [(n, seed) for n in SIZES for seed in range(40) if not run_f32(n, seed, NCX=ncx, NGW=ngw)]
     assert not bad, bad[:5]
 
 

@@ -251,3 +251,23 @@ def test_streamed_fp32_apply_many_chunks(built_lib):
         assert np.linalg.norm(ys[0] - y64) < 1e-5 * np.linalg.norm(y64)
     finally:
         dm2.close()
+
+
+def test_streamed_fp32_variants_bit_identical(built_lib):
+    """Every slot-ring depth / gather-warp count of the streamed FP32 kernel (stream_f32_variant 0..3)
+    runs the same arithmetic in the same order: outputs are bit-identical to the default's."""
+    from m3tet_sph_gb300 import stokes, workloads
+    w = workloads.make_workload('c1')
+    dm2 = stokes.DeviceMesh(w['levels'])
+    try:
+        dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
+        x = np.random.default_rng(13).standard_normal(3 * w['levels'][0]['nnod']).astype(np.float32)
+        y0 = dm2.level_apply32(0, x)
+        try:
+            for v in (1, 2, 3):
+                dm2.set_option("stream_f32_variant", v)
+                assert np.array_equal(dm2.level_apply32(0, x), y0), v
+        finally:
+            dm2.set_option("stream_f32_variant", 0)
+    finally:
+        dm2.close()
