@@ -166,6 +166,10 @@ M3SPH_API int m3sph_ml_train_epoch(m3sph_mesh *mesh, int32_t batch, float lr, ui
  * rows X (n x 64 FP32, rounded to BF16), targets T (n x 32): for checks against a CPU autograd. */
 M3SPH_API int m3sph_ml_gradients(m3sph_mesh *mesh, const float *X, const float *T, int32_t n, float *grad, double *loss);
 M3SPH_API int m3sph_ml_forward(m3sph_mesh *mesh, const float *X, int32_t n, float *Y);
+/* One learned sweep of level img (0 or 1) in FP32 as the V-cycle runs it: d += the partition-of-
+ * unity sum of the network's element corrections for the residual r - kd (kd may be NULL: r).
+ * Host vectors of 3*nnod(img); needs a set-up with precision 1 and parameters loaded. */
+M3SPH_API int m3sph_ml_sweep32(m3sph_mesh *mesh, int32_t img, const float *r, const float *kd, float *d);
 
 /* Kernel-variant switches for measurement and tests (per process, results equal to rounding):
  * "stream_apply" (streamed finest-level FP32 operator, default 1; 0: one launch per colour),
@@ -174,7 +178,9 @@ M3SPH_API int m3sph_ml_forward(m3sph_mesh *mesh, const float *X, int32_t n, floa
  * "split_apply" (4-warp per-colour kernels when streaming is off, default 1), "graphs" (CUDA-graph
  * replay of MG-PCG iterations, default 1), "df_outer" (double-float outer operator on the mixed
  * path, default 1), "ml_schedule" (learned smoothing: 0 learned-Jacobi-learned, 1 one learned
- * sweep per side; per handle). */
+ * sweep per side; per handle), "ml_infer" (learned sweep kernels: 1 fused tcgen05 sweep, default;
+ * 0 WMMA tile kernel), "stream_f32_variant" (slot-ring depth / gather warps of the streamed FP32
+ * kernel, 0-3, default 0). */
 M3SPH_API int m3sph_set_option(m3sph_mesh *mesh, const char *name, int32_t value);
 /* Cumulative number of CUDA kernels this library has launched (all handles). */
 M3SPH_API int m3sph_launch_count(unsigned long long *count);

@@ -181,6 +181,8 @@ int ml_build(m3sph_mesh *M);
 int ml_features(m3sph_mesh *M, const double *h_visc);
 template <typename T> int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *tmp, T *d);
 int ml_init_kernels();
+int ml_set_infer(int v);
+int ml_check(m3sph_mesh *M);
 bool ml_ready(m3sph_mesh *M);
 int ml_add_samples(m3sph_mesh *M, const double *r, const double *err, int stride, int offset);
 int ml_reserve(m3sph_mesh *M, long cap);

@@ -194,6 +194,369 @@ __global__ void k_ml_gather(int nnod, int nel, const int *__restrict__ ptr, cons
 }
 
 // ---------------------------------------------------------------------------------------
+// Fused sweep on the 5th-generation tensor cores (the default inference path).
+//
+// Persistent CTAs of 8 warps take tiles of 128 consecutive stored elements (tile = MMA M = TMEM
+// lanes). Warps 4-7 gather: thread g computes the 52 features of element g of a tile (the local
+// residual r0 - kd is formed here) and writes them, BF16, as row g of a K-major 128-byte-swizzled
+// A tile; two A tiles alternate, so the gather of the next tile overlaps the MMAs and the GELU of
+// this one. Warps 0-3 compute: one thread issues H = A W1^T (M 128, N 128, K 64) into TMEM, thread
+// t reads row t of H (tcgen05.ld), adds b1, applies GELU and writes G (BF16, swizzled), one thread
+// issues Y = G W2^T (M 128, N 32, K 128) into the same TMEM columns, and thread t stores
+// s (Y + b2) as the element's 30 corrections C[e][30]. The weights stay in shared memory for the
+// CTA's lifetime. Every mbarrier wait is bounded; a wait that gives up sets the error word and the
+// CTA still frees its TMEM before it returns.
+// ---------------------------------------------------------------------------------------
+namespace tc {
+constexpr int ROWS = 128;                       // elements per tile = MMA M = TMEM lanes
+constexpr int THREADS = 256;                    // 4 compute warps + 4 gather warps
+constexpr int OFF_W1 = 0;                       // W1: [128 hidden][64 in] BF16, K-major, 128 B swizzle
+constexpr int OFF_W2 = OFF_W1 + HID * 128;      // W2: 2 atoms (hidden 0-63, 64-127) of [32 out][64]
+constexpr int W2_ATOM = OUTP * 128;
+constexpr int ATOM = ROWS * 128;                // one [128][64] BF16 operand atom
+constexpr int OFF_F = OFF_W2 + 2 * W2_ATOM;     // two feature tiles
+constexpr int OFF_G = OFF_F + 2 * ATOM;         // G: 2 atoms (hidden 0-63, 64-127)
+constexpr int OFF_B1 = OFF_G + 2 * ATOM;
+constexpr int OFF_B2 = OFF_B1 + HID * 4;
+constexpr int OFF_S = OFF_B2 + OUTP * 4;        // residual norms of the two feature tiles
+constexpr int OFF_BAR = OFF_S + 2 * ROWS * 4;   // f_full[2], f_empty[2], mma_done
+constexpr int OFF_TM = OFF_BAR + 5 * 8;
+constexpr int SMEM = OFF_TM + 8;
+constexpr int SMEM_ALLOC = SMEM + 1024;         // room to align the base to 1024 B
+constexpr int TMEM_COLS = 128;                  // H uses 128 columns, Y reuses the first 32
+constexpr unsigned long long TIMEOUT_NS = 1000000000ull;
+static_assert(OFF_W2 % 1024 == 0 && W2_ATOM % 1024 == 0 && OFF_F % 1024 == 0 && OFF_G % 1024 == 0,
+              "swizzle atoms start on 1024 B");
+static_assert(OFF_BAR % 8 == 0 && 2 * (SMEM_ALLOC + 1024) <= 233472, "two CTAs per SM");
+// instruction descriptor of tcgen05.mma kind::f16: D f32 (bits 4-5 = 1), A and B BF16 (bits 7-9,
+// 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28
+constexpr uint32_t idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+}  // namespace tc
+
+__device__ __forceinline__ uint32_t tc_smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// byte offset of 16-byte chunk c of row r in a 128-byte-swizzled K-major atom
+__device__ __forceinline__ uint32_t tc_sw(int r, int c) { return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4)); }
+__device__ __forceinline__ void tc_st16(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+__device__ __forceinline__ uint32_t tc_pack(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(id), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ bool tc_bar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool tc_bar_wait(uint32_t bar, uint32_t parity) {
+  if (tc_bar_test(bar, parity)) return true;
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    for (int i = 0; i < 32; ++i)
+      if (tc_bar_test(bar, parity)) return true;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > tc::TIMEOUT_NS) return false;
+  }
+}
+
+// features of element e as 32 BF16 pairs from the Jacobi-scaled residual z = (r0 - kd) Dinv
+// (same arithmetic and order as element_features)
+__device__ __forceinline__ float element_features_packed(const FeatLevel &L, int e, const float *__restrict__ z,
+                                                         uint32_t (&xp)[32]) {
+  float rt[30];
+  float s2 = 0.f;
+#pragma unroll
+  for (int n = 0; n < 10; ++n) {
+    const int nod = L.el2nod[(size_t)n * L.nel + e];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float v = z[3 * nod + c];
+      rt[3 * n + c] = v;
+      s2 += v * v;
+    }
+  }
+  const float s = sqrtf(s2);
+  const float is = s > 0.f ? 1.0f / s : 0.f;
+#pragma unroll
+  for (int q = 0; q < 15; ++q) xp[q] = tc_pack(rt[2 * q] * is, rt[2 * q + 1] * is);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) xp[15 + q] = tc_pack(L.lvisc[(size_t)(2 * q) * L.nel + e], L.lvisc[(size_t)(2 * q + 1) * L.nel + e]);
+#pragma unroll
+  for (int q = 0; q < 6; ++q) xp[20 + q] = tc_pack(L.geo[(size_t)(2 * q) * L.nel + e], L.geo[(size_t)(2 * q + 1) * L.nel + e]);
+#pragma unroll
+  for (int q = 26; q < 32; ++q) xp[q] = 0u;
+  return s;
+}
+
+// z = (r0 - kd) Dinv in FP32 (kd may be null), the per-dof input of the features
+template <typename T>
+__global__ void k_ml_scale(const T *__restrict__ r0, const T *__restrict__ kd, const T *__restrict__ Dinv,
+                           float *__restrict__ z, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T rv = kd ? (T)(r0[i] - kd[i]) : r0[i];
+  z[i] = (float)(rv * Dinv[i]);
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+// barrier of the 128 compute threads (named barrier 1) that ANDs a predicate over them
+__device__ __forceinline__ bool tc_group_and(bool v) {
+  uint32_t out;
+  __syncwarp();
+  asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}"
+               : "=r"(out)
+               : "r"((uint32_t)v)
+               : "memory");
+  return out != 0;
+}
+__device__ __forceinline__ void tc_arrive(uint32_t bar) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(tc::THREADS, 2) k_ml_sweep_tc(FeatLevel L, MlpDev w, const float *__restrict__ z,
+                                                                float *__restrict__ C, int *__restrict__ err) {
+  using namespace tc;
+  extern __shared__ unsigned char smraw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t sbase = tc_smem_u32(sm);
+  const uint32_t f_full = sbase + OFF_BAR, f_empty = f_full + 16, mma_done = f_full + 32;
+  float *sb1 = reinterpret_cast<float *>(sm + tc::OFF_B1);
+  float *sb2 = reinterpret_cast<float *>(sm + tc::OFF_B2);
+  float *sS = reinterpret_cast<float *>(sm + OFF_S);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + OFF_TM);
+  // weights into the swizzled layouts: W1 row n (64 inputs = 8 chunks); W2 row n, hidden chunk k
+  {
+    const uint4 *g1 = reinterpret_cast<const uint4 *>(w.W1);
+    for (int i = tid; i < HID * 8; i += THREADS) {
+      const uint4 v = g1[i];
+      tc_st16(sbase + tc::OFF_W1 + tc_sw(i >> 3, i & 7), v.x, v.y, v.z, v.w);
+    }
+    const uint4 *g2 = reinterpret_cast<const uint4 *>(w.W2);
+    for (int i = tid; i < OUTP * 16; i += THREADS) {
+      const int n = i >> 4, k = i & 15;
+      const uint4 v = g2[i];
+      tc_st16(sbase + tc::OFF_W2 + (k >> 3) * W2_ATOM + tc_sw(n, k & 7), v.x, v.y, v.z, v.w);
+    }
+    if (tid < HID) sb1[tid] = w.b1[tid];
+    if (tid < OUTP) sb2[tid] = w.b2[tid];
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(f_full + 8 * b) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(f_empty + 8 * b) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mma_done) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem_u32(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int ntile = (L.nel + ROWS - 1) / ROWS;
+
+  if (warp >= 4) {
+    // ---------------- gather warps: features of tile i into feature buffer i & 1 ----------------
+    const int g = tid - 128;
+    int i = 0;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x, ++i) {
+      const int b = i & 1;
+      if (i >= 2 && !__all_sync(0xffffffffu, tc_bar_wait(f_empty + 8 * b, ((i >> 1) - 1) & 1))) {
+        if (lane == 0) atomicOr(err, 2);
+        break;
+      }
+      const int e = tile * ROWS + g;
+      uint32_t xp[32];
+      float s = 0.f;
+      if (e < L.nel) {
+        s = element_features_packed(L, e, z, xp);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) xp[q] = 0u;
+      }
+      const uint32_t fb = sbase + OFF_F + b * ATOM;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) tc_st16(fb + tc_sw(g, c), xp[4 * c], xp[4 * c + 1], xp[4 * c + 2], xp[4 * c + 3]);
+      sS[b * ROWS + g] = s;
+      tc_fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc_arrive(f_full + 8 * b);
+    }
+  } else {
+    // ---------------- compute warps: thread t owns row t (TMEM lane t) ----------------
+    const int t = tid;
+    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    uint32_t phase = 0;
+    bool ok = true, pending = false;
+    int i = 0;
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x, ++i) {
+      const int b = i & 1;
+      ok = tc_bar_wait(f_full + 8 * b, (i >> 1) & 1);
+      const float s = sS[b * ROWS + t];
+      // every thread has read its norm and its row of the previous Y: the MMAs may start
+      tc_fence_before();
+      if (!tc_group_and(ok)) break;
+      if (t == 0) {
+        tc_fence_after();
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          tc_mma(tmem, tc_sdesc(sbase + OFF_F + b * ATOM + 32 * k), tc_sdesc(sbase + tc::OFF_W1 + 32 * k),
+                 idesc(ROWS, HID), k > 0);
+        tc_commit(f_empty + 8 * b);      // the feature buffer is free once these MMAs are done
+        tc_commit(mma_done);
+      }
+      pending = true;
+      ok = tc_bar_wait(mma_done, phase);
+      if (!tc_group_and(ok)) break;
+      phase ^= 1;
+      pending = false;
+      tc_fence_after();
+      // G = gelu(H + b1): hidden 64a..64a+63 in atom a, 16-column chunk c in swizzle chunks 2c, 2c+1
+#pragma unroll 1
+      for (int c2 = 0; c2 < HID / 32; ++c2) {
+        float h[32];
+        tc_ld32(trow + 32 * c2, h);
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int c = 2 * c2 + half;
+          uint32_t gv[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            gv[q] = tc_pack(gelu(h[16 * half + 2 * q] + sb1[16 * c + 2 * q]),
+                            gelu(h[16 * half + 2 * q + 1] + sb1[16 * c + 2 * q + 1]));
+          const uint32_t atom = sbase + OFF_G + (c >> 2) * ATOM;
+          tc_st16(atom + tc_sw(t, 2 * (c & 3)), gv[0], gv[1], gv[2], gv[3]);
+          tc_st16(atom + tc_sw(t, 2 * (c & 3) + 1), gv[4], gv[5], gv[6], gv[7]);
+        }
+      }
+      tc_fence_async_smem();
+      tc_fence_before();
+      tc_group_and(true);
+      if (t == 0) {
+        tc_fence_after();
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          tc_mma(tmem, tc_sdesc(sbase + OFF_G + (k >> 2) * ATOM + 32 * (k & 3)),
+                 tc_sdesc(sbase + tc::OFF_W2 + (k >> 2) * W2_ATOM + 32 * (k & 3)), idesc(ROWS, OUTP), k > 0);
+        tc_commit(mma_done);
+      }
+      pending = true;
+      ok = tc_bar_wait(mma_done, phase);
+      if (!tc_group_and(ok)) break;
+      phase ^= 1;
+      pending = false;
+      tc_fence_after();
+      float y[32];
+      tc_ld32(trow, y);
+      const int e = tile * ROWS + t;
+      if (e < L.nel) {
+        float2 *out = reinterpret_cast<float2 *>(C + (size_t)e * OUT);
+#pragma unroll
+        for (int q = 0; q < OUT / 2; ++q)
+          out[q] = make_float2(s * (y[2 * q] + sb2[2 * q]), s * (y[2 * q + 1] + sb2[2 * q + 1]));
+      }
+    }
+    if (!ok) {
+      if (t == 0) atomicOr(err, 1);
+      if (pending) tc_bar_wait(mma_done, phase);    // MMAs of the abandoned wait, if they still run
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// gather of row-layout corrections C[e][30]: code entries e * 10 + a, element order (same sums as
+// k_ml_gather); each (element, node) triple is read with one 8-byte and one 4-byte load
+template <typename T>
+__global__ void k_ml_gather_rows(int nnod, const int *__restrict__ ptr, const int *__restrict__ code,
+                                 const float *__restrict__ C, const uint8_t *__restrict__ mask, T *__restrict__ d) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnod) return;
+  const int b = ptr[n], e = ptr[n + 1];
+  if (e <= b) return;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  for (int k = b; k < e; ++k) {
+    const int el = code[k] / 10, a = code[k] - 10 * el;
+    const float *c = C + (size_t)el * OUT + 3 * a;
+    if ((a & 1) == 0) {
+      const float2 v = *reinterpret_cast<const float2 *>(c);
+      s0 += v.x;
+      s1 += v.y;
+      s2 += c[2];
+    } else {
+      const float2 v = *reinterpret_cast<const float2 *>(c + 1);
+      s0 += c[0];
+      s1 += v.x;
+      s2 += v.y;
+    }
+  }
+  const float w = 1.0f / (float)(e - b);
+  if (mask[3 * n] && isfinite(s0)) d[3 * n] += (T)(w * s0);
+  if (mask[3 * n + 1] && isfinite(s1)) d[3 * n + 1] += (T)(w * s1);
+  if (mask[3 * n + 2] && isfinite(s2)) d[3 * n + 2] += (T)(w * s2);
+}
+
+// ---------------------------------------------------------------------------------------
 // training: fused forward + backward on TR_ROWS samples per CTA, gradients atomically summed
 // ---------------------------------------------------------------------------------------
 constexpr size_t TR_SMEM = sizeof(__nv_bfloat16) * (TR_ROWS * LDX + HID * LDX + TR_ROWS * LDH + OUTP * LDH +
@@ -368,7 +731,8 @@ namespace m3sph {
 struct MlLevel {
   int *n2e_ptr = nullptr, *n2e_code = nullptr;   // node -> (stored element * 10 + local node)
   float *lvisc = nullptr, *geo = nullptr;         // [10][nel], [12][nel]
-  float *C = nullptr;                             // [30][nel] corrections
+  float *C = nullptr;                             // 30 corrections per element ([30][nel] or [nel][30])
+  float *z = nullptr;                             // [3 nnod] Jacobi-scaled residual (fused sweep)
 };
 
 struct MlState {
@@ -379,6 +743,7 @@ struct MlState {
   float *b1 = nullptr, *b2 = nullptr;
   bool trained = false;
   long adam_t = 0;
+  int *err = nullptr;          // bounded waits of the fused sweep that gave up
   // dataset
   __nv_bfloat16 *X = nullptr, *X2 = nullptr;
   float *T = nullptr, *T2 = nullptr;
@@ -436,11 +801,11 @@ int ml_build(m3sph_mesh *M) {
     MlState *S = reinterpret_cast<MlState *>(p);
     for (int i = 0; i < 2; ++i)
       for (void *q : {(void *)S->lev[i].n2e_ptr, (void *)S->lev[i].n2e_code, (void *)S->lev[i].lvisc,
-                      (void *)S->lev[i].geo, (void *)S->lev[i].C})
+                      (void *)S->lev[i].geo, (void *)S->lev[i].C, (void *)S->lev[i].z})
         if (q) cudaFree(q);
     for (void *q : {(void *)S->params, (void *)S->m, (void *)S->v, (void *)S->grad, (void *)S->loss, (void *)S->W1,
                     (void *)S->W2, (void *)S->b1, (void *)S->b2, (void *)S->X, (void *)S->X2, (void *)S->T,
-                    (void *)S->T2})
+                    (void *)S->T2, (void *)S->err})
       if (q) cudaFree(q);
     delete S;
   };
@@ -465,7 +830,10 @@ int ml_build(m3sph_mesh *M) {
     M3_TRY(ml_alloc(&ml.lvisc, 10 * (size_t)L.nel));
     M3_TRY(ml_alloc(&ml.geo, 12 * (size_t)L.nel));
     M3_TRY(ml_alloc(&ml.C, 30 * (size_t)L.nel));
+    M3_TRY(ml_alloc(&ml.z, (size_t)L.ndof));
   }
+  M3_TRY(ml_alloc(&S->err, 1));
+  M3_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int), s));
   M3_TRY(ml_alloc(&S->params, NPARAM));
   M3_TRY(ml_alloc(&S->m, NPARAM));
   M3_TRY(ml_alloc(&S->v, NPARAM));
@@ -516,19 +884,56 @@ __global__ void k_sub(const T *a, const T *b, T *out, size_t n) {
   if (i < n) out[i] = a[i] - b[i];
 }
 
+// inference kernels: 1 fused tcgen05 sweep (default), 0 the WMMA tile kernel with column-layout
+// corrections and a separate residual pass (kept as the reference form for tests)
+static int g_ml_infer = 1;
+static int g_nsm = 152;
+int ml_set_infer(int v) {
+  if (v != 0 && v != 1) {
+    set_error("ml_infer must be 0 or 1");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  g_ml_infer = v;
+  return M3SPH_OK;
+}
+
+int ml_check(m3sph_mesh *M) {
+  MlState *S = mls(M);
+  if (!S || !S->err) return M3SPH_OK;
+  int h = 0;
+  M3_CUDA(cudaMemcpyAsync(&h, S->err, sizeof(int), cudaMemcpyDeviceToHost, M->stream));
+  M3_CUDA(cudaStreamSynchronize(M->stream));
+  if (h) {
+    M3_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int), M->stream));
+    set_error("learned smoother sweep: a bounded wait gave up");
+    return M3SPH_ERR_CUDA;
+  }
+  return M3SPH_OK;
+}
+
 // d += PoU(MLP(features(r0 - kd))) on level j (kd may be null: residual r0)
 template <typename T>
 int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *tmp, T *d) {
   MlState *S = mls(M);
   Level &L = M->lev[j];
   cudaStream_t s = M->stream;
+  FeatLevel f{L.nel, L.el2nod, S->lev[j].lvisc, S->lev[j].geo};
+  MlpDev w{S->W1, S->W2, S->b1, S->b2};
+  if (g_ml_infer == 1) {
+    const int ntile = (L.nel + tc::ROWS - 1) / tc::ROWS;
+    const int grid = std::min(ntile, 2 * g_nsm);
+    k_ml_scale<T><<<(unsigned)((L.ndof + 255) / 256), 256, 0, s>>>(r0, kd, Dinv, S->lev[j].z, L.ndof); count_launch();
+    k_ml_sweep_tc<<<grid, tc::THREADS, tc::SMEM_ALLOC, s>>>(f, w, S->lev[j].z, S->lev[j].C, S->err); count_launch();
+    k_ml_gather_rows<T><<<(L.nnod + 127) / 128, 128, 0, s>>>(L.nnod, S->lev[j].n2e_ptr, S->lev[j].n2e_code,
+                                                              S->lev[j].C, L.freemask, d); count_launch();
+    M3_CUDA(cudaGetLastError());
+    return M3SPH_OK;
+  }
   const T *r = r0;
   if (kd) {
     k_sub<T><<<(unsigned)((L.ndof + 255) / 256), 256, 0, s>>>(r0, kd, tmp, L.ndof); count_launch();
     r = tmp;
   }
-  FeatLevel f{L.nel, L.el2nod, S->lev[j].lvisc, S->lev[j].geo};
-  MlpDev w{S->W1, S->W2, S->b1, S->b2};
   k_ml_infer<T><<<(L.nel + INF_ROWS - 1) / INF_ROWS, 256, INF_SMEM, s>>>(f, w, r, Dinv, S->lev[j].C); count_launch();
   k_ml_gather<T><<<(L.nnod + 127) / 128, 128, 0, s>>>(L.nnod, L.nel, S->lev[j].n2e_ptr, S->lev[j].n2e_code,
                                                        S->lev[j].C, L.freemask, d); count_launch();
@@ -542,6 +947,10 @@ int ml_init_kernels() {
   M3_CUDA(cudaFuncSetAttribute(k_ml_infer<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)INF_SMEM));
   M3_CUDA(cudaFuncSetAttribute(k_ml_infer<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)INF_SMEM));
   M3_CUDA(cudaFuncSetAttribute(k_ml_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TR_SMEM));
+  M3_CUDA(cudaFuncSetAttribute(k_ml_sweep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_ALLOC));
+  int dev = 0;
+  M3_CUDA(cudaGetDevice(&dev));
+  M3_CUDA(cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev));
   return M3SPH_OK;
 }
 

@@ -1307,6 +1307,7 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   M3_TRY(coupled_residual(M, U, Pd, rel));
   inf.rel_residual = rel;
   M3_TRY(stream_check(L0, s));
+  M3_TRY(ml_check(M));
   return M3SPH_OK;
 }
 
@@ -1553,6 +1554,29 @@ extern "C" int m3sph_level_apply32(m3sph_mesh *M, int32_t img, const float *x, f
   return M3SPH_OK;
 }
 
+extern "C" int m3sph_ml_sweep32(m3sph_mesh *M, int32_t img, const float *r, const float *kd, float *d) {
+  M3_TRY(need_op(M));
+  if (!M->ml || img < 0 || img >= std::min(2, M->nmg)) {
+    set_error("m3sph_ml_sweep32: no learned smoother on this level");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Level &L = M->lev[img];
+  if (!L.Dinv32) {
+    set_error("no FP32 operator on this level (set up with precision 1)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  const size_t n = L.ndof;
+  M3_CUDA(cudaMemcpyAsync(W->r32[img], r, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  if (kd) M3_CUDA(cudaMemcpyAsync(W->kd32[img], kd, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(W->d32[img], d, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  M3_TRY(ml_sweep<float>(M, img, W->r32[img], kd ? W->kd32[img] : nullptr, L.Dinv32, W->t32[img], W->d32[img]));
+  M3_CUDA(cudaMemcpyAsync(d, W->d32[img], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  return ml_check(M);
+}
+
 extern "C" int m3sph_prolong(m3sph_mesh *M, int32_t img, const double *xc, double *xf) {
   M3_TRY(need_op(M));
   if (img < 0 || img + 1 >= M->nmg) {
@@ -1685,6 +1709,8 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
       return M3SPH_ERR_BAD_INPUT;
     }
     M->ml_schedule = value;
+  } else if (n == "ml_infer") {
+    M3_TRY(ml_set_infer(value));
   } else if (n == "stream_f32_variant") {
     M3_TRY(stream_set_f32_variant(value));
   } else if (n == "stream_outer") {

@@ -52,6 +52,15 @@ def forward(dm, X):
     return Y
 
 
+def sweep32(dm, level, r, d, kd=None):
+    """One learned sweep of `level` in FP32 (m3sph_ml_sweep32): returns d + the gathered corrections."""
+    r = np.ascontiguousarray(r, dtype=np.float32)
+    out = np.array(d, dtype=np.float32, copy=True)
+    kdp = None if kd is None else L.fptr(np.ascontiguousarray(kd, dtype=np.float32))
+    L.check(L.lib().m3sph_ml_sweep32(dm.h, int(level), L.fptr(r), kdp, L.fptr(out)))
+    return out
+
+
 def gradients(dm, X, T):
     X = np.ascontiguousarray(X, dtype=np.float32)
     T = np.ascontiguousarray(T, dtype=np.float32)

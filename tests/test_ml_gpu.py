@@ -79,3 +79,45 @@ def test_learned_smoother_solution_and_fallback(dm_tiny):
     assert np.linalg.norm(U1 - U0) < 1e-6 * np.linalg.norm(U0)
     print(f"jacobi: {i0['nitU'] + i0['nitZ']} its, learned: {i1['nitU'] + i1['nitZ']} its, "
           f"fallbacks {i1['smoother_fallbacks']}")
+
+
+def _sweep_both(dm, level, r, d0, kd):
+    from m3tet_sph_gb300 import learned
+    y1 = learned.sweep32(dm, level, r, d0, kd)
+    y1b = learned.sweep32(dm, level, r, d0, kd)
+    try:
+        dm.set_option("ml_infer", 0)
+        y0 = learned.sweep32(dm, level, r, d0, kd)
+    finally:
+        dm.set_option("ml_infer", 1)
+    return y1, y1b, y0
+
+
+@pytest.mark.parametrize("mesh", ["tiny", "shell491k"])
+def test_fused_tcgen05_sweep_matches_wmma_kernel(built_lib, tiny_plates, mesh):
+    """The fused tcgen05 sweep (default) against the WMMA tile kernel on the same residuals and
+    the trained weights: the same features, FP32 accumulation in either order, BF16 hidden
+    activations (a rounding flip moves an output by ~1e-3 of its size), the same node sums. The
+    491,520-element shell gives each persistent CTA several tiles."""
+    from pathlib import Path
+    from m3tet_sph_gb300 import learned, stokes, workloads
+    w = tiny_plates if mesh == "tiny" else workloads.make_workload('prof')
+    dm = stokes.DeviceMesh(w['levels'])
+    try:
+        dm.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
+        p = np.load(Path(learned.__file__).with_name('smoother_c1.npy'))
+        learned.set_params(dm, p, trained=True)
+        rng = np.random.default_rng(21)
+        for level in (0, 1):
+            n = 3 * w['levels'][level]['nnod']
+            r, kd, d0 = (rng.standard_normal(n).astype(np.float32) for _ in range(3))
+            for k in (kd, None):
+                y1, y1b, y0 = _sweep_both(dm, level, r, d0, k)
+                assert np.array_equal(y1, y1b)                     # deterministic
+                c1, c0 = y1 - d0, y0 - d0
+                assert np.all(np.isfinite(c1)) and np.linalg.norm(c0) > 0
+                assert np.linalg.norm(c1 - c0) < 1e-2 * np.linalg.norm(c0), (level, k is None)
+                fixed = c0 == 0
+                assert np.all(c1[fixed] == 0)                      # fixed dofs untouched
+    finally:
+        dm.close()
