@@ -221,7 +221,7 @@ struct m3sph_mesh {
   bool use_graphs = true;
   bool df_outer = true;               // double-float outer operator on the mixed path
   bool split_apply = true;            // 4-warp split element-by-element kernels on the finest level
-  int ml_schedule = 0;                // learned smoothing per side: 0 learned-Jacobi-learned, 1 one learned sweep
+  int ml_schedule = 1;                // learned smoothing per side: 0 learned-Jacobi-learned, 1 one learned sweep
   unsigned long long graph_kernels = 0;   // kernel launches per captured iteration
   void *ml = nullptr;                 // learned smoother state
   void (*ml_free)(void *) = nullptr;

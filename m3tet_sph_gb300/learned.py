@@ -110,7 +110,7 @@ def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_
     return get_params(dm), dict(mse=hist, t_collect=t_collect, t_train=t_train, stride=stride)
 
 
-def evaluate(dm, w, params=None, solver_kw=None, repeats=1, schedule=0):
+def evaluate(dm, w, params=None, solver_kw=None, repeats=1, schedule=1):
     """Solve once with the Jacobi smoother and once with the learned smoother on the mesh and fields
     of workload `w` (FP32 V-cycle): iteration counts, times and the difference of the answers."""
     kw = dict(rtol_Pat=1e-7, rtol_U=5e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=1e-8)
@@ -144,7 +144,7 @@ def main(argv=None):
     ap.add_argument("--samples", type=int, default=2_000_000)
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--schedule", type=int, default=0, help="0: learned-Jacobi-learned per side, 1: one learned sweep")
+    ap.add_argument("--schedule", type=int, default=1, help="0: learned-Jacobi-learned per side, 1: one learned sweep")
     a = ap.parse_args(argv)
     w = workloads.make_workload(a.workload, seed=a.seed)
     dm = stokes.DeviceMesh(w['levels'])
