@@ -195,7 +195,7 @@ def run_gb300(args, rank, ws, td):
 
     # the same FP32 solve with weighted-Jacobi smoothing (reported beside the product)
     jac = None
-    if use_learned:
+    if use_learned and not args.skip_jacobi:
         ms_j, infos_j, _ = timed(0, 1, args.steps)
         lj = infos_j[-1]
         jac = {"s_per_solve": allmax(td, ms_j) / 1e3, "nitU": lj["nitU"], "nitZ": lj["nitZ"], "itPat": lj["itPat"],
@@ -224,7 +224,7 @@ def run_gb300(args, rank, ws, td):
         learned = {"schedule": "one learned sweep per side on levels 0 and 1 (ml_schedule 1)",
                    "nitU": last["nitU"], "nitZ": last["nitZ"], "itPat": last["itPat"],
                    "smoother_fallbacks": last["smoother_fallbacks"], "fp32_mg_jacobi": jac,
-                   "speedup_vs_jacobi": jac["s_per_solve"] / (ms / 1e3),
+                   "speedup_vs_jacobi": jac["s_per_solve"] / (ms / 1e3) if jac else None,
                    "weights": "trained on the 130,662-DOF shell, 20 viscosity fields (contrast 1e2-1e5), ~2M pairs"}
     # ---- end-to-end through the public API with host buffers ----
     U = np.empty(ndof)
@@ -456,7 +456,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=988,
                     help="MG-PCG iterations the reference arm charges per solve (nitU + nitZ of the "
                          "plain-FP64 GPU solve of the 8M-DOF shell)")
-    ap.add_argument("--skip-learned", action="store_true")
+    ap.add_argument("--skip-learned", action="store_true", help="time the Jacobi-smoothed FP32 solve instead")
+    ap.add_argument("--skip-jacobi", action="store_true", help="skip the Jacobi-smoothed comparison solve")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--sl-only", action="store_true", help="semi-Lagrangian rates only (profiling)")
     ap.add_argument("--sweep-only", action="store_true", help="with --sl-only: the location sweep alone")
