@@ -121,6 +121,8 @@ def peaks():
 # DRAM bytes per element of one streamed FP32 apply (both kernels), from the ncu capture of the
 # 491,520-element shell: (948.76 + 20.05 + 83.85 + 4.28) MB / 491,520
 TRAFFIC_PER_ELEMENT_F32 = (948.76e6 + 20.05e6 + 83.85e6 + 4.28e6) / 491520
+# the same for the double-float outer apply (k_stream_rowlane<RlDF> + k_node_gather_f64)
+TRAFFIC_PER_ELEMENT_DF = (1.900e9 + 72.74e6 + 190.52e6 + 10.03e6) / 491520
 
 
 def apply_bytes_df(nel, ndof):
@@ -212,13 +214,31 @@ def run_gb300(args, rank, ws, td):
     ms = allmax(td, ms)
     clocks = clk.summary(dev)
     last = infos[-1]
-    # ---- operator roofline: the finest-level FP32 apply (phase 1 k_stream_elem_f32 + phase 2
-    # k_node_gather_f32), the dominant unit of the V-cycle; and the double-float outer apply ----
+    # ---- operator rooflines: the finest-level FP32 apply (phase 1 k_stream_elem_f32 + phase 2
+    # k_node_gather_f32) and the double-float outer apply, both timed with CUDA events ----
     ms_apply32 = dm.apply_timing(0, 1, 10)
     ms_apply_df = dm.apply_timing(0, 2, 10)
     hbm, peak_kind = peaks()
     b32 = apply_bytes(nel, ndof, 4)
     achieved = b32 / (ms_apply32 * 1e-3) / 1e9
+    # dominant kernel: with the learned smoother (2 finest FP32 applies per iteration) the one
+    # double-float outer apply per iteration takes the largest share; with Jacobi (6 FP32 applies
+    # per iteration) the FP32 apply does
+    bdf = apply_bytes_df(nel, ndof)
+    fp32 = {"kernel": "finest-level FP32 apply: k_stream_elem_f32 + k_node_gather_f32",
+            "achieved": achieved, "frac": achieved / hbm, "traffic": TRAFFIC_PER_ELEMENT_F32 * nel,
+            "bytes_per_apply": b32, "ms_per_apply": ms_apply32, "dof_per_s": ndof / (ms_apply32 * 1e-3)}
+    df = {"kernel": "finest-level double-float outer apply: k_stream_rowlane<RlDF> + k_node_gather_f64",
+          "achieved": bdf / (ms_apply_df * 1e-3) / 1e9, "traffic": TRAFFIC_PER_ELEMENT_DF * nel,
+          "bytes_per_apply": bdf, "ms_per_apply": ms_apply_df, "dof_per_s": ndof / (ms_apply_df * 1e-3)}
+    df["frac"] = df["achieved"] / hbm
+    top, other = (df, fp32) if use_learned else (fp32, df)
+    roofline = {"bound": "hbm", **top, "peak": hbm, "unit": "GB/s", "peak_kind": peak_kind,
+                "traffic_source": "ncu dram__bytes_read+write of both kernels on the 491,520-element shell, "
+                                  "scaled by element count",
+                "other_apply": other,
+                "fp64_apply_ms": fp64_apply_ms if plain else None,
+                "fp64_apply_gbs": apply_bytes(nel, ndof, 8) / (fp64_apply_ms * 1e-3) / 1e9 if plain else None}
     learned = None
     if use_learned:
         learned = {"schedule": "one learned sweep per side on levels 0 and 1 (ml_schedule 1)",
@@ -263,17 +283,7 @@ def run_gb300(args, rank, ws, td):
             "itPat": plain["info"]["itPat"], "nitU": plain["info"]["nitU"], "nitZ": plain["info"]["nitZ"],
             "t_setup_ms": plain["info"]["t_setup_ms"], "fp64_apply_ms": fp64_apply_ms,
             "speedup_mixed_vs_plain": plain["s_per_solve"] / (ms / 1e3)},
-        "roofline": {"bound": "hbm", "kernel": "finest-level FP32 apply: k_stream_elem_f32 + k_node_gather_f32",
-                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
-                     "traffic": TRAFFIC_PER_ELEMENT_F32 * nel,
-                     "traffic_source": "ncu dram__bytes_read+write of both kernels on the 491,520-element shell, "
-                                       "scaled by element count",
-                     "bytes_per_apply": b32, "ms_per_apply": ms_apply32,
-                     "dof_per_s": ndof / (ms_apply32 * 1e-3),
-                     "outer_df_apply_ms": ms_apply_df,
-                     "outer_df_apply_gbs": apply_bytes_df(nel, ndof) / (ms_apply_df * 1e-3) / 1e9,
-                     "fp64_apply_ms": fp64_apply_ms if plain else None,
-                     "fp64_apply_gbs": apply_bytes(nel, ndof, 8) / (fp64_apply_ms * 1e-3) / 1e9 if plain else None},
+        "roofline": roofline,
         "learned_smoother": learned,
         "accuracy": accuracy,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
