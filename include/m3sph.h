@@ -155,9 +155,9 @@ M3SPH_API int m3sph_ml_nparam(int32_t *n);
 M3SPH_API int m3sph_ml_set_params(m3sph_mesh *mesh, const float *params, int32_t trained);
 M3SPH_API int m3sph_ml_get_params(m3sph_mesh *mesh, float *params);
 /* Training data: reserve room for `capacity` samples, then append (local residual, local error)
- * pairs of the current operator: a seeded random right-hand side is solved with the plain
- * multigrid to 1e-10 and every `stride`-th element of n_iterates plain-multigrid iterates
- * contributes one sample. */
+ * pairs of the current operator: for each of n_iterates seeded white-noise errors e on the free
+ * dofs, r = K e with the outer (FP64-accurate) operator, and every `stride`-th element contributes
+ * the features of r and its local values of e. */
 M3SPH_API int m3sph_ml_reserve(m3sph_mesh *mesh, int64_t capacity);
 M3SPH_API int m3sph_ml_collect(m3sph_mesh *mesh, uint64_t seed, int32_t n_iterates, int32_t stride, int64_t *count);
 /* One Adam epoch over the shuffled samples (batch a multiple of 64); mse = mean squared error. */

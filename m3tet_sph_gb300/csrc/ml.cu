@@ -6,8 +6,9 @@
 // correction that is gathered to the nodes with partition-of-unity weights 1/multiplicity
 // (atomic-free). The network replaces Jacobi sweeps on the two finest levels of the V-cycle; the
 // FP64 outer CG judges its effect, so it changes iteration counts but not the converged answer.
-// Training pairs (local residual, local error) come from the plain-multigrid iterates of the
-// project's own solves; training runs here with these forward / backward kernels and Adam.
+// Training pairs (local residual, local error) are (K e, e) for white-noise errors e on the
+// project's own operators; training runs here with these forward / backward kernels and Adam.
+// Inference runs either as the fused tcgen05 sweep (default) or as the WMMA tile kernel.
 #include <mma.h>
 
 #include "common.cuh"
