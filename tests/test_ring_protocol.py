@@ -1,4 +1,5 @@
-"""CPU model of the mbarrier ring protocols of the streamed element applies (csrc/stream_apply.cu).
+"""CPU model of the mbarrier ring protocols of the streamed element applies (csrc/stream_apply.cu)
+and of the fused learned-smoother sweep (csrc/ml.cu, k_ml_sweep_tc).
 
 Each agent (producer warp, gather warps, consumer groups / warps) is a generator that yields while it
 waits; a seeded scheduler interleaves them and completes in-flight copies at random moments. A barrier
@@ -200,6 +201,83 @@ def run_rowlane(nchunk, seed, tags=True, NST=7, NOWN=4):
     done = _schedule(tasks, inflight, rnd)
     return done and sorted(m for m, *_ in log) == list(range(nchunk)) and \
         all(h == d == ('c', m) for m, h, d in log)
+
+
+def run_mlsweep(ntile, seed, commit_after_mma2=False, free_early=False):
+    """k_ml_sweep_tc: 4 gather warps fill feature buffer i & 1 (f_full, count 4) once the MMA that
+    read it has completed (f_empty); the compute group issues MMA1 (commit -> f_empty, mma_done), reads
+    H, writes G, issues MMA2 (commit -> mma_done) and reads Y. MMAs complete asynchronously.
+    `free_early` models a wrong protocol that frees the buffer when MMA1 is issued instead of when it
+    completes."""
+    rnd = random.Random(seed)
+    f_full = [Bar(4) for _ in range(2)]
+    f_empty = [Bar(1) for _ in range(2)]
+    mma_done = Bar(1)
+    feat, norm = [None, None], [None, None]
+    tmem, g_buf = [None], [None]
+    inflight, log = [], []
+
+    def gather(wid):
+        for i in range(ntile):
+            b = i & 1
+            if i >= 2:
+                while not f_empty[b].test(((i >> 1) - 1) & 1):
+                    yield 'w'
+            if wid == 0:
+                feat[b], norm[b] = ('f', i), ('s', i)
+            yield 's'
+            f_full[b].arrive()
+
+    def compute():
+        phase = 0
+        for i in range(ntile):
+            b = i & 1
+            while not f_full[b].test((i >> 1) & 1):
+                yield 'w'
+            s = norm[b]
+            # MMA1 reads the feature buffer when it completes
+            src = b
+            # both commits track the same MMA: they arrive together once it has read its operands
+            mma_done.arrive(tx=1)
+            if free_early:
+                f_empty[b].arrive()
+            else:
+                f_empty[b].arrive(tx=1)
+
+            def mma1_done(src=src, b=b):
+                tmem[0] = ('H', feat[src])
+                if not free_early:
+                    f_empty[b].complete(1)
+            inflight.append((mma_done, mma1_done))
+            while not mma_done.test(phase):
+                yield 'w'
+            phase ^= 1
+            h = tmem[0]
+            g_buf[0] = ('G', h)
+            yield 's'
+            mma_done.arrive(tx=1)
+            inflight.append((mma_done, lambda: tmem.__setitem__(0, ('Y', g_buf[0]))))
+            while not mma_done.test(phase):
+                yield 'w'
+            phase ^= 1
+            log.append((i, s, tmem[0]))
+
+    tasks = {'C': compute(), **{f'G{w}': gather(w) for w in range(4)}}
+    done = _schedule(tasks, inflight, rnd)
+    return done and [m for m, *_ in log] == list(range(ntile)) and \
+        all(s == ('s', m) and y == ('Y', ('G', ('H', ('f', m)))) for m, s, y in log)
+
+
+def test_mlsweep_protocol_never_deadlocks_or_mixes_tiles():
+    bad = [(n, seed) for n in (1, 2, 3, 4, 7, 20) for seed in range(80) if not run_mlsweep(n, seed)]
+    assert not bad, bad[:5]
+
+
+def test_mlsweep_freeing_at_issue_is_wrong():
+    """Freeing the feature buffer when MMA1 is issued (not when it completes) lets the gather of tile
+    i + 2 overwrite features that MMA1 of tile i has not read yet."""
+    bad = sum(not run_mlsweep(n, seed, free_early=True) for n in (3, 4, 7, 20) for seed in range(80))
+    assert bad > 0
 
 
 SIZES = [1, 2, 3, 5, 7, 13, 40, 150]
