@@ -178,7 +178,8 @@ M3SPH_API int m3sph_ml_sweep32(m3sph_mesh *mesh, int32_t img, const float *r, co
  * "split_apply" (4-warp per-colour kernels when streaming is off, default 1), "graphs" (CUDA-graph
  * replay of MG-PCG iterations, default 1), "df_outer" (double-float outer operator on the mixed
  * path, default 1), "ml_schedule" (learned smoothing: 0 learned-Jacobi-learned, 1 one learned
- * sweep per side, default; per handle), "ml_infer" (learned sweep kernels: 1 fused tcgen05 sweep, default;
+ * sweep per side, default; per handle), "ml_omega_pct" (relaxation weight of the learned correction
+ * in percent, 10-300, default 100; per handle), "ml_infer" (learned sweep kernels: 1 fused tcgen05 sweep, default;
  * 0 WMMA tile kernel), "stream_f32_variant" (slot-ring depth / gather warps of the streamed FP32
  * kernel, 0-3, default 0). */
 M3SPH_API int m3sph_set_option(m3sph_mesh *mesh, const char *name, int32_t value);

@@ -222,6 +222,7 @@ struct m3sph_mesh {
   bool df_outer = true;               // double-float outer operator on the mixed path
   bool split_apply = true;            // 4-warp split element-by-element kernels on the finest level
   int ml_schedule = 1;                // learned smoothing per side: 0 learned-Jacobi-learned, 1 one learned sweep
+  float ml_omega = 1.0f;              // relaxation weight of the learned correction
   unsigned long long graph_kernels = 0;   // kernel launches per captured iteration
   void *ml = nullptr;                 // learned smoother state
   void (*ml_free)(void *) = nullptr;

@@ -171,10 +171,11 @@ __global__ void __launch_bounds__(256) k_ml_infer(FeatLevel L, MlpDev w, const T
   }
 }
 
-// d[3n+c] += sum over (element, local node) of node n of C[3a+c][e] / multiplicity(n)
+// d[3n+c] += omega * sum over (element, local node) of node n of C[3a+c][e] / multiplicity(n)
 template <typename T>
 __global__ void k_ml_gather(int nnod, int nel, const int *__restrict__ ptr, const int *__restrict__ code,
-                            const float *__restrict__ C, const uint8_t *__restrict__ mask, T *__restrict__ d) {
+                            const float *__restrict__ C, const uint8_t *__restrict__ mask, float omega,
+                            T *__restrict__ d) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nnod) return;
   const int b = ptr[n], e = ptr[n + 1];
@@ -188,7 +189,7 @@ __global__ void k_ml_gather(int nnod, int nel, const int *__restrict__ ptr, cons
   }
   // a non-finite correction (an unusable network) is dropped; the outer CG's rate check then
   // switches the smoother off
-  const float w = 1.0f / (float)(e - b);
+  const float w = omega / (float)(e - b);
   if (mask[3 * n] && isfinite(s0)) d[3 * n] += (T)(w * s0);
   if (mask[3 * n + 1] && isfinite(s1)) d[3 * n + 1] += (T)(w * s1);
   if (mask[3 * n + 2] && isfinite(s2)) d[3 * n + 2] += (T)(w * s2);
@@ -530,7 +531,8 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_ml_sweep_tc(FeatLevel L, Mlp
 // k_ml_gather); each (element, node) triple is read with one 8-byte and one 4-byte load
 template <typename T>
 __global__ void k_ml_gather_rows(int nnod, const int *__restrict__ ptr, const int *__restrict__ code,
-                                 const float *__restrict__ C, const uint8_t *__restrict__ mask, T *__restrict__ d) {
+                                 const float *__restrict__ C, const uint8_t *__restrict__ mask, float omega,
+                                 T *__restrict__ d) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nnod) return;
   const int b = ptr[n], e = ptr[n + 1];
@@ -551,7 +553,7 @@ __global__ void k_ml_gather_rows(int nnod, const int *__restrict__ ptr, const in
       s2 += v.y;
     }
   }
-  const float w = 1.0f / (float)(e - b);
+  const float w = omega / (float)(e - b);
   if (mask[3 * n] && isfinite(s0)) d[3 * n] += (T)(w * s0);
   if (mask[3 * n + 1] && isfinite(s1)) d[3 * n + 1] += (T)(w * s1);
   if (mask[3 * n + 2] && isfinite(s2)) d[3 * n + 2] += (T)(w * s2);
@@ -926,7 +928,7 @@ int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *t
     k_ml_scale<T><<<(unsigned)((L.ndof + 255) / 256), 256, 0, s>>>(r0, kd, Dinv, S->lev[j].z, L.ndof); count_launch();
     k_ml_sweep_tc<<<grid, tc::THREADS, tc::SMEM_ALLOC, s>>>(f, w, S->lev[j].z, S->lev[j].C, S->err); count_launch();
     k_ml_gather_rows<T><<<(L.nnod + 127) / 128, 128, 0, s>>>(L.nnod, S->lev[j].n2e_ptr, S->lev[j].n2e_code,
-                                                              S->lev[j].C, L.freemask, d); count_launch();
+                                                              S->lev[j].C, L.freemask, M->ml_omega, d); count_launch();
     M3_CUDA(cudaGetLastError());
     return M3SPH_OK;
   }
@@ -937,7 +939,7 @@ int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *t
   }
   k_ml_infer<T><<<(L.nel + INF_ROWS - 1) / INF_ROWS, 256, INF_SMEM, s>>>(f, w, r, Dinv, S->lev[j].C); count_launch();
   k_ml_gather<T><<<(L.nnod + 127) / 128, 128, 0, s>>>(L.nnod, L.nel, S->lev[j].n2e_ptr, S->lev[j].n2e_code,
-                                                       S->lev[j].C, L.freemask, d); count_launch();
+                                                       S->lev[j].C, L.freemask, M->ml_omega, d); count_launch();
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }

@@ -1709,6 +1709,12 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
       return M3SPH_ERR_BAD_INPUT;
     }
     M->ml_schedule = value;
+  } else if (n == "ml_omega_pct") {
+    if (value < 10 || value > 300) {
+      set_error("ml_omega_pct must be in 10..300");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    M->ml_omega = value / 100.0f;
   } else if (n == "ml_infer") {
     M3_TRY(ml_set_infer(value));
   } else if (n == "stream_f32_variant") {
