@@ -344,6 +344,27 @@ class CoarseChol:
         return sla.cho_solve(self.c, r)
 
 
+class ThreadedCSR:
+    """y = A @ x with the rows of a CSR matrix split into one block per thread. The reference's own
+    product (mgpcg_solver_p.m:728-733, MUTILS spmv) runs on several threads the same way; each row
+    is still summed in the same order, so the result is bit-identical to ``A @ x``."""
+
+    def __init__(self, A, pool, nthreads):
+        A = A.tocsr()
+        self.shape = A.shape
+        self.bounds = np.linspace(0, A.shape[0], nthreads + 1).astype(np.int64)
+        self.blocks = [A[self.bounds[i]:self.bounds[i + 1]] for i in range(nthreads)]
+        self.pool = pool
+
+    def __matmul__(self, x):
+        y = np.empty(self.shape[0], dtype=np.result_type(self.blocks[0].dtype, x.dtype))
+
+        def one(i):
+            y[self.bounds[i]:self.bounds[i + 1]] = self.blocks[i] @ x
+        list(self.pool.map(one, range(len(self.blocks))))
+        return y
+
+
 class MGPCG:
     """mgpcg_solver_p (flexible Polak-Ribiere PCG, V-cycle v2, Jacobi weights 'Setup 3')."""
 
@@ -357,6 +378,16 @@ class MGPCG:
         self.wd = [[0.9, 0.4, 0.25]] + [[0.25, 0.4, 0.9]] * (self.nmesh - 2)
         self.wu = [[0.25, 0.4, 0.9]] + [[0.9, 0.4, 0.25]] * (self.nmesh - 2)
         self.napply = 0
+        self.PT = [None] * len(Ic2f)
+
+    def use_threads(self, nthreads):
+        """Run the sparse products on `nthreads` host threads (the CPU baseline's timing mode)."""
+        from concurrent.futures import ThreadPoolExecutor
+        pool = ThreadPoolExecutor(nthreads)
+        self.K1 = ThreadedCSR(self.K1, pool, nthreads)
+        self.KK = [self.KK[0]] + [ThreadedCSR(K, pool, nthreads) for K in self.KK[1:]]
+        self.PT = [ThreadedCSR(P.T, pool, nthreads) for P in self.P]
+        self.P = [ThreadedCSR(P, pool, nthreads) for P in self.P]
 
     def _K(self, j, x):
         self.napply += 1
@@ -373,7 +404,7 @@ class MGPCG:
                 d1 = d1 + w * r1 * self.KDi[j]
                 r1 = r0 - self._K(j, d1)
             dd.append(d1)
-            r0 = self.P[j].T @ r1
+            r0 = (self.P[j].T if self.PT[j] is None else self.PT[j]) @ r1
         d = self.coarse.solve(r0)
         for j in range(self.nmesh - 2, -1, -1):
             d = dd[j] + self.P[j] @ d

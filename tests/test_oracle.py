@@ -63,3 +63,19 @@ def test_transfer_matches_host_setup(tiny):
     dense = np.zeros_like(Ic2f)
     np.add.at(dense, (np.repeat(np.arange(len(cols)), 10), cols.ravel()), W.ravel())
     assert np.abs(dense - Ic2f).max() < 1e-12
+
+
+def test_threaded_sparse_products_match_serial(tiny):
+    """The CPU baseline's threaded mode: row-block products equal the serial CSR product bit for
+    bit, and MG-PCG iterates agree with the serial solver to rounding."""
+    w = tiny
+    s1 = O.StokesSystem(w['levels'], w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'])
+    s4 = O.StokesSystem(w['levels'], w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'])
+    s4.mg.use_threads(4)
+    x = np.random.default_rng(3).standard_normal(s1.mg.K1.shape[0])
+    assert np.array_equal(s4.mg.K1 @ x, s1.mg.K1 @ x)
+    b = np.random.default_rng(4).standard_normal(len(s1.ifree))
+    x1, it1, _ = s1.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
+    x4, it4, _ = s4.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
+    assert it1 == it4
+    assert np.linalg.norm(x4 - x1) <= 1e-12 * np.linalg.norm(x1)
