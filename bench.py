@@ -405,7 +405,20 @@ def cpu_baseline(w, gpu_info, args):
         t_el = (time.perf_counter() - t) / S
     c1 = workloads.make_workload("c1", seed=args.seed)
     sysm = O.StokesSystem(c1["levels"], c1["visc"], c1["dens"], c1["ifix"], c1["vfix"], c1["phys"])
-    sysm.mg.use_threads(nth)
+    # sparse products on threads only where that makes an MG-PCG iteration faster on this host (it
+    # depends on whether the installed scipy releases the GIL in its CSR product, and on other
+    # threads competing for the cores): time two iterations both ways
+    nth_mg, t_ser, t_thr = 1, None, None
+    if nth > 1:
+        bt = np.random.default_rng(1).standard_normal(len(sysm.ifree))
+        its = lambda: sysm.mg.solve(bt, np.zeros_like(bt), rtol=1e-30, itmax=2)
+        t_ser = best_time(its, reps=2)
+        sysm.mg.use_threads(nth)
+        t_thr = best_time(its, reps=2)
+        if t_thr < 0.95 * t_ser:
+            nth_mg = nth
+        else:
+            sysm.mg.use_serial()
     rng = np.random.default_rng(0)
     b = rng.standard_normal(len(sysm.ifree))
     t = time.perf_counter()
@@ -418,7 +431,25 @@ def cpu_baseline(w, gpu_info, args):
     return {"value": est, "unit": "s", "cores": nth, "kind": "port",
             "sample": f"oracle element matrices of {S} of {nel} elements of this mesh ({t_el * 1e3:.3f} ms/el) + "
                       f"{it} MG-PCG iterations on the 130,662-DOF shell ({t_it:.2f} s/it; sparse products on "
-                      f"{nth} threads) scaled by DOF x {iters} iterations of the plain-FP64 solve"}
+                      f"{nth_mg} thread(s){thr_note(t_ser, t_thr, nth)}) scaled by DOF x {iters} iterations of "
+                      f"the plain-FP64 solve"}
+
+
+def best_time(f, reps=5):
+    """Shortest of `reps` timed calls of f (after one untimed call)."""
+    f()
+    best = float("inf")
+    for _ in range(reps):
+        t = time.perf_counter()
+        f()
+        best = min(best, time.perf_counter() - t)
+    return best
+
+
+def thr_note(t_ser, t_thr, nth):
+    if t_ser is None:
+        return ""
+    return f"; two iterations {t_ser:.2f} s on 1 thread, {t_thr:.2f} s on {nth}"
 
 
 def host_threads():

@@ -384,10 +384,18 @@ class MGPCG:
         """Run the sparse products on `nthreads` host threads (the CPU baseline's timing mode)."""
         from concurrent.futures import ThreadPoolExecutor
         pool = ThreadPoolExecutor(nthreads)
+        if not hasattr(self, "_serial"):
+            self._serial = (self.K1, list(self.KK), list(self.P), list(self.PT))
         self.K1 = ThreadedCSR(self.K1, pool, nthreads)
         self.KK = [self.KK[0]] + [ThreadedCSR(K, pool, nthreads) for K in self.KK[1:]]
         self.PT = [ThreadedCSR(P.T, pool, nthreads) for P in self.P]
         self.P = [ThreadedCSR(P, pool, nthreads) for P in self.P]
+
+    def use_serial(self):
+        """Back to the serial products after use_threads."""
+        if hasattr(self, "_serial"):
+            self.K1, self.KK, self.P, self.PT = self._serial[0], list(self._serial[1]), list(self._serial[2]), \
+                list(self._serial[3])
 
     def _K(self, j, x):
         self.napply += 1
