@@ -110,6 +110,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def clock_csv_path():
+    """A private temporary file for the nvidia-smi samples (M3SPH_CLOCKS_CSV overrides it)."""
+    import tempfile
+    p = os.environ.get("M3SPH_CLOCKS_CSV")
+    if p:
+        return p
+    fd, p = tempfile.mkstemp(prefix="m3sph_clocks_", suffix=".csv")
+    os.close(fd)
+    return p
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -202,8 +213,7 @@ def run_gb300(args, rank, ws, td):
         lj = infos_j[-1]
         jac = {"s_per_solve": allmax(td, ms_j) / 1e3, "nitU": lj["nitU"], "nitZ": lj["nitZ"], "itPat": lj["itPat"],
                "rel_residual": lj["rel_residual"]}
-    clk = ClockSampler(str(ROOT / "gpurun_out" / "clocks_bench.csv") if (ROOT / "gpurun_out").is_dir()
-                       else "/tmp/m3sph_clocks.csv")
+    clk = ClockSampler(clock_csv_path())
     ms, infos, launches = timed(sm, args.warmup, args.steps, clk)
     accuracy = None
     if plain is not None:

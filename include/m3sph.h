@@ -70,10 +70,13 @@ typedef struct m3sph_slm_opts {
   double r_cmb, r_surf;   /* MESH.r_cmb, MESH.r_surf */
 } m3sph_slm_opts;
 
-/* Point-location counters: points placed by the walk, points on shared faces resolved by the
- * tie rule, points in frame gaps placed with a grown tolerance, brute-force placements, lost. */
+/* Point-location counters: points placed by the walk, points that several elements contain
+ * (within 1e-10 in barycentric coordinates) resolved by the tie rule, points in frame gaps placed
+ * with a grown tolerance, brute-force placements, lost points, and the ties that the reference
+ * rejects with error('no good') (tsearch2_sph.m:387-392: cross-frame, no isoparametric element, not
+ * at a shared vertex), which are resolved by the largest id. */
 typedef struct m3sph_locate_info {
-  int32_t npt, nwalk, nties, ngap, nbrute, nlost;
+  int32_t npt, nwalk, nties, ngap, nbrute, nlost, nambig;
 } m3sph_locate_info;
 
 /* Physical parameters used by the element operator (PHYSICS, NUMSCALE fields). */
@@ -142,8 +145,65 @@ M3SPH_API int m3sph_stokes_solve(m3sph_mesh *mesh, double *U_xyz, double *P, con
 M3SPH_API int m3sph_stokes_step_device(m3sph_mesh *mesh, const m3sph_opts *opts, m3sph_info *info);
 /* Copy the device-resident solution of the last solve: U_xyz (3*nnod) and P (nvnod). */
 M3SPH_API int m3sph_solution(m3sph_mesh *mesh, double *U_xyz, double *P);
+/* Replaces calculate_dt (calculate_dt.m:40-52) on the device-resident velocity of the last solve
+ * (the VAR.Ux/Uy/Uz that flow3d_patera_sph returns): a device max-reduction of |Ux|, |Uy|, |Uz|,
+ * then dt_adv = dt_adv_limit * min(Lx/max|Ux|, Ly/max|Uy|, Lz/max|Uz|) with MESH.Lx/Ly/Lz the extents
+ * of the finest mesh (init_mesh_curved_p.m:264-272), dt = min(dtmax, dt_adv); a zero velocity gives
+ * dt = dtmax and dt_adv = 0. dt_adv may be NULL. */
+M3SPH_API int m3sph_calculate_dt(m3sph_mesh *mesh, double dt_adv_limit, double dtmax, double *dt, double *dt_adv);
 /* The CUDA stream (cudaStream_t) the handle launches its kernels on. */
 M3SPH_API int m3sph_stream(m3sph_mesh *mesh, void **stream);
+
+/* Rock properties of rock_prop (rock_prop.m:5-66). A cut-off that is NaN is not applied. */
+typedef struct m3sph_rock_params {
+  double Visc0;      /* PHYSICS.Visc: reference viscosity */
+  double Dens0;      /* PHYSICS.Dens: reference density */
+  double T_ref;      /* PHYSICS.T_ref (degC) */
+  double alpha;      /* PHYSICS.alpha: thermal expansivity */
+  double Ea;         /* PHYSICS.Ea (J/mol; 0: no Arrhenius factor; 0 < Ea < 1000 is rejected as kJ/mol) */
+  double Va;         /* PHYSICS.Va (m^3/mol; 0: no pressure factor) */
+  double g;          /* PHYSICS.g */
+  double L0;         /* NUMSCALE.L0: metres per mesh length unit */
+  double a_UM2LM;    /* PHYSICS.a_UM2LM: cap of the pressure factor (<= 0: none) */
+  double minDens, maxDens, minVisc, maxVisc;
+} m3sph_rock_params;
+
+/* Replaces rock_prop (rock_prop.m:5-66): nodal Visc and Dens (nnod each) from T (nnod):
+ * Dens = Dens0 (1 - alpha (T - T_ref)); Arrhenius factor exp(Ea/(R T0) (T0/T - 1)) in Kelvin,
+ * clamped to [1e-8, 1e8]; pressure factor exp(|g Dens0 L0 depth| Va / (R T0)) with depth below the
+ * outermost node; Visc = Visc0 times the smaller of (Arrhenius x pressure, Arrhenius x a_UM2LM). */
+M3SPH_API int m3sph_rock_prop(m3sph_mesh *mesh, const m3sph_rock_params *p, const double *T, double *Visc,
+                              double *Dens);
+
+/* One time step of the reference's loop (M3TET_SPH_SOUTH_ATLANTIC_PLUME.m:213-296) on device-
+ * resident fields: rock_prop (optional) -> flow3d_patera_sph (operator rebuild from the resident
+ * viscosity/density and the boundary conditions of the last m3sph_stokes_setup, Patera solve
+ * warm-started from the previous step's pressure) -> calculate_dt -> advect3d_slm_p_sph of the
+ * resident temperature in the new velocity (search guesses carried between steps as WS_SLM).
+ * No counterpart call in the reference, whose loop calls the functions one by one from MATLAB. */
+typedef struct m3sph_step_opts {
+  m3sph_opts stokes;          /* solver options (precision must match the set-up's) */
+  m3sph_slm_opts slm;         /* advection options */
+  int32_t rock_prop;          /* 1: Visc, Dens from the resident T by rock_prop before the solve */
+  m3sph_rock_params rock;
+  double dt_adv_limit;        /* SETTINGS.dt_adv_limit (calculate_dt.m) */
+  double dtmax;               /* SETTINGS.dtmax */
+} m3sph_step_opts;
+
+typedef struct m3sph_step_info {
+  m3sph_info stokes;          /* the Patera solve of this step */
+  m3sph_locate_info locate;   /* point location of the advection */
+  double dt, dt_adv;          /* calculate_dt outputs */
+  double time;                /* model time after the step */
+  double t_rock_ms, t_stokes_ms, t_dt_ms, t_advect_ms, t_total_ms;
+  int32_t status;
+} m3sph_step_info;
+
+/* Upload the temperature T (nnod) that the time steps advect (and restart the step counter, the
+ * model time and the advection search guesses); read it back. */
+M3SPH_API int m3sph_set_temperature(m3sph_mesh *mesh, const double *T, double time);
+M3SPH_API int m3sph_get_temperature(m3sph_mesh *mesh, double *T);
+M3SPH_API int m3sph_time_step(m3sph_mesh *mesh, const m3sph_step_opts *opts, m3sph_step_info *info);
 
 /* Learned element smoother (no counterpart in the reference: M3TET_SPH smooths with weighted
  * Jacobi only). A 52-128-30 MLP (BF16 tensor cores, FP32 accumulation) replaces Jacobi sweeps on
@@ -210,9 +270,10 @@ M3SPH_API int m3sph_interp3d_cubic(m3sph_mesh *mesh, const int32_t *els, const d
  * work runs on the handle's stream (m3sph_stream), which is synchronised before returning.
  * Scratch lives in one fixed 8 MiB array per device that every call shares (7 values per element
  * + 4 per vertex, about 120k elements of a spherical-shell mesh; larger meshes are rejected with
- * M3SPH_ERR_BAD_INPUT). The first call on a device looks up the array's address, so make that
- * first call before any stream capture. Calls that overlap on the GPU (two handles on two
- * threads) race on the shared scratch. It calls no cudaMalloc / cudaFree. */
+ * M3SPH_ERR_BAD_INPUT). The array's device address is looked up, and this entry point's kernels
+ * are loaded, when the mesh handle is created (m3sph_mesh_create), so under CUDA's lazy module
+ * loading the array is committed at start-up and not inside a call. Calls that overlap on the GPU
+ * (two handles on two threads) race on the shared scratch. It calls no cudaMalloc / cudaFree. */
 M3SPH_API int m3sph_interp3d_cubic_noalloc(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
                                            const double *V, int32_t monotonic, int32_t method_wght, double *Vi);
 /* Replaces advect3d_slm_p_sph (advect3d_slm_p_sph.m:1-139): Ux,Uy,Uz Cartesian nodal velocity,

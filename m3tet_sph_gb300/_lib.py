@@ -37,7 +37,7 @@ class SlmOpts(C.Structure):
 
 class LocateInfo(C.Structure):
     _fields_ = [("npt", C.c_int32), ("nwalk", C.c_int32), ("nties", C.c_int32), ("ngap", C.c_int32),
-                ("nbrute", C.c_int32), ("nlost", C.c_int32)]
+                ("nbrute", C.c_int32), ("nlost", C.c_int32), ("nambig", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -61,6 +61,29 @@ class Info(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RockParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("Visc0", "Dens0", "T_ref", "alpha", "Ea", "Va", "g", "L0", "a_UM2LM",
+                                          "minDens", "maxDens", "minVisc", "maxVisc")]
+
+
+class StepOpts(C.Structure):
+    _fields_ = [("stokes", Opts), ("slm", SlmOpts), ("rock_prop", C.c_int32), ("rock", RockParams),
+                ("dt_adv_limit", C.c_double), ("dtmax", C.c_double)]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [("stokes", Info), ("locate", LocateInfo), ("dt", C.c_double), ("dt_adv", C.c_double),
+                ("time", C.c_double), ("t_rock_ms", C.c_double), ("t_stokes_ms", C.c_double),
+                ("t_dt_ms", C.c_double), ("t_advect_ms", C.c_double), ("t_total_ms", C.c_double),
+                ("status", C.c_int32)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["stokes"] = self.stokes.as_dict()
+        d["locate"] = self.locate.as_dict()
+        return d
 
 
 # exported symbols and their argtypes (None = opaque handle pointer)
@@ -88,6 +111,11 @@ SIGNATURES = {
     "m3sph_vcycle": ([P, DP, DP], C.c_int),
     "m3sph_stokes_step_device": ([P, C.POINTER(Opts), C.POINTER(Info)], C.c_int),
     "m3sph_solution": ([P, DP, DP], C.c_int),
+    "m3sph_calculate_dt": ([P, C.c_double, C.c_double, DP, DP], C.c_int),
+    "m3sph_rock_prop": ([P, C.POINTER(RockParams), DP, DP, DP], C.c_int),
+    "m3sph_set_temperature": ([P, DP, C.c_double], C.c_int),
+    "m3sph_get_temperature": ([P, DP], C.c_int),
+    "m3sph_time_step": ([P, C.POINTER(StepOpts), C.POINTER(StepInfo)], C.c_int),
     "m3sph_stream": ([P, C.POINTER(P)], C.c_int),
     "m3sph_tsearch_sph": ([P, DP, C.c_int32, IP, IP, DP, C.POINTER(LocateInfo)], C.c_int),
     "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),

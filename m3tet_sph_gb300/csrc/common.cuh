@@ -177,6 +177,11 @@ struct SetupArgs {
 };
 
 int slm_build(m3sph_mesh *M, const m3sph_level &f0);
+int slm_advect_resident(m3sph_mesh *M, const double *U_soa, double *T, double dt, const m3sph_slm_opts *o,
+                        bool first_step, m3sph_locate_info *info);
+int stokes_velocity_soa(m3sph_mesh *M, double *dst);
+int stokes_resident_solve(m3sph_mesh *M, const m3sph_opts *opts, bool zero_p, m3sph_info &inf);
+int stokes_calc_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv);
 int ml_build(m3sph_mesh *M);
 int ml_features(m3sph_mesh *M, const double *h_visc);
 template <typename T> int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *tmp, T *d);
@@ -230,6 +235,12 @@ struct m3sph_mesh {
   bool smoother_active = false;       // learned smoother in use for the current solve
   int smoother_fallbacks = 0;
   double r_min = 0.0, r_max = 0.0;    // shell radii (features)
+  double Lx = 0.0, Ly = 0.0, Lz = 0.0; // extents of the finest mesh (MESH.Lx/Ly/Lz, init_mesh_curved_p.m:264-272)
+  double rad_max = 0.0;               // largest node radius sqrt(x^2+y^2+z^2) (rock_prop.m:10-11)
+  double *T = nullptr;                // [nnod] resident temperature of the time step
+  double *Usoa = nullptr;             // [3][nnod] Cartesian velocity handed to the advection
+  long long ts_steps = 0;             // time steps taken since the temperature was set
+  double ts_time = 0.0;               // model time accumulated by the time steps
   void *slm = nullptr;                // advection / point-location state
   void (*slm_free)(void *) = nullptr;
   double *red = nullptr;              // reduction partials

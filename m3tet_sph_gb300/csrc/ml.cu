@@ -854,15 +854,63 @@ int ml_build(m3sph_mesh *M) {
 }
 
 // recompute the per-element features from the current viscosity (called by the operator set-up)
+// sums of log(visc) and log(visc)^2 in a fixed order: per-block partial sums, then one block
+constexpr int LOGSTAT_BLOCKS = 512;
+__global__ void k_logstats_partial(const double *v, int n, double *part) {
+  __shared__ double s1[256], s2[256];
+  double a = 0.0, b = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double l = log(v[i]);
+    a += l;
+    b += l * l;
+  }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s1[0];
+    part[2 * blockIdx.x + 1] = s2[0];
+  }
+}
+__global__ void k_logstats_final(const double *part, int nb, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k < nb; ++k) {
+    a += part[2 * k];
+    b += part[2 * k + 1];
+  }
+  out[0] = a;
+  out[1] = b;
+}
+
+// features of the learned smoother; h_visc (nnod, host) or nullptr: the statistics of log(visc)
+// are then reduced on the device from the resident viscosity
 int ml_features(m3sph_mesh *M, const double *h_visc) {
   MlState *S = mls(M);
   if (!S) return M3SPH_OK;
   Level &L0 = M->lev[0];
   double mu = 0.0, m2 = 0.0, rmin = 1e300, rmax = 0.0;
-  for (int n = 0; n < L0.nnod; ++n) {
-    const double l = std::log(h_visc[n]);
-    mu += l;
-    m2 += l * l;
+  if (h_visc) {
+    for (int n = 0; n < L0.nnod; ++n) {
+      const double l = std::log(h_visc[n]);
+      mu += l;
+      m2 += l * l;
+    }
+  } else {
+    // M->red holds 4096 doubles of reduction partials; scal[16..17] the two sums
+    k_logstats_partial<<<LOGSTAT_BLOCKS, 256, 0, M->stream>>>(M->fin.visc, L0.nnod, M->red); count_launch();
+    k_logstats_final<<<1, 32, 0, M->stream>>>(M->red, LOGSTAT_BLOCKS, M->scal + 16); count_launch();
+    M3_CUDA(cudaMemcpyAsync(M->h_scal + 16, M->scal + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, M->stream));
+    M3_CUDA(cudaStreamSynchronize(M->stream));
+    mu = M->h_scal[16];
+    m2 = M->h_scal[17];
   }
   mu /= L0.nnod;
   const double sig = std::sqrt(std::max(m2 / L0.nnod - mu * mu, 1e-12)) + 1e-3;

@@ -22,7 +22,22 @@ namespace m3sph {
 
 constexpr int WALK_MAX_STEPS = 512;
 constexpr float WALK32_MARGIN = 1e-4f;   // FP32 barycentric margin before the FP64 walk takes over
-constexpr double TIE_EPS = 1e-10;
+// Point-location rule (the oracle states the same rule):
+//  1. C = {e : need(e) <= TIE_BAND}, need = max(-min barycentric, max barycentric - 1) in the
+//     element's own frame. Non-empty C (tsearch2_sph.m:374-404): drop isoparametric elements if a
+//     non-isoparametric one is in C (:380-382); if the point is at a vertex of every remaining
+//     element keep those of the first frame in the reference's pass order (X-90, original, Z-180;
+//     :383-386); take the largest id (:404).
+//  2. Else tolerance in 1e-6 steps up to 15e-3 (locate_points_in_neighboring_element.m): among the
+//     elements of the smallest step count, the smallest last Newton step if all are isoparametric,
+//     else the smallest non-isoparametric id.
+constexpr double TIE_BAND = 1e-10;
+constexpr double TIE_TRIGGER = 1e-7;     // closer than this to the found element's boundary: resolve
+constexpr double IFACE_TRIGGER = 15e-3;  // the same for elements next to another frame or to iso elements
+constexpr double GAP_STEP = 1e-6;
+constexpr int GAP_QMAX = 15000;          // 15e-3 in 1e-6 steps
+constexpr int MAX_CAND = 64;             // candidates within the tie band kept per point
+constexpr int MAX_RING_VERTS = 96;       // vertices of the 1-ring gathered for the 2-ring search
 
 struct SlmMesh {
   int nel, nnod, nvnod;
@@ -34,6 +49,7 @@ struct SlmMesh {
   const double *SX;      // [3][nnod]  X-90 frame of all nodes
   const int *v2e_ptr;    // [nvnod+1]
   const int *v2e;        // vertex -> elements
+  const uint8_t *iface;  // [nel] 1 if an element sharing a vertex has another frame or iso-ness
   const float *S0f, *SZf, *SXf;   // FP32 copies of S0, SZ, SX (the FP32 part of the walk)
   // start grid for walks without a guess: cells equal in cos(theta), phi and r
   const int *grid;       // [gnr][gnt][gnp] element id
@@ -183,44 +199,129 @@ __device__ __forceinline__ void bary_minmax(const double *lc, double &mn, double
   }
 }
 
-// tie / gap resolution among elements sharing a vertex with e0
-__device__ int resolve_local(const SlmMesh &m, int e0, const PointFrames &f, double *lc_out, bool gap) {
-  int best = -1, best_iso = 1;
-  double best_need = 1e300;
-  double blc[3] = {0, 0, 0};
-  for (int i = 0; i < 4; ++i) {
-    const int v = m.el2nod[(size_t)i * m.nel + e0];
-    for (int k = m.v2e_ptr[v]; k < m.v2e_ptr[v + 1]; ++k) {
-      const int e = m.v2e[k];
-      double lc[3], mn, mx;
-      int am;
-      local_coords(m, e, f, lc);
-      bary_minmax(lc, mn, mx, am);
-      const double need = fmax(-mn, mx - 1.0);
-      // quantise the tolerance to the reference's 1e-6 steps when searching a gap
-      const double q = gap ? ceil(need / 1e-6 - 1e-9) : (need <= 0.0 ? 0.0 : 1e300);
-      const int iso = m.cls[e] == M3SPH_IN_CONE_ISO;
-      bool better = false;
-      if (q < best_need) better = true;
-      else if (q == best_need) {
-        if (iso < best_iso) better = true;
-        else if (iso == best_iso && e > best) better = true;
-      }
-      if (better) {
-        best = e; best_need = q; best_iso = iso;
-        blc[0] = lc[0]; blc[1] = lc[1]; blc[2] = lc[2];
-      }
-    }
+// frame of each class in the reference's pass order: X-90 (cone classes) 0, original 1, Z-180 2
+__device__ __forceinline__ int frame_rank(int cls) { return cls >= M3SPH_IN_CONE_NO_ISO ? 0 : (cls == 0 ? 1 : 2); }
+
+// candidate flags: bit 0 isoparametric, bits 1-2 frame rank, bit 3 point at one of its vertices
+struct CandList {
+  int n = 0, overflow = 0;
+  int id[MAX_CAND];
+  uint8_t fl[MAX_CAND];
+  __device__ void add(int e, uint8_t f) {
+    for (int k = 0; k < n; ++k)
+      if (id[k] == e) return;
+    if (n < MAX_CAND) { id[n] = e; fl[n] = f; ++n; } else overflow = 1;
   }
-  if (best >= 0 && (!gap || best_need * 1e-6 <= 15e-3 + 1e-6) && (gap || best_need == 0.0)) {
-    lc_out[0] = blc[0]; lc_out[1] = blc[1]; lc_out[2] = blc[2];
-    return best;
+};
+
+// rule 1 over n candidates; *ambiguous: neither the iso drop nor the shared-vertex drop applied and
+// the remaining candidates span frames (the reference's error('no good'), tsearch2_sph.m:387-392)
+__device__ int tie_rule(const int *id, const uint8_t *fl, int n, int *ambiguous) {
+  bool any_iso = false, any_non = false;
+  for (int k = 0; k < n; ++k) {
+    if (fl[k] & 1) any_iso = true; else any_non = true;
   }
-  return -1;
+  const bool drop_iso = any_iso && any_non;
+  bool all_vtx = true;
+  int rmin = 3, rmax = -1;
+  for (int k = 0; k < n; ++k) {
+    if (drop_iso && (fl[k] & 1)) continue;
+    if (!(fl[k] & 8)) all_vtx = false;
+    const int r = (fl[k] >> 1) & 3;
+    rmin = min(rmin, r);
+    rmax = max(rmax, r);
+  }
+  const bool vtx_drop = all_vtx && n >= 2;
+  int best = -1;
+  for (int k = 0; k < n; ++k) {
+    if (drop_iso && (fl[k] & 1)) continue;
+    if (vtx_drop && ((fl[k] >> 1) & 3) != rmin) continue;
+    best = max(best, id[k]);
+  }
+  *ambiguous = (n >= 2 && !drop_iso && !all_vtx && rmax > rmin) ? 1 : 0;
+  return best;
 }
 
-// one thread per point: walk from the guess to the containing element.
-// status bits: 1 = found by walk, 2 = tie resolved locally, 4 = gap (tolerance), 8 = not found
+// smallest quantised tolerance and, at that tolerance, the best isoparametric (smallest Newton
+// step, then smallest id) and non-isoparametric (smallest id) elements
+struct GapBest {
+  int q = GAP_QMAX + 1, non = -1, iso = -1;
+  double iso_step = 1e300;
+  __device__ void add(int e, int qe, bool is_iso, double step) {
+    if (qe > GAP_QMAX) return;
+    if (qe < q) { q = qe; non = -1; iso = -1; iso_step = 1e300; }
+    if (qe != q) return;
+    if (!is_iso) {
+      if (non < 0 || e < non) non = e;
+    } else if (step < iso_step || (step == iso_step && e < iso)) {
+      iso = e;
+      iso_step = step;
+    }
+  }
+  __device__ int pick() const { return non >= 0 ? non : iso; }
+};
+
+__device__ __forceinline__ void eval_candidate(const SlmMesh &m, int e, const PointFrames &f, CandList &C, GapBest &G) {
+  double lc[3], mn, mx;
+  int am;
+  const double step = local_coords(m, e, f, lc);
+  bary_minmax(lc, mn, mx, am);
+  const double need = fmax(-mn, mx - 1.0);
+  const int cls = m.cls[e];
+  const bool iso = cls == M3SPH_IN_CONE_ISO;
+  if (need <= TIE_BAND) {
+    C.add(e, (uint8_t)((iso ? 1 : 0) | (frame_rank(cls) << 1) | (mx >= 1.0 - TIE_BAND ? 8 : 0)));
+  } else if (need <= (GAP_QMAX + 1) * GAP_STEP) {
+    G.add(e, (int)ceil(need / GAP_STEP - 1e-9), iso, step);
+  }
+}
+
+// Apply the rule over the elements sharing a vertex with e0 (depth 1) or with any of those
+// (depth 2, for points the walk could not place). Returns the element (or -1) and sets kind bits:
+// 2 tie, 4 gap, 32 ambiguous for the reference, 64 candidate list overflow.
+__device__ __noinline__ int resolve_ring(const SlmMesh &m, int e0, int depth, const PointFrames &f, double *lc_out, int &kind) {
+  CandList C;
+  GapBest G;
+  if (depth == 1) {
+    for (int i = 0; i < 4; ++i) {
+      const int v = m.el2nod[(size_t)i * m.nel + e0];
+      for (int k = m.v2e_ptr[v]; k < m.v2e_ptr[v + 1]; ++k) eval_candidate(m, m.v2e[k], f, C, G);
+    }
+  } else {
+    int verts[MAX_RING_VERTS];
+    int nv = 0;
+    for (int i = 0; i < 4; ++i) {
+      const int v = m.el2nod[(size_t)i * m.nel + e0];
+      for (int k = m.v2e_ptr[v]; k < m.v2e_ptr[v + 1]; ++k) {
+        const int e1 = m.v2e[k];
+        for (int j = 0; j < 4; ++j) {
+          const int w = m.el2nod[(size_t)j * m.nel + e1];
+          bool seen = false;
+          for (int a = 0; a < nv; ++a) seen |= verts[a] == w;
+          if (!seen && nv < MAX_RING_VERTS) verts[nv++] = w;
+        }
+      }
+    }
+    for (int a = 0; a < nv; ++a)
+      for (int k = m.v2e_ptr[verts[a]]; k < m.v2e_ptr[verts[a] + 1]; ++k) eval_candidate(m, m.v2e[k], f, C, G);
+  }
+  int e = -1;
+  kind = C.overflow ? 64 : 0;
+  if (C.n > 0) {
+    int amb = 0;
+    e = tie_rule(C.id, C.fl, C.n, &amb);
+    kind |= (C.n >= 2 ? 2 : 0) | (amb ? 32 : 0);
+  } else {
+    e = G.pick();
+    if (e >= 0) kind |= 4;
+  }
+  if (e >= 0) local_coords(m, e, f, lc_out);
+  return e;
+}
+
+// one thread per point: walk from the guess to the containing element, then the rule above.
+// status bits: 1 placed, 2 tie, 4 gap (tolerance), 8 not placed yet (brute force next), 16 placed by
+// brute force, 32 ambiguous for the reference, 64 candidate list overflow
 __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const int *__restrict__ guess,
                          const int *__restrict__ node_guess, int *__restrict__ els, double *__restrict__ lc_out,
                          uint8_t *__restrict__ status, int adjust) {
@@ -303,20 +404,20 @@ __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const
     double mn, mx;
     int am;
     bary_minmax(lc, mn, mx, am);
-    if (mn < TIE_EPS || mx > 1.0 - TIE_EPS) {
-      const int r = resolve_local(m, found, f, lc, false);
-      if (r >= 0) {
-        found = r;
-        st |= 2;
-      }
+    if (mn < TIE_TRIGGER || mx > 1.0 - TIE_TRIGGER || (m.iface[found] && mn < IFACE_TRIGGER)) {
+      int kind = 0;
+      const int r = resolve_ring(m, found, 1, f, lc, kind);
+      if (r >= 0) found = r;
+      st |= kind;
     }
   } else {
-    const int r = resolve_local(m, e, f, lc, true);
+    int kind = 0;
+    const int r = resolve_ring(m, e, 2, f, lc, kind);
     if (r >= 0) {
       found = r;
-      st = 4;
+      st = (kind & 4) ? kind : (1 | kind);
     } else {
-      st = 8;
+      st = 8 | kind;
     }
   }
   if (adjust && found >= 0) {   // adjust_local_coords (locate_points_interp_vars_3d_sph.m:180-198)
@@ -331,42 +432,83 @@ __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const
   status[i] = st;
 }
 
-// brute force over all elements for points the walk could not place (status 8)
-__global__ void k_locate_brute(SlmMesh m, const double *__restrict__ P, int npt, const int *__restrict__ todo,
-                               int ntodo, int *__restrict__ els, double *__restrict__ lc_out, uint8_t *status) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// brute force over all elements for points the walk could not place (status 8): one warp per point,
+// the same rule over every element. Candidates within the tie band go to a per-warp list in shared
+// memory (the rule does not depend on their order); the gap choice is reduced across the warp.
+constexpr int BRUTE_WARPS = 8;
+__global__ void __launch_bounds__(BRUTE_WARPS * 32) k_locate_brute(SlmMesh m, const double *__restrict__ P, int npt,
+                                                                  const int *__restrict__ todo, int ntodo,
+                                                                  int *__restrict__ els, double *__restrict__ lc_out,
+                                                                  uint8_t *status, int adjust) {
+  __shared__ int s_id[BRUTE_WARPS][MAX_CAND];
+  __shared__ uint8_t s_fl[BRUTE_WARPS][MAX_CAND];
+  __shared__ int s_n[BRUTE_WARPS];
+  const int wl = threadIdx.x >> 5;
+  const int w = blockIdx.x * BRUTE_WARPS + wl;
   const int lane = threadIdx.x & 31;
+  if (lane == 0) s_n[wl] = 0;
+  __syncwarp();
   if (w >= ntodo) return;
   const int i = todo[w];
   PointFrames f;
   point_frames(P[i], P[npt + i], P[2 * npt + i], f);
-  double best_need = 1e300;
-  int best = -1;
+  GapBest G;
   for (int e = lane; e < m.nel; e += 32) {
     double lc[3], mn, mx;
     int am;
-    local_coords(m, e, f, lc);
+    const double step = local_coords(m, e, f, lc);
     bary_minmax(lc, mn, mx, am);
-    const double need = fmax(fmax(-mn, mx - 1.0), 0.0);
-    if (need < best_need || (need == best_need && e > best)) { best_need = need; best = e; }
+    const double need = fmax(-mn, mx - 1.0);
+    const int cls = m.cls[e];
+    const bool iso = cls == M3SPH_IN_CONE_ISO;
+    if (need <= TIE_BAND) {
+      const int slot = atomicAdd(&s_n[wl], 1);
+      if (slot < MAX_CAND) {
+        s_id[wl][slot] = e;
+        s_fl[wl][slot] = (uint8_t)((iso ? 1 : 0) | (frame_rank(cls) << 1) | (mx >= 1.0 - TIE_BAND ? 8 : 0));
+      }
+    } else if (need <= (GAP_QMAX + 1) * GAP_STEP) {
+      G.add(e, (int)ceil(need / GAP_STEP - 1e-9), iso, step);
+    }
   }
+  __syncwarp();
+  // warp reduction of the gap choice: smallest q, then the per-kind bests at that q
+  int q = G.q;
+  for (int o = 16; o > 0; o >>= 1) q = min(q, __shfl_xor_sync(0xffffffffu, q, o));
+  int non = (G.q == q) ? G.non : -1;
+  int iso_e = (G.q == q) ? G.iso : -1;
+  double iso_s = (G.q == q) ? G.iso_step : 1e300;
   for (int o = 16; o > 0; o >>= 1) {
-    const double on = __shfl_xor_sync(0xffffffffu, best_need, o);
-    const int oe = __shfl_xor_sync(0xffffffffu, best, o);
-    if (on < best_need || (on == best_need && oe > best)) { best_need = on; best = oe; }
+    const int on = __shfl_xor_sync(0xffffffffu, non, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, iso_e, o);
+    const double os = __shfl_xor_sync(0xffffffffu, iso_s, o);
+    if (on >= 0 && (non < 0 || on < non)) non = on;
+    if (oi >= 0 && (iso_e < 0 || os < iso_s || (os == iso_s && oi < iso_e))) { iso_e = oi; iso_s = os; }
   }
-  if (lane == 0 && best >= 0 && best_need <= 15e-3) {
-    double lc[3];
-    local_coords(m, best, f, lc);
+  if (lane != 0) return;
+  const int nc = s_n[wl];
+  int e = -1, kind = nc > MAX_CAND ? 64 : 0;
+  if (nc > 0) {
+    int amb = 0;
+    e = tie_rule(s_id[wl], s_fl[wl], min(nc, MAX_CAND), &amb);
+    kind |= (nc >= 2 ? 2 : 0) | (amb ? 32 : 0);
+  } else if (q <= GAP_QMAX) {
+    e = non >= 0 ? non : iso_e;
+    kind |= 4;
+  }
+  if (e < 0) return;
+  double lc[3];
+  local_coords(m, e, f, lc);
+  if (adjust) {   // adjust_local_coords (locate_points_interp_vars_3d_sph.m:180-198)
     for (int k = 0; k < 3; ++k) lc[k] = fmin(fmax(lc[k], 0.0), 1.0);
-    const double s = lc[0] + lc[1] + lc[2];
-    if (s > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= s;
-    els[i] = best;
-    lc_out[i] = lc[0];
-    lc_out[npt + i] = lc[1];
-    lc_out[2 * npt + i] = lc[2];
-    status[i] = 16;
+    const double sm = lc[0] + lc[1] + lc[2];
+    if (sm > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= sm;
   }
+  els[i] = e;
+  lc_out[i] = lc[0];
+  lc_out[npt + i] = lc[1];
+  lc_out[2 * npt + i] = lc[2];
+  status[i] = (uint8_t)(16 | kind);
 }
 
 // P2 interpolation (interp3d_tet.m:39-69): V is [nvar][nnod], out [nvar][npt]
@@ -616,7 +758,7 @@ struct SlmState {
   bool built = false;
   int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr, *grid = nullptr;
   float *S0f = nullptr, *SZf = nullptr, *SXf = nullptr;
-  uint8_t *cls = nullptr;
+  uint8_t *cls = nullptr, *iface = nullptr;
   double *S0 = nullptr, *SZ = nullptr, *SX = nullptr;
   // work
   double *P = nullptr, *lc = nullptr, *V = nullptr, *out = nullptr, *upu = nullptr, *rpu = nullptr, *U = nullptr;
@@ -646,6 +788,8 @@ static int sl_upload(T **p, const T *h, size_t n, cudaStream_t s) {
   return M3SPH_OK;
 }
 
+static int noalloc_prepare(int device);
+
 // face neighbours, vertex->element adjacency, per-frame node coordinates (set-up, host + upload)
 int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
   SlmState *S = new SlmState();
@@ -658,7 +802,7 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
                     (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->Xc, (void *)S->kk, (void *)S->acc,
                     (void *)S->els, (void *)S->guess,
                     (void *)S->todo, (void *)S->status, (void *)S->grid, (void *)S->S0f, (void *)S->SZf,
-                    (void *)S->SXf})
+                    (void *)S->SXf, (void *)S->iface})
       if (q) cudaFree(q);
     delete S;
   };
@@ -767,23 +911,37 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
     grid.swap(g2);
   }
   std::vector<uint8_t> cls(f0.elclass, f0.elclass + nel);
+  // interface elements: some element sharing a vertex has another frame or another iso-ness (the
+  // own-frame shapes of such neighbours overlap or leave gaps)
+  std::vector<uint8_t> vmask(nv, 0), iface(nel, 0);
+  auto key = [&](int e) { const int c = cls[e]; return (c >= 2 ? 0 : (c == 0 ? 1 : 2)) * 2 + (c == 3 ? 1 : 0); };
+  for (int e = 0; e < nel; ++e)
+    for (int i = 0; i < 4; ++i) vmask[el[(size_t)e * 10 + i]] |= (uint8_t)(1u << key(e));
+  for (int e = 0; e < nel; ++e)
+    for (int i = 0; i < 4; ++i) {
+      const uint8_t mk = vmask[el[(size_t)e * 10 + i]];
+      if (mk & (mk - 1)) iface[e] = 1;
+    }
   int st;
   if ((st = sl_upload(&S->el2nod, soa.data(), soa.size(), s)) || (st = sl_upload(&S->nbr, nbr.data(), nbr.size(), s)) ||
       (st = sl_upload(&S->v2e_ptr, ptr.data(), ptr.size(), s)) || (st = sl_upload(&S->v2e, adj.data(), adj.size(), s)) ||
       (st = sl_upload(&S->node_guess, first.data(), first.size(), s)) ||
       (st = sl_upload(&S->cls, cls.data(), cls.size(), s)) || (st = sl_upload(&S->S0, S0.data(), S0.size(), s)) ||
       (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)) ||
-      (st = sl_upload(&S->grid, grid.data(), grid.size(), s)))
+      (st = sl_upload(&S->grid, grid.data(), grid.size(), s)) ||
+      (st = sl_upload(&S->iface, iface.data(), iface.size(), s)))
     return st;
   const std::vector<float> S0f(S0.begin(), S0.end()), SZf(SZ.begin(), SZ.end()), SXf(SX.begin(), SX.end());
   if ((st = sl_upload(&S->S0f, S0f.data(), S0f.size(), s)) || (st = sl_upload(&S->SZf, SZf.data(), SZf.size(), s)) ||
       (st = sl_upload(&S->SXf, SXf.data(), SXf.size(), s)))
     return st;
   M3_CUDA(cudaStreamSynchronize(s));
-  S->view = SlmMesh{nel, nnod, nv, S->el2nod, S->nbr, S->cls, S->S0, S->SZ, S->SX, S->v2e_ptr, S->v2e,
+  S->view = SlmMesh{nel, nnod, nv, S->el2nod, S->nbr, S->cls, S->S0, S->SZ, S->SX, S->v2e_ptr, S->v2e, S->iface,
                     S->S0f, S->SZf, S->SXf, S->grid, gnt, gnp, gnr, grmin, grmax};
   S->built = true;
-  return M3SPH_OK;
+  // the allocation-free interpolation's scratch address and kernels are resolved here, at handle
+  // creation, so that its calls never load code or commit memory later
+  return noalloc_prepare(M->device);
 }
 
 static int slm_reserve(SlmState *S, size_t npt, int nel, int nnod, int nv) {
@@ -823,18 +981,18 @@ static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool 
   M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
   std::vector<int> todo;
-  int nwalk = 0, ntie = 0, ngap = 0;
+  int nwalk = 0;
   for (int i = 0; i < npt; ++i) {
     if (hs[i] & 1) nwalk++;
-    if (hs[i] & 2) ntie++;
-    if (hs[i] & 4) ngap++;
     if (hs[i] & 8) todo.push_back(i);
   }
   int nbrute = 0, nlost = 0;
   if (!todo.empty()) {
     M3_CUDA(cudaMemcpyAsync(S->todo, todo.data(), sizeof(int) * todo.size(), cudaMemcpyHostToDevice, s));
     const int nt = (int)todo.size();
-    k_locate_brute<<<(nt * 32 + 255) / 256, 256, 0, s>>>(S->view, S->P, npt, S->todo, nt, S->els, S->lc, S->status); count_launch();
+    k_locate_brute<<<(nt + BRUTE_WARPS - 1) / BRUTE_WARPS, BRUTE_WARPS * 32, 0, s>>>(S->view, S->P, npt, S->todo, nt,
+                                                                                    S->els, S->lc, S->status,
+                                                                                    adjust ? 1 : 0); count_launch();
     M3_CUDA(cudaGetLastError());
     M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
     M3_CUDA(cudaStreamSynchronize(s));
@@ -843,6 +1001,13 @@ static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool 
       else nlost++;
     }
   }
+  int ntie = 0, ngap = 0, nambig = 0, noverflow = 0;
+  for (int i = 0; i < npt; ++i) {
+    if (hs[i] & 2) ntie++;
+    if (hs[i] & 4) ngap++;
+    if (hs[i] & 32) nambig++;
+    if (hs[i] & 64) noverflow++;
+  }
   if (info) {
     info->npt = npt;
     info->nwalk = nwalk;
@@ -850,6 +1015,12 @@ static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool 
     info->ngap = ngap;
     info->nbrute = nbrute;
     info->nlost = nlost;
+    info->nambig = nambig;
+  }
+  if (noverflow) {
+    set_error("point location: more than " + std::to_string(MAX_CAND) + " elements tie at " +
+              std::to_string(noverflow) + " points");
+    return M3SPH_ERR_BAD_INPUT;
   }
   if (nlost) {
     set_error("some nodes have not been located");
@@ -1023,12 +1194,14 @@ static int advect_device(m3sph_mesh *M, double dt, const m3sph_slm_opts *o, bool
     info->ngap = i1.ngap + i2.ngap;
     info->nbrute = i1.nbrute + i2.nbrute;
     info->nlost = i1.nlost + i2.nlost;
+    info->nambig = i1.nambig + i2.nambig;
   }
   return M3SPH_OK;
 }
 
 static void add_info(m3sph_locate_info &a, const m3sph_locate_info &b) {
   a.npt += b.npt; a.nwalk += b.nwalk; a.nties += b.nties; a.ngap += b.ngap; a.nbrute += b.nbrute; a.nlost += b.nlost;
+  a.nambig += b.nambig;
 }
 
 static int advect_device_rk4(m3sph_mesh *M, double dt, const m3sph_slm_opts *o, int nsub, bool use_ws,
@@ -1078,6 +1251,35 @@ static int advect_device_rk4(m3sph_mesh *M, double dt, const m3sph_slm_opts *o, 
   if (info) *info = tot;
   return M3SPH_OK;
 }
+
+namespace m3sph {
+// advect3d_slm_p_sph on device-resident data (the time step): U_soa [3][nnod] Cartesian nodal
+// velocity, T (nnod) advected in place. The search guesses carry over from the previous call of the
+// same handle (the reference's WS_SLM) unless first_step.
+int slm_advect_resident(m3sph_mesh *M, const double *U_soa, double *T, double dt, const m3sph_slm_opts *o,
+                        bool first_step, m3sph_locate_info *info) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (o->method_BT != 1 && o->method_BT != 2) {
+    set_error("method_BT must be 1 (PC2) or 2 (RK4, 3 substeps)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  const int n = L0.nnod;
+  if ((st = slm_reserve(S, n, L0.nel, n, L0.nvnod))) return st;
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(S->U, U_soa, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(S->V, T, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  if (o->method_BT == 2) {
+    M3_TRY(advect_device_rk4(M, dt, o, 3, !first_step, info));
+  } else {
+    M3_TRY(advect_device(M, dt, o, !first_step, info));
+  }
+  M3_CUDA(cudaMemcpyAsync(T, S->out, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  return M3SPH_OK;
+}
+}  // namespace m3sph
 
 extern "C" int m3sph_advect_slm(m3sph_mesh *M, const double *Ux, const double *Uy, const double *Uz, double *T,
                                 double dt, const m3sph_slm_opts *o, int32_t *els_BT, int32_t *els_INTERP,
@@ -1176,6 +1378,33 @@ static int noalloc_scratch(int device, double **out) {
   return M3SPH_OK;
 }
 
+__global__ void k_cubic_interp_caller(SlmMesh m, const double *__restrict__ X, const int32_t *__restrict__ els,
+                                      const double *__restrict__ lc, int npt, const double *__restrict__ B,
+                                      const double *__restrict__ gn, const double *__restrict__ wn,
+                                      const double *__restrict__ gel, int monotonic, double *__restrict__ out);
+
+// zero n doubles (the nodal sums): a kernel of this module rather than cudaMemsetAsync, so that
+// nothing the call uses is loaded outside noalloc_prepare
+__global__ void k_noalloc_zero(double *a, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = 0.0;
+}
+
+// Run once per handle, from m3sph_mesh_create with the handle's device current. With CUDA's lazy
+// module loading, the first use of this file's module -- the scratch lookup or the first launch of
+// one of its kernels -- is where the driver loads the code and commits the 8 MiB array; doing both
+// here keeps those allocations out of m3sph_interp3d_cubic_noalloc.
+static int noalloc_prepare(int device) {
+  double *scr = nullptr;
+  int st = noalloc_scratch(device, &scr);
+  if (st) return st;
+  cudaFuncAttributes fa;
+  M3_CUDA(cudaFuncGetAttributes(&fa, k_cubic_elgrad));
+  M3_CUDA(cudaFuncGetAttributes(&fa, k_cubic_scatter));
+  M3_CUDA(cudaFuncGetAttributes(&fa, k_cubic_interp_caller));
+  M3_CUDA(cudaFuncGetAttributes(&fa, k_noalloc_zero));
+  return M3SPH_OK;
+}
+
 // quasi-cubic value at one point of element e with local coordinates (r,s,t): the same arithmetic
 // as k_cubic_interp (interp3d_cubic_p.m:243-382)
 __device__ double cubic_point(const SlmMesh &m, const double *__restrict__ X, int e, double r, double s, double t,
@@ -1259,7 +1488,8 @@ extern "C" int m3sph_interp3d_cubic_noalloc(m3sph_mesh *M, const int32_t *els, c
   cudaStream_t s = M->stream;
   k_cubic_elgrad<<<(unsigned)((nel + 127) / 128), 128, 0, s>>>(S->view, M->fin.gcoord, V, method_wght, gel, wel); count_launch();
   // the array keeps the previous call's contents: the nodal sums must start at zero
-  M3_CUDA(cudaMemsetAsync(gn, 0, sizeof(double) * 4 * nv, s));   // gn (3 nv) and wn (nv) are contiguous
+  k_noalloc_zero<<<(unsigned)std::min<size_t>((4 * nv + 255) / 256, 1024), 256, 0, s>>>(gn, 4 * nv); count_launch();
+  // (gn (3 nv) and wn (nv) are contiguous)
   for (size_t c = 0; c + 1 < L0.cstart.size(); ++c) {
     const int b = L0.cstart[c], e = L0.cstart[c + 1];
     if (e > b) k_cubic_scatter<<<(e - b + 127) / 128, 128, 0, s>>>(L0.perm, (int)nel, b, e, S->el2nod, gel, wel, gn,

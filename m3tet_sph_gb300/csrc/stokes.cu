@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <atomic>
 #include <mutex>
@@ -439,6 +440,8 @@ extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
   dfree(M->bc_rhs);
   dfree(M->red);
   dfree(M->scal);
+  dfree(M->T);
+  dfree(M->Usoa);
   for (void *p : M->work) dfree(p);
   if (M->h_scal) cudaFreeHost(M->h_scal);
   clear_graphs(M);
@@ -568,6 +571,21 @@ extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t
     }
     M->r_min = rmin;
     M->r_max = rmax;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int n = 0; n < nnod; ++n)
+      for (int c = 0; c < 3; ++c) {
+        lo[c] = std::min(lo[c], f0.GCOORD[3 * (size_t)n + c]);
+        hi[c] = std::max(hi[c], f0.GCOORD[3 * (size_t)n + c]);
+      }
+    M->Lx = hi[0] - lo[0];
+    M->Ly = hi[1] - lo[1];
+    M->Lz = hi[2] - lo[2];
+    double r2max = 0.0;
+    for (int n = 0; n < nnod; ++n) {
+      const double *x = f0.GCOORD + 3 * (size_t)n;
+      r2max = std::max(r2max, std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]));
+    }
+    M->rad_max = r2max;
   }
   if ((st = ml_build(M)) || (st = ml_init_kernels())) return fail(st);
   *out = M;
@@ -1110,13 +1128,28 @@ __global__ void k_scale(double *a, double c, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i < n) a[i] *= c;
 }
+// Cartesian component r of node n's velocity from its rotated-frame dofs (U_xyz = RR U)
+__device__ __forceinline__ double rotate_back_comp(const double *U, const double *RR, int nnod, int n, int r) {
+  double v = 0.0;
+  for (int c = 0; c < 3; ++c) v += RR[(size_t)(r * 3 + c) * nnod + n] * U[3 * n + c];
+  return v;
+}
 __global__ void k_rotate_back(const double *U, const double *RR, int nnod, double *Uxyz) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nnod) return;
+  for (int r = 0; r < 3; ++r) Uxyz[3 * n + r] = rotate_back_comp(U, RR, nnod, n, r);
+}
+
+// max |Ux|, |Uy|, |Uz| of the resident solution (calculate_dt.m:40-42): warp-shuffle maxima, one
+// atomicMax per warp on the bit patterns (non-negative doubles order like their uint64 bits)
+__global__ void k_absmax_xyz(const double *U, const double *RR, int nnod, unsigned long long *out) {
+  double m[3] = {0.0, 0.0, 0.0};
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnod; n += gridDim.x * blockDim.x)
+    for (int r = 0; r < 3; ++r) m[r] = fmax(m[r], fabs(rotate_back_comp(U, RR, nnod, n, r)));
   for (int r = 0; r < 3; ++r) {
-    double v = 0.0;
-    for (int c = 0; c < 3; ++c) v += RR[(size_t)(r * 3 + c) * nnod + n] * U[3 * n + c];
-    Uxyz[3 * n + r] = v;
+    double v = m[r];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out + r, (unsigned long long)__double_as_longlong(v));
   }
 }
 
@@ -1219,6 +1252,7 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   double norm_rP0 = norm_rP, rd = 0.0, rdlast = 0.0, tol_Z = 0.0;
   int itPat = 0;
   const double target = opts->target_rel_residual;
+  bool converged = false;
   for (itPat = 1; itPat <= itmax_Pat; ++itPat) {
     M3_TRY(precondition_P(M, r, d));
     if (restart) {
@@ -1264,15 +1298,28 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
       double rel;
       M3_TRY(coupled_residual(M, U, Pd, rel));
       if (rel > target) {
-        // the coupled residual is not yet at the target: tighten both tolerances and go on
+        // the coupled residual is not yet at the target: tighten both tolerances, replace the
+        // recursively updated pressure residual (it drifts from -G'U over many iterations) by the
+        // true one of a velocity solved for the current pressure, and restart the CG direction
         tol_Pat *= 0.1;
         rtol_U *= 0.1;
         tol_U_restart = rtol_U * tol_Pat;
-        done = false;
+        M3_TRY(build_rhs(M, Pd, W->Rhs));
+        M3_TRY(mgpcg(M, W->Rhs, U, tol_U_restart, true, itmax_U, cs));
+        inf.nitU += cs.it;
+        M3_TRY(div_apply(L0, M->fin.G64, U, r, s));
+        k_scale<<<(np + 255) / 256, 256, 0, s>>>(r, -1.0, np); count_launch();
+        M3_TRY(remove_mean(M, r));
+        M3_TRY(pdot(M, r, r, rr));
+        norm_rP = std::sqrt(rr) / sqp;
         restart = true;
+        continue;
       }
     }
-    if (done) break;
+    if (done) {
+      converged = true;
+      break;
+    }
     if (norm_rP < rtol_restart * norm_rP0 || norm_rP > 10 * norm_rP0) {
       M3_TRY(build_rhs(M, Pd, W->Rhs));
       M3_TRY(mgpcg(M, W->Rhs, U, tol_U_restart, true, itmax_U, cs));
@@ -1308,6 +1355,18 @@ static int solve_core(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info &inf) {
   inf.rel_residual = rel;
   M3_TRY(stream_check(L0, s));
   M3_TRY(ml_check(M));
+  // The reference returns its last iterate silently when itmax_Pat runs out or after the second
+  // convergence problem (flow3d_patera_mg_sph_p.m:580-606); here the iterate is still returned, but
+  // with M3SPH_ERR_NOT_CONVERGED. With a target the final coupled residual decides.
+  if (target > 0) converged = rel <= target;
+  if (!converged) {
+    char msg[200];
+    snprintf(msg, sizeof msg, "Patera iteration not converged: %d iterations (itmax_Pat %d), norm_rP %.3e, "
+             "coupled residual %.3e (target %.1e)", inf.itPat, itmax_Pat, norm_rP, rel, target);
+    set_error(msg);
+    inf.status = M3SPH_ERR_NOT_CONVERGED;
+    return M3SPH_ERR_NOT_CONVERGED;
+  }
   return M3SPH_OK;
 }
 
@@ -1347,8 +1406,9 @@ extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const
   M3_CUDA(cudaEventCreate(&e1));
   M3_CUDA(cudaEventRecord(e0, s));
   m3sph_info inf{};
-  int st = solve_core(M, opts, inf);
-  if (st) {
+  // M3SPH_ERR_NOT_CONVERGED still delivers the last iterate (and the info) to the caller
+  const int st = solve_core(M, opts, inf);
+  if (st && st != M3SPH_ERR_NOT_CONVERGED) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return st;
@@ -1363,9 +1423,9 @@ extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const
   inf.t_setup_ms = M->last_setup_ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  inf.status = M3SPH_OK;
+  inf.status = st;
   if (info) *info = inf;
-  return M3SPH_OK;
+  return st;
 }
 
 extern "C" int m3sph_stokes_step_device(m3sph_mesh *M, const m3sph_opts *opts, m3sph_info *info) {
@@ -1385,15 +1445,16 @@ extern "C" int m3sph_stokes_step_device(m3sph_mesh *M, const m3sph_opts *opts, m
   M3_CUDA(cudaEventRecord(e1, s));
   M3_CUDA(cudaMemsetAsync(W->pP, 0, sizeof(double) * M->lev[0].nvnod, s));
   m3sph_info inf{};
-  M3_TRY(solve_core(M, opts, inf));
+  const int st = solve_core(M, opts, inf);
+  if (st && st != M3SPH_ERR_NOT_CONVERGED) return st;
   M3_CUDA(cudaEventRecord(e2, s));
   M3_CUDA(cudaEventSynchronize(e2));
   M3_TRY(time_since(e0, e1, inf.t_setup_ms));
   M3_TRY(time_since(e1, e2, inf.t_iter_ms));
   for (cudaEvent_t e : {e0, e1, e2}) cudaEventDestroy(e);
-  inf.status = M3SPH_OK;
+  inf.status = st;
   if (info) *info = inf;
-  return M3SPH_OK;
+  return st;
 }
 
 extern "C" int m3sph_stream(m3sph_mesh *M, void **stream) {
@@ -1414,6 +1475,81 @@ extern "C" int m3sph_solution(m3sph_mesh *M, double *U_xyz, double *P) {
   if (U_xyz) M3_CUDA(cudaMemcpyAsync(U_xyz, W->tmp, sizeof(double) * L0.ndof, cudaMemcpyDeviceToHost, s));
   if (P) M3_CUDA(cudaMemcpyAsync(P, W->pP, sizeof(double) * L0.nvnod, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
+  return M3SPH_OK;
+}
+
+__global__ void k_velocity_soa(const double *U, const double *RR, int nnod, double *out) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnod) return;
+  for (int r = 0; r < 3; ++r) out[(size_t)r * nnod + n] = rotate_back_comp(U, RR, nnod, n, r);
+}
+
+namespace m3sph {
+// hooks for the device-resident time step (timestep.cu)
+int stokes_velocity_soa(m3sph_mesh *M, double *dst) {
+  Work *W = get_work(M);
+  const int n = M->lev[0].nnod;
+  k_velocity_soa<<<(n + 255) / 256, 256, 0, M->stream>>>(W->U, M->fin.RR, n, dst); count_launch();
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+int stokes_resident_solve(m3sph_mesh *M, const m3sph_opts *opts, bool zero_p, m3sph_info &inf) {
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  cudaEvent_t e0, e1, e2;
+  M3_CUDA(cudaEventCreate(&e0));
+  M3_CUDA(cudaEventCreate(&e1));
+  M3_CUDA(cudaEventCreate(&e2));
+  M3_CUDA(cudaEventRecord(e0, s));
+  M3_TRY(rebuild_operator(M));
+  M3_CUDA(cudaEventRecord(e1, s));
+  if (zero_p) M3_CUDA(cudaMemsetAsync(W->pP, 0, sizeof(double) * M->lev[0].nvnod, s));
+  inf = m3sph_info{};
+  const int st = solve_core(M, opts, inf);
+  if (st && st != M3SPH_ERR_NOT_CONVERGED) return st;
+  M3_CUDA(cudaEventRecord(e2, s));
+  M3_CUDA(cudaEventSynchronize(e2));
+  M3_TRY(time_since(e0, e1, inf.t_setup_ms));
+  M3_TRY(time_since(e1, e2, inf.t_iter_ms));
+  for (cudaEvent_t e : {e0, e1, e2}) cudaEventDestroy(e);
+  inf.status = st;
+  return st;
+}
+int stokes_calc_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv);
+}  // namespace m3sph
+
+extern "C" int m3sph_calculate_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv) {
+  M3_TRY(need_op_fwd(M));
+  if (!dt) {
+    set_error("m3sph_calculate_dt: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  return m3sph::stokes_calc_dt(M, dt_adv_limit, dtmax, dt, dt_adv);
+}
+
+int m3sph::stokes_calc_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv) {
+  Work *W = get_work(M);
+  cudaStream_t s = M->stream;
+  Level &L0 = M->lev[0];
+  unsigned long long *mx = reinterpret_cast<unsigned long long *>(M->scal + 12);
+  M3_CUDA(cudaMemsetAsync(mx, 0, 3 * sizeof(double), s));
+  k_absmax_xyz<<<152 * 4, 256, 0, s>>>(W->U, M->fin.RR, L0.nnod, mx); count_launch();
+  M3_CUDA(cudaGetLastError());
+  M3_CUDA(cudaMemcpyAsync(M->h_scal + 12, M->scal + 12, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  const double mux = M->h_scal[12], muy = M->h_scal[13], muz = M->h_scal[14];
+  if (std::isnan(mux) || std::isnan(muy) || std::isnan(muz)) {
+    set_error("m3sph_calculate_dt: velocity contains NaNs");
+    return M3SPH_ERR_NAN;
+  }
+  // calculate_dt.m:43-52; Lx/0 is +Inf and drops out of the min as in MATLAB
+  double adv = 0.0, out = dtmax;
+  if (!(mux == 0.0 && muy == 0.0 && muz == 0.0)) {
+    adv = dt_adv_limit * std::min(std::min(M->Lx / mux, M->Ly / muy), M->Lz / muz);
+    out = std::min(dtmax, adv);
+  }
+  *dt = out;
+  if (dt_adv) *dt_adv = adv;
   return M3SPH_OK;
 }
 

@@ -154,29 +154,88 @@ class DeviceMesh:
         return x, it.value, rr.value
 
     def solve(self, P0=None, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20,
-              target_rel_residual=0.0, smoother=0):
+              target_rel_residual=0.0, smoother=0, allow_not_converged=False):
+        """Patera solve from host arrays. A solve that runs out of iterations above its tolerance
+        raises M3SphError(ERR_NOT_CONVERGED) whose ``result`` holds (U, P, info); with
+        ``allow_not_converged`` the last iterate is returned instead, with info['status'] = 4."""
         U = np.empty(self.ndof)
         P = np.zeros(self.nvnod) if P0 is None else np.ascontiguousarray(P0, dtype=np.float64).copy()
         o = L.Opts(rtol_Pat=rtol_Pat, rtol_U=rtol_U, itmax_Pat=itmax_Pat, itmin_Pat=itmin_Pat, itmax_U=itmax_U,
                    precision=int(self.precision or 0), smoother=smoother, target_rel_residual=target_rel_residual)
         info = L.Info()
-        L.check(L.lib().m3sph_stokes_solve(self.h, L.dptr(U), L.dptr(P), C.byref(o), C.byref(info)))
-        return U, P, info.as_dict()
+        code = L.lib().m3sph_stokes_solve(self.h, L.dptr(U), L.dptr(P), C.byref(o), C.byref(info))
+        return self._finish(code, (U, P, info.as_dict()), allow_not_converged)
 
     def step_device(self, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20,
-                    target_rel_residual=0.0, smoother=0):
+                    target_rel_residual=0.0, smoother=0, allow_not_converged=False):
         """Rebuild the operator from resident inputs and solve from P=0; results stay on device."""
         o = L.Opts(rtol_Pat=rtol_Pat, rtol_U=rtol_U, itmax_Pat=itmax_Pat, itmin_Pat=itmin_Pat, itmax_U=itmax_U,
                    precision=int(self.precision or 0), smoother=smoother, target_rel_residual=target_rel_residual)
         info = L.Info()
-        L.check(L.lib().m3sph_stokes_step_device(self.h, C.byref(o), C.byref(info)))
-        return info.as_dict()
+        code = L.lib().m3sph_stokes_step_device(self.h, C.byref(o), C.byref(info))
+        return self._finish(code, info.as_dict(), allow_not_converged)
+
+    @staticmethod
+    def _finish(code, result, allow_not_converged):
+        if code == L.ERR_NOT_CONVERGED:
+            if allow_not_converged:
+                return result
+            err = L.M3SphError(code, L.lib().m3sph_last_error().decode())
+            err.result = result
+            raise err
+        L.check(code)
+        return result
 
     def solution(self):
         U = np.empty(self.ndof)
         P = np.empty(self.nvnod)
         L.check(L.lib().m3sph_solution(self.h, L.dptr(U), L.dptr(P)))
         return U, P
+
+    def calculate_dt(self, dt_adv_limit, dtmax):
+        """calculate_dt.m:40-52 on the device-resident velocity of the last solve: (dt, dt_adv)."""
+        dt, adv = C.c_double(), C.c_double()
+        L.check(L.lib().m3sph_calculate_dt(self.h, float(dt_adv_limit), float(dtmax), C.byref(dt), C.byref(adv)))
+        return dt.value, adv.value
+
+    def rock_prop(self, T, params):
+        """rock_prop.m:5-66 on the GPU: (Visc, Dens) of nodal T; params: dict of m3sph_rock_params
+        fields (a missing or None cut-off is not applied)."""
+        rp = rock_params_struct(params)
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        V, D = np.empty_like(T), np.empty_like(T)
+        L.check(L.lib().m3sph_rock_prop(self.h, C.byref(rp), L.dptr(T), L.dptr(V), L.dptr(D)))
+        return V, D
+
+    def set_temperature(self, T, time=0.0):
+        L.check(L.lib().m3sph_set_temperature(self.h, L.dptr(np.ascontiguousarray(T, dtype=np.float64)), float(time)))
+
+    def get_temperature(self):
+        T = np.empty(self.nnod)
+        L.check(L.lib().m3sph_get_temperature(self.h, L.dptr(T)))
+        return T
+
+    def time_step(self, stokes_kw=None, slm=None, rock=None, dt_adv_limit=0.005, dtmax=0.1, smoother=0,
+                  r_cmb=3480.0, r_surf=6371.0, allow_not_converged=False):
+        """One device-resident time step (rock_prop if `rock` is given -> Stokes -> calculate_dt ->
+        semi-Lagrangian advection of the resident T). Returns the step info as a dict."""
+        kw = dict(rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20, target_rel_residual=0.0)
+        kw.update(stokes_kw or {})
+        slm = dict(slm or {})
+        o = L.StepOpts()
+        o.stokes = L.Opts(precision=int(self.precision or 0), smoother=smoother, **kw)
+        o.slm = L.SlmOpts(method_BT=1 if slm.get('method_BT', 'PC2') == 'PC2' else 2,
+                          method_interp=1 if slm.get('method_interp', 'cubic') == 'cubic' else 0,
+                          monotonic=int(slm.get('monotonic', 1)),
+                          method_wght=1 if slm.get('method_wght', 'dist') == 'dist' else 0, r_cmb=r_cmb, r_surf=r_surf)
+        o.rock_prop = 1 if rock is not None else 0
+        if rock is not None:
+            o.rock = rock_params_struct(rock)
+        o.dt_adv_limit = dt_adv_limit
+        o.dtmax = dtmax
+        info = L.StepInfo()
+        code = L.lib().m3sph_time_step(self.h, C.byref(o), C.byref(info))
+        return self._finish(code, info.as_dict(), allow_not_converged)
 
     def set_option(self, name, value):
         L.check(L.lib().m3sph_set_option(self.h, name.encode(), int(value)))
@@ -219,3 +278,35 @@ def flow3d_patera_sph(VAR, MESH, COMM, UBC, SETTINGS, PHYSICS, NUMSCALE, dt):
     VAR['Uth'], VAR['Uph'], VAR['Ur'] = Ul[:, 0].copy(), Ul[:, 1].copy(), Ul[:, 2].copy()
     VAR['P'] = P
     return VAR, info
+
+
+def calculate_dt(MESH, COMM, SETTINGS, NUMSCALE, VAR):
+    """Mirror of calculate_dt.m:1-62 for the velocity of the last GPU solve on MESH['device_mesh']
+    (the VAR.Ux/Uy/Uz that flow3d_patera_sph returned): dt = min(dtmax, dt_adv_limit * min(L/max|U|))."""
+    dt, _ = MESH['device_mesh'].calculate_dt(SETTINGS['dt_adv_limit'], SETTINGS['dtmax'])
+    return dt
+
+
+def rock_params_struct(p):
+    """m3sph_rock_params from a dict of PHYSICS / NUMSCALE values; absent cut-offs are NaN."""
+    nan = float('nan')
+    g = lambda k, d=0.0: d if p.get(k) is None else float(p[k])
+    return L.RockParams(Visc0=g('Visc0'), Dens0=g('Dens0'), T_ref=g('T_ref'), alpha=g('alpha'), Ea=g('Ea'),
+                        Va=g('Va'), g=g('g'), L0=g('L0', 1.0), a_UM2LM=g('a_UM2LM'), minDens=g('minDens', nan),
+                        maxDens=g('maxDens', nan), minVisc=g('minVisc', nan), maxVisc=g('maxVisc', nan))
+
+
+def rock_prop(VAR, PHYSICS, NUMSCALE, MESH, SETTINGS=None):
+    """Mirror of rock_prop.m:1 (VAR = rock_prop(VAR,PHYSICS,NUMSCALE,MESH,SETTINGS)) on the GPU:
+    VAR['Visc'] and VAR['Dens'] from VAR['T']."""
+    dm = MESH.get('device_mesh')
+    if dm is None:
+        dm = DeviceMesh(MESH['levels'])
+        MESH['device_mesh'] = dm
+    p = dict(Visc0=PHYSICS['Visc'], Dens0=PHYSICS['Dens'], T_ref=PHYSICS['T_ref'], alpha=PHYSICS['alpha'],
+             Ea=PHYSICS['Ea'], Va=PHYSICS['Va'], g=PHYSICS['g'], L0=NUMSCALE['L0'], a_UM2LM=PHYSICS.get('a_UM2LM'),
+             minDens=PHYSICS.get('minDens'), maxDens=PHYSICS.get('maxDens'), minVisc=PHYSICS.get('minVisc'),
+             maxVisc=PHYSICS.get('maxVisc'))
+    VAR = dict(VAR)
+    VAR['Visc'], VAR['Dens'] = dm.rock_prop(VAR['T'], p)
+    return VAR

@@ -157,3 +157,15 @@ def make_workload(name, seed=0, nmg=None, level=None, nlayer=None):
     ifix, vfix = boundary_conditions(levels[0], bc, seed)
     return dict(name=name, levels=levels, visc=visc, dens=dens, T=T, ifix=ifix, vfix=vfix, phys=physics(),
                 level=L, nlayer=n, nmg=g, contrast=contrast)
+
+
+def rock_params(contrast=1e6):
+    """rock_prop parameters (rock_prop.m) for temperatures in degC (T_C = DT_K * T): Arrhenius law
+    about 1250 degC, an activation volume whose factor reaches a_UM2LM = 30 at 660 km depth (the
+    upper/lower-mantle jump), and viscosity cut-offs giving the requested contrast around 1e21 Pa s."""
+    eta0 = 1e21 / SCALE['Visc0']
+    T0_K = 1250.0 + 273.0
+    P660 = 9.81 * SCALE['Dens0'] * SCALE['L0'] * 660.0
+    return dict(Visc0=eta0, Dens0=SCALE['Dens0'], T_ref=1250.0, alpha=ALPHA, Ea=250e3,
+                Va=np.log(30.0) * 8.314472 * T0_K / P660, g=-9.81, L0=SCALE['L0'], a_UM2LM=30.0,
+                minVisc=eta0 / np.sqrt(contrast), maxVisc=eta0 * np.sqrt(contrast))

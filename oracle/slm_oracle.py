@@ -13,13 +13,30 @@ Restated reference behaviour (paths inside the reference project):
 * mfiles_M3TET/interp3d_tet.m:39-69 (P2 interpolation, monotone clamp)
 * mfiles_M3TET/interp3d_cubic_p.m:80-382 (quasi-cubic interpolation, 'dist' weighted gradients)
 
-Point location. The reference's ``tsearch2_sph`` runs MUTILS ``tsearch2`` (not vendored, not runnable
-here) in up to five rotated frames and filters by element class. Its semantics for a point that
-lies strictly inside exactly one element, in that element's own frame, is that element; this
-oracle finds every containing element by an exhaustive own-frame barycentric test over the
-nearest elements and applies a deterministic rule for ties: prefer non-isoparametric elements,
-then the largest element id (the reference takes ``max`` over its candidate columns,
-tsearch2_sph.m:404). MUTILS's own choice among tied elements is unpinned.
+Point location (one explicit rule, shared with the CUDA walk). The reference's ``tsearch2_sph``
+runs MUTILS ``tsearch2`` (not vendored, not runnable here) in up to five rotated frames, keeps at most
+one element per frame pass and then resolves points that several passes placed. Here every element
+is tested in its own frame (class 0: original, class 1: Z-180, classes 2-3: X-90), with
+need(e) = max(-min barycentric, max barycentric - 1):
+
+1. C = {e : need(e) <= TIE_BAND}. If C is not empty (tsearch2_sph.m:374-404):
+   a. if C holds a non-isoparametric element, the isoparametric ones are dropped (:380-382);
+   b. if the point is at a vertex of every remaining element (max barycentric >= 1 - TIE_BAND),
+      only those of the first frame in the reference's pass order are kept -- X-90 (cone classes),
+      then original, then Z-180 (:383-386 keeps the first candidate column);
+   c. the largest id is taken (:404).
+   Ties (|C| >= 2) are counted; so are the ties where neither (a) nor (b) applies and the remaining
+   elements lie in more than one frame -- the reference raises error('no good') there (:387-392).
+2. Otherwise the tolerance grows in 1e-6 steps up to 15e-3
+   (locate_points_in_neighboring_element.m:1-158): q(e) = ceil(need/1e-6 - 1e-9) <= 15000, and among
+   the elements of the smallest q: if all are isoparametric, the one with the smallest last Newton
+   step (:52-58), otherwise the non-isoparametric one of the smallest id (the reference takes the
+   first of the remaining list, :60-66). These points are counted as gaps.
+3. Otherwise the point is not located (the reference raises 'some nodes have not been located').
+
+The Newton iteration for isoparametric elements stops per point (local_coords_curved_3d_sph.m stops
+when the largest error of the whole batch is below 1e-8, which makes a point's coordinates depend
+on the batch it is processed with). MUTILS's own choice among tied elements is unpinned.
 """
 from __future__ import annotations
 
@@ -91,30 +108,36 @@ def sf10(r, s, t):
 
 def local_coords_curved(SX, EL, els, pX):
     """local_coords_curved_3d_sph: linear guess + up to 6 Newton steps on the 10-node map in the
-    X-90 frame, stopping when the largest error of all points is below 1e-8. Returns lc and the
-    last Newton step delS."""
+    X-90 frame; a point stops once its own error is below 1e-8. Returns lc and the sum of |delS| of
+    each point's last Newton step (0 if it took none)."""
     V = SX[:, EL[els, :4]].transpose(1, 0, 2)
     lc = compute_lc(V, pX)
     G = SX[:, EL[els]]                      # (3,n,10)
-    delS = np.zeros_like(lc)
+    step = np.zeros(lc.shape[1])
+    active = np.ones(lc.shape[1], bool)
     for _ in range(6):
         N, dN = sf10(*lc)                   # N (10,n), dN (10,3,n)
         TH0 = np.einsum('kni,in->kn', G, N)
         dTH = pX - TH0
         err = np.sqrt((dTH * dTH).sum(0))
-        if err.size == 0 or err.max() < 1e-8:
+        active &= ~(err < 1e-8)
+        if not active.any():
             break
-        J = np.einsum('kni,ijn->nkj', G, dN)    # (n,3,3): d TH_k / d s_j
-        delS = np.linalg.solve(J, dTH.T[:, :, None])[:, :, 0].T
-        lc = lc + delS
-    return lc, delS
+        a = np.nonzero(active)[0]
+        J = np.einsum('kni,ijn->nkj', G[:, a], dN[:, :, a])    # (n,3,3): d TH_k / d s_j
+        delS = np.linalg.solve(J, dTH[:, a].T[:, :, None])[:, :, 0].T
+        lc[:, a] = lc[:, a] + delS
+        step[a] = np.abs(delS).sum(0)
+    return lc, step
 
 
-def local_coords(F, els, P):
-    """Own-frame local coordinates (3,n) of points P (3,n, original (theta,phi,r)) in elements els."""
+def local_coords(F, els, P, return_step=False):
+    """Own-frame local coordinates (3,n) of points P (3,n, original (theta,phi,r)) in elements els
+    (and the last Newton step of isoparametric elements, 0 elsewhere)."""
     els = np.asarray(els, dtype=np.int64)
     P0, PZ, PX = F.point_frames(P)
     lc = np.zeros((3, len(els)))
+    step = np.zeros(len(els))
     cls = F.cls[els]
     EL = F.EL
     for c, S, Pp in ((0, F.S0, P0), (1, F.SZ, PZ), (2, F.SX, PX)):
@@ -124,8 +147,8 @@ def local_coords(F, els, P):
             lc[:, m] = compute_lc(V, Pp[:, m])
     m = cls == 3
     if m.any():
-        lc[:, m], _ = local_coords_curved(F.SX, EL, els[m], PX[:, m])
-    return lc
+        lc[:, m], step[m] = local_coords_curved(F.SX, EL, els[m], PX[:, m])
+    return (lc, step) if return_step else lc
 
 
 def inside(lc, tol=0.0):
@@ -133,56 +156,167 @@ def inside(lc, tol=0.0):
     return (lc.min(0) >= -tol) & (lc.max(0) <= 1 + tol) & (l4 >= -tol) & (l4 <= 1 + tol)
 
 
+TIE_BAND = 1e-10          # containment test: every barycentric within [-TIE_BAND, 1 + TIE_BAND]
+TIE_TRIGGER = 1e-7        # an element placing the point this close to its boundary may tie with another
+IFACE_TRIGGER = 15e-3     # the same next to another frame or to isoparametric elements (overlaps)
+GAP_STEP, GAP_QMAX = 1e-6, 15000
+FRAME_RANK = np.array([1, 2, 0, 0])     # pass order of each class's frame: X-90 0, original 1, Z-180 2
+
+
+def tie_rule(ids, iso, frame, atvtx):
+    """Rule 1 of the module docstring for candidates `ids` (all within TIE_BAND): returns
+    (element, ambiguous)."""
+    ids, iso, frame, atvtx = map(np.asarray, (ids, iso, frame, atvtx))
+    keep = np.ones(len(ids), bool)
+    dropped_iso = (~iso).any() and iso.any()
+    if dropped_iso:
+        keep &= ~iso
+    all_vtx = bool(atvtx[keep].all())
+    if all_vtx and keep.sum() >= 2:
+        keep &= frame == frame[keep].min()
+    ambiguous = len(ids) >= 2 and not dropped_iso and not all_vtx and len(np.unique(frame[keep])) > 1
+    return int(ids[keep].max()), bool(ambiguous)
+
+
+def gap_rule(ids, iso, q, step):
+    """Rule 2 of the module docstring for elements `ids` with quantised tolerances q <= GAP_QMAX."""
+    ids, iso, q, step = map(np.asarray, (ids, iso, q, step))
+    g = q == q.min()
+    if iso[g].all():
+        s = step[g]
+        return int(ids[g][s == s.min()].min())
+    return int(ids[g & ~iso].min())
+
+
 class Locator:
-    """Exhaustive own-frame point location over the k nearest elements (by centroid)."""
+    """Point location by the explicit rule of the module docstring. Candidate elements come from
+    the k nearest element centroids; an element that places the point near its boundary has its
+    vertex neighbours added (every other element within the tie band shares a vertex with it),
+    and a point outside all of them is tested against every element whose centroid lies within
+    1.5 circumradii."""
 
     def __init__(self, mesh, k=48):
         self.F = Frames(mesh)
         X = mesh['GCOORD']
         EL = mesh['EL2NOD']
-        self.cent = X[:, EL[:, :4]].mean(axis=2).T
+        EL4 = EL[:, :4]
+        nel = len(EL)
+        cls = mesh['cls']
+        self.iso = cls == 3
+        self.frame = FRAME_RANK[cls]
+        nv = int(EL4.max()) + 1
+        order = np.argsort(EL4.ravel(), kind='stable')
+        self.v2e = order // 4
+        self.v2e_ptr = np.searchsorted(EL4.ravel()[order], np.arange(nv + 1))
+        self.EL4 = EL4
+        key = self.frame * 2 + self.iso
+        kmin = np.full(nv, 99)
+        kmax = np.full(nv, -1)
+        np.minimum.at(kmin, EL4.ravel(), np.repeat(key, 4))
+        np.maximum.at(kmax, EL4.ravel(), np.repeat(key, 4))
+        self.iface = (kmin[EL4] != kmax[EL4]).any(1)
+        V = X[:, EL4]                                           # (3,nel,4)
+        self.cent = V.mean(axis=2).T
+        self.rad = np.sqrt(((V - self.cent.T[:, :, None]) ** 2).sum(0)).max()
         self.tree = cKDTree(self.cent)
-        self.k = k
-        self.iso = mesh['cls'] == 3
+        self.k = min(k, nel)
+
+    def ring1(self, e):
+        return np.unique(np.concatenate([self.v2e[self.v2e_ptr[v]:self.v2e_ptr[v + 1]] for v in self.EL4[e]]))
+
+    def _eval(self, els, P):
+        lc, step = local_coords(self.F, els, P, return_step=True)
+        l4 = 1 - lc.sum(0)
+        mn = np.minimum(lc.min(0), l4)
+        mx = np.maximum(lc.max(0), l4)
+        return lc, step, mn, mx, np.maximum(-mn, mx - 1.0)
+
+    def _resolve_many(self, lists, P):
+        """Rules 1-3 for points P (3,m), point i over candidate elements lists[i]: (els, lc, kind)."""
+        m = len(lists)
+        R = max(len(l) for l in lists)
+        ring = np.full((m, R), -1, np.int64)
+        for i, l in enumerate(lists):
+            ring[i, :len(l)] = l
+        valid = ring >= 0
+        rows, cols = np.nonzero(valid)
+        lc_v, step_v, mn_v, mx_v, need_v = self._eval(ring[rows, cols], P[:, rows])
+        need = np.full((m, R), np.inf)
+        mx = np.zeros((m, R))
+        step = np.zeros((m, R))
+        need[rows, cols], mx[rows, cols], step[rows, cols] = need_v, mx_v, step_v
+        idx = np.full((m, R), -1)
+        idx[rows, cols] = np.arange(len(rows))
+        iso = self.iso[np.maximum(ring, 0)] & valid
+        frame = self.frame[np.maximum(ring, 0)]
+        # rule 1
+        cand = need <= TIE_BAND
+        drop = (cand & ~iso).any(1) & (cand & iso).any(1)
+        keep = cand & ~(drop[:, None] & iso)
+        atv = mx >= 1 - TIE_BAND
+        all_vtx = (~keep | atv).all(1)
+        vdrop = all_vtx & (keep.sum(1) >= 2)
+        rmin = np.where(keep, frame, 9).min(1)
+        rmax = np.where(keep, frame, -1).max(1)
+        keep2 = keep & (~vdrop[:, None] | (frame == rmin[:, None]))
+        tie_e = np.where(keep2, ring, -1).max(1)
+        ncand = cand.sum(1)
+        amb = (ncand >= 2) & ~drop & ~all_vtx & (rmax > rmin)
+        # rule 2
+        q = np.where(valid & ~cand, np.ceil(need / GAP_STEP - 1e-9), np.inf)
+        q[q > GAP_QMAX] = np.inf
+        qmin = q.min(1)
+        G = np.isfinite(q) & (q == qmin[:, None])
+        all_iso = (~G | iso).all(1)
+        non_e = np.where(G & ~iso, ring, np.iinfo(np.int64).max).min(1)
+        smin = np.where(G & iso, step, np.inf).min(1)
+        iso_e = np.where(G & iso & (step == smin[:, None]), ring, np.iinfo(np.int64).max).min(1)
+        gap_e = np.where(all_iso, iso_e, non_e)
+        has_tie = ncand > 0
+        has_gap = ~has_tie & np.isfinite(qmin)
+        els = np.where(has_tie, tie_e, np.where(has_gap, gap_e, -1))
+        kind = np.where(has_tie, 1 | np.where(ncand >= 2, 2, 0) | np.where(amb, 32, 0), np.where(has_gap, 4, 8))
+        lcs = np.zeros((3, m))
+        ok = els >= 0
+        j = np.argmax(ring == els[:, None], axis=1)
+        lcs[:, ok] = lc_v[:, idx[np.nonzero(ok)[0], j[ok]]]
+        return els, lcs, kind.astype(np.int32)
 
     def locate(self, P, return_info=False):
-        """Element ids (0-based) and lc of points P (3,n). info: number of candidates per point
-        with exact containment, and min barycentric margin of the chosen element."""
+        """Element ids (0-based, -1 if not located) and own-frame lc (3,n) of points P (3,n,
+        (theta,phi,r)). info: per-point kind bits (1 placed, 2 tie, 4 gap, 8 not located,
+        32 ambiguous for the reference) and counts."""
         n = P.shape[1]
         Xp = sph2cart(P).T
         _, nb = self.tree.query(Xp, k=self.k)
-        els = np.full(n, -1, np.int64)
-        lcs = np.zeros((3, n))
-        ncand = np.zeros(n, np.int32)
-        margin = np.full(n, -np.inf)
-        Pk = np.repeat(P, self.k, axis=1)
-        cand = nb.ravel()
-        lc = local_coords(self.F, cand, Pk).reshape(3, n, self.k)
-        l4 = 1 - lc.sum(0)
-        mn = np.minimum(lc.min(0), l4)          # (n,k) smallest barycentric
-        mx = np.maximum(lc.max(0), l4)
-        ok = (mn >= 0) & (mx <= 1)
-        ncand = ok.sum(1)
-        for i in range(n):
-            c = np.nonzero(ok[i])[0]
-            if len(c) == 0:
-                # grow the tolerance in 1e-6 steps up to 15e-3 (locate_points_in_neighboring_element.m)
-                need = np.maximum(-mn[i], mx[i] - 1.0)
-                steps = np.ceil(need / 1e-6 - 1e-9)
-                smin = steps.min()
-                if smin * 1e-6 > 15e-3 + 1e-6:
-                    continue
-                c = np.nonzero(steps == smin)[0]
-            ids = nb[i, c]
-            noniso = ~self.iso[ids]
-            if noniso.any() and not noniso.all():
-                c, ids = c[noniso], ids[noniso]
-            j = np.argmax(ids)
-            els[i] = ids[j]
-            lcs[:, i] = lc[:, i, c[j]]
-            margin[i] = mn[i, c[j]]
+        nb = nb.reshape(n, self.k)
+        lc, _, mn, mx, need = self._eval(nb.ravel(), np.repeat(P, self.k, axis=1))
+        lc, mn, mx, need = lc.reshape(3, n, self.k), mn.reshape(n, -1), mx.reshape(n, -1), need.reshape(n, -1)
+        j = np.argmin(need, axis=1)
+        r = np.arange(n)
+        best = nb[r, j]
+        els = best.copy()
+        lcs = lc[:, r, j].copy()
+        kind = np.ones(n, np.int32)
+        found = need[r, j] <= TIE_BAND
+        mnb, mxb = mn[r, j], mx[r, j]
+        trig = found & ((mnb < TIE_TRIGGER) | (mxb > 1 - TIE_TRIGGER) | (self.iface[best] & (mnb < IFACE_TRIGGER)))
+        for sel, lists in ((np.nonzero(trig)[0], None), (np.nonzero(~found)[0], None)):
+            if len(sel) == 0:
+                continue
+            if sel is not None and found[sel[0]]:
+                lists = [self.ring1(best[i]) for i in sel]
+            else:
+                lists = [np.array(sorted(self.tree.query_ball_point(Xp[i], 1.5 * self.rad)), dtype=np.int64)
+                         for i in sel]
+            for c in range(0, len(sel), 4096):
+                ss = sel[c:c + 4096]
+                e, l, k = self._resolve_many(lists[c:c + 4096], P[:, ss])
+                els[ss], lcs[:, ss], kind[ss] = e, l, k
         if return_info:
-            return els, lcs, dict(ncand=ncand, margin=margin)
+            info = dict(kind=kind, npt=n, nties=int(((kind & 2) > 0).sum()), ngap=int(((kind & 4) > 0).sum()),
+                        nambig=int(((kind & 32) > 0).sum()), nlost=int(((kind & 8) > 0).sum()))
+            return els, lcs, info
         return els, lcs
 
 

@@ -610,3 +610,59 @@ def patera(sysm, P0=None, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmax_U=20,
     info['itPat'] = itPat
     info['norm_rP'] = norm_rP
     return U, P, info
+
+
+def calculate_dt(GCOORD, Ux, Uy, Uz, dt_adv_limit, dtmax):
+    """CFL time step (calculate_dt.m:40-52): dt_adv = dt_adv_limit * min(Lx/max|Ux|, Ly/max|Uy|,
+    Lz/max|Uz|) with Lx = max(x) - min(x) of the mesh (init_mesh_curved_p.m:264-272), dt = min(dtmax,
+    dt_adv); an all-zero velocity gives (dtmax, 0). Returns (dt, dt_adv)."""
+    mx = [float(np.max(np.abs(u))) for u in (Ux, Uy, Uz)]
+    if mx[0] == 0 and mx[1] == 0 and mx[2] == 0:
+        return float(dtmax), 0.0
+    Lxyz = GCOORD.max(axis=1) - GCOORD.min(axis=1)
+    with np.errstate(divide='ignore'):
+        adv = dt_adv_limit * min(float(np.float64(Lxyz[k]) / np.float64(mx[k])) for k in range(3))
+    return min(float(dtmax), adv), adv
+
+
+ROCK_R = 8.314472            # J/(mol K), rock_prop.m
+
+
+def rock_prop(T, GCOORD, Visc0, Dens0, T_ref, alpha, Ea, Va, g, L0, a_UM2LM=0.0, minDens=None, maxDens=None,
+              minVisc=None, maxVisc=None):
+    """Nodal density and viscosity from temperature (rock_prop.m:5-66): thermal expansion about
+    T_ref with cut-offs; Arrhenius factor exp(Ea/(R T0_K) (T0_K/T_K - 1)) clamped to [1e-8, 1e8];
+    activation-volume factor exp(P Va / (R T0_K)) with lithostatic P = |g Dens0 L0 depth|, depth
+    below the outermost node; the lower-mantle factor a_UM2LM; their minimum (so the two do not
+    compound) times Visc0, with cut-offs. Returns (Visc, Dens)."""
+    T = np.asarray(T, dtype=np.float64)
+    radius = np.sqrt((GCOORD ** 2).sum(0))
+    depth = radius.max() - radius
+    Dens = Dens0 * (1 - alpha * (T - T_ref))
+    if maxDens is not None:
+        Dens = np.minimum(Dens, maxDens)
+    if minDens is not None:
+        Dens = np.maximum(Dens, minDens)
+    v = np.ones_like(T)
+    T0_K = T_ref + 273
+    if Ea > 0:
+        if Ea < 1000:
+            raise ValueError(" Activation energy PHYSICS.Ea seems to be in kJ/mol. Convert to J/mol.")
+        T_K = T + 273
+        eta = Ea / (ROCK_R * T0_K)
+        v = v * np.exp(eta * ((T0_K / T_K) - 1))
+        v = np.minimum(v, 1e8)
+        v = np.maximum(v, 1e-8)
+    v2 = v.copy()
+    if Va > 0:
+        P = np.abs(g * Dens0 * L0 * depth)
+        v2 = v2 * np.exp(P * Va / (ROCK_R * T0_K))
+    v3 = v.copy()
+    if a_UM2LM > 0:
+        v3 = v3 * a_UM2LM
+    Visc = np.minimum(v2, v3) * Visc0
+    if maxVisc is not None:
+        Visc = np.minimum(Visc, maxVisc)
+    if minVisc is not None:
+        Visc = np.maximum(Visc, minVisc)
+    return Visc, Dens

@@ -79,3 +79,51 @@ def test_threaded_sparse_products_match_serial(tiny):
     x4, it4, _ = s4.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
     assert it1 == it4
     assert np.linalg.norm(x4 - x1) <= 1e-12 * np.linalg.norm(x1)
+
+
+def test_tie_rule_follows_the_reference_preferences():
+    """tsearch2_sph.m:374-404 as restated: iso dropped when a non-iso candidate exists, the first
+    frame kept at a shared vertex, then the largest id; cross-frame face ties are flagged."""
+    from oracle.slm_oracle import tie_rule
+    # one iso + two non-iso on a face: iso dropped, largest remaining id
+    assert tie_rule([7, 3, 5], [True, False, False], [0, 0, 1], [False] * 3) == (5, False)
+    # all at a shared vertex, frames X-90 (0) and original (1): X-90 kept, then largest id
+    assert tie_rule([9, 4, 6], [False] * 3, [1, 0, 0], [True] * 3) == (6, False)
+    # cross-frame face tie without iso: the reference's error('no good') -> largest id, flagged
+    assert tie_rule([2, 8], [False, False], [1, 2], [False, False]) == (8, True)
+    # same-frame face tie: largest id, not flagged
+    assert tie_rule([2, 8], [False, False], [1, 1], [False, False]) == (8, False)
+    # two iso elements only: largest id
+    assert tie_rule([11, 12], [True, True], [0, 0], [False, False]) == (12, False)
+
+
+def test_gap_rule_follows_the_reference_preferences():
+    """locate_points_in_neighboring_element.m: smallest tolerance step; iso dropped if a non-iso
+    element remains (then the smallest id); all iso -> the smallest Newton step."""
+    from oracle.slm_oracle import gap_rule
+    assert gap_rule([5, 3, 9], [False, False, False], [4, 4, 7], [0, 0, 0]) == 3
+    assert gap_rule([5, 3, 9], [True, False, True], [4, 4, 4], [0, 0, 0]) == 3
+    assert gap_rule([5, 3, 9], [True, True, False], [4, 4, 9], [0.2, 0.1, 0]) == 3
+    assert gap_rule([5, 3], [True, True], [4, 4], [0.1, 0.1]) == 3
+
+
+def test_locator_independent_of_batch_and_neighbour_count():
+    """The located element of a point depends on the point alone: not on the other points of the
+    call (per-point Newton) nor on how many centroid neighbours seed the search."""
+    import numpy as np
+    from m3tet_sph_gb300 import workloads
+    from oracle import slm_oracle as SO
+    w = workloads.make_workload('tiny')
+    f = w['levels'][0]
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=(3, 3000))
+    v /= np.linalg.norm(v, axis=0)
+    r = (3480.0 ** 3 + rng.uniform(size=3000) * (6371.0 ** 3 - 3480.0 ** 3)) ** (1 / 3)
+    P = np.hstack([SO.cart2sph(v * r), f['GCOORD_SPH'][:, :1500]])
+    L1, L2 = SO.Locator(f, k=16), SO.Locator(f, k=48)
+    e1, lc1, i1 = L1.locate(P, return_info=True)
+    e2, lc2 = L2.locate(P)
+    assert np.array_equal(e1, e2) and np.array_equal(lc1, lc2)
+    e3 = np.concatenate([L1.locate(P[:, :1000])[0], L1.locate(P[:, 1000:])[0]])
+    assert np.array_equal(e1, e3)
+    assert i1['nlost'] == 0 and i1['nties'] >= 1000

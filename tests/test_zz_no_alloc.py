@@ -62,23 +62,43 @@ def test_noalloc_matches_existing_entry_point(case):
             assert np.abs(got - ref).max() <= TOL * np.abs(V).max(), (monotonic, wght)
 
 
-def test_noalloc_reserves_no_device_memory(case):
-    """After the first call (which looks up the scratch address) further calls leave the device's
-    free memory unchanged."""
+def _free_bytes():
     import torch
-    w, dm = case
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
+def test_noalloc_reserves_no_device_memory(built_lib):
+    """On a freshly created handle, the first call and the ones after it leave the device's free
+    memory unchanged: the scratch array is committed when the handle is created. The device-wide
+    free figure can move with other processes, so a change below the 2 MiB granularity of a device
+    allocation is tolerated and a mismatch is re-read a few times; torch's own pool must not move."""
+    import time
+    import torch
+    from m3tet_sph_gb300 import stokes, workloads
+    w = workloads.make_workload('c1')
     nel = w['levels'][0]['nel']
     els, lc = _points(nel, 4096, 11)
     els_d, lc_d = torch.from_numpy(els).cuda(), torch.from_numpy(lc).cuda()
     V_d = torch.from_numpy(np.ascontiguousarray(w['T'])).cuda()
     out_d = torch.empty(len(els), dtype=torch.float64, device='cuda')
-    _noalloc(dm, els_d, lc_d, V_d, out_d, 1, 1)
-    torch.cuda.synchronize()
-    free0 = torch.cuda.mem_get_info()[0]
-    for _ in range(3):
-        _noalloc(dm, els_d, lc_d, V_d, out_d, 1, 1)
-    torch.cuda.synchronize()
-    assert torch.cuda.mem_get_info()[0] == free0
+    dm = stokes.DeviceMesh(w['levels'])
+    try:
+        reserved0 = torch.cuda.memory_reserved()
+        free0 = _free_bytes()
+        drop = None
+        for attempt in range(4):
+            for _ in range(3):
+                _noalloc(dm, els_d, lc_d, V_d, out_d, 1, 1)
+            drop = free0 - _free_bytes()
+            if drop < 2 << 20:
+                break
+            time.sleep(0.5)
+            free0 = _free_bytes()
+        assert drop < 2 << 20, f"free device memory fell by {drop} bytes across allocation-free calls"
+        assert torch.cuda.memory_reserved() == reserved0
+    finally:
+        dm.close()
 
 
 def test_noalloc_rejects_meshes_beyond_its_scratch(built_lib):
