@@ -10,13 +10,15 @@ solve from P = 0 until the coupled FP64 residual is below 1e-8.
 Arms:
   default (--impl gb300): FP32 V-cycle with the learned element smoother (one learned sweep per side
       on the two finest levels, weights trained on the 130k-DOF shell; weighted Jacobi below) inside
-      FP64 outer CG / Patera on the GPU (libm3sph.so); `value` is its solve time. The plain-FP64 GPU
-      path (FP64 V-cycle) and the same FP32 solve with weighted-Jacobi smoothing are timed on the
-      same inputs for the comparison (--skip-learned makes the Jacobi solve the timed one);
-      semi-Lagrangian rates are measured on the 130k-DOF shell (RK4 + cubic step, 16M-point
-      location sweep).
-  --impl reference: the FP64 CPU oracle (numpy/scipy restatement of the reference algorithm) on
-      the host cores, on a bounded sample of the same workload, extrapolated to one solve.
+      FP64 outer CG / Patera on the GPU (libm3sph.so); `value` is its solve time. Beside it, on the
+      same GPU: the plain-FP64 path and the Jacobi-smoothed FP32 solve of the same shell; the same
+      three solves on the 130k-DOF shell next to the FP64 oracle's full solve of it on the host
+      (`c1`); on the 64M-DOF shell (`c5`) one learned and one plain-FP64 solve to 1e-8 and
+      device-resident time steps (rock_prop -> Stokes -> calculate_dt -> semi-Lagrangian
+      advection); semi-Lagrangian rates on the 130k-DOF shell.
+  --impl reference: the FP64 CPU oracle (numpy/scipy restatement of the reference algorithm with
+      OpenMP sparse products on all host threads): one step = one full solve of the 130k-DOF shell
+      (set-up + Patera / MG-PCG to a 1e-8 coupled residual), timed, not extrapolated.
 
 Prints one JSON line. Multi-GPU runs are independent replicas (the solve does not shard).
 """
@@ -136,6 +138,13 @@ TRAFFIC_PER_ELEMENT_F32 = (948.76e6 + 20.05e6 + 83.85e6 + 4.28e6) / 491520
 TRAFFIC_PER_ELEMENT_DF = (1.900e9 + 72.74e6 + 190.52e6 + 10.03e6) / 491520
 
 
+def algorithmic_apply_bytes(nel, ndof, nvnod, s):
+    """Algorithmic bytes of one matrix-free operator application y = K x (the per-unit figure of
+    the hot-path scope): x read and y written in the vector precision s, 10 int32 connectivity
+    entries and a class byte per element, (theta, phi, r) and log-viscosity of every vertex."""
+    return 2 * s * ndof + 40 * nel + nel + (24 + 8) * nvnod
+
+
 def apply_bytes_df(nel, ndof):
     """Algorithmic bytes of one double-float outer apply: two FP32 packed matrices per element,
     connectivity, x read and y written in FP64."""
@@ -159,8 +168,11 @@ def run_gb300(args, rank, ws, td):
     t_mesh = time.time() - t0
     lv0 = w["levels"][0]
     nel, ndof = lv0["nel"], 3 * lv0["nnod"]
+    nvnod = int(lv0["EL2NOD"][:, :4].max()) + 1
     dm = stokes.DeviceMesh(w["levels"], device=dev)
     torch.cuda.set_device(dev)
+    wfile = ROOT / "m3tet_sph_gb300" / "smoother_c1.npy"
+    use_learned = not args.skip_learned
 
     def setup(prec):
         dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=prec)
@@ -170,7 +182,7 @@ def run_gb300(args, rank, ws, td):
     if not args.skip_plain:
         setup(0)
         for _ in range(args.plain_warmup):
-            info64 = dm.step_device(**SOLVER_KW)
+            dm.step_device(**SOLVER_KW)
         barrier(td)
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -183,72 +195,60 @@ def run_gb300(args, rank, ws, td):
     # ---- the product: FP32 V-cycle with the learned element smoother (one learned sweep per
     # side on the two finest levels) inside FP64 outer CG / Patera; timed region ----
     setup(1)
-    wfile = ROOT / "m3tet_sph_gb300" / "smoother_c1.npy"
-    use_learned = not args.skip_learned
     if use_learned:
         from m3tet_sph_gb300 import learned as LS
         LS.set_params(dm, np.load(wfile), trained=True)
         dm.set_option("ml_schedule", 1)
     sm = 1 if use_learned else 0
     stream = torch.cuda.ExternalStream(dm.stream())
-
-    def timed(smoother, warmup, steps, clk=None):
-        for _ in range(warmup):
-            dm.step_device(smoother=smoother, **SOLVER_KW)
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        n0 = _lib.launch_count()
-        barrier(td)
-        torch.cuda.synchronize()
-        with (clk if clk is not None else _Null()):
-            ev0.record(stream)
-            infos = [dm.step_device(smoother=smoother, **SOLVER_KW) for _ in range(steps)]
-            ev1.record(stream)
-            ev1.synchronize()
-        return ev0.elapsed_time(ev1) / steps, infos, _lib.launch_count() - n0
+    timed = make_timed(dm, stream, td, _lib)
 
     # the same FP32 solve with weighted-Jacobi smoothing (reported beside the product)
     jac = None
     if use_learned and not args.skip_jacobi:
-        ms_j, infos_j, _ = timed(0, 1, args.steps)
+        ms_j, infos_j, _ = timed(0, 1, min(args.steps, args.jacobi_steps))
         lj = infos_j[-1]
         jac = {"s_per_solve": allmax(td, ms_j) / 1e3, "nitU": lj["nitU"], "nitZ": lj["nitZ"], "itPat": lj["itPat"],
-               "rel_residual": lj["rel_residual"]}
+               "rel_residual": lj["rel_residual"], "solves_timed": len(infos_j)}
     clk = ClockSampler(clock_csv_path())
     ms, infos, launches = timed(sm, args.warmup, args.steps, clk)
     accuracy = None
     if plain is not None:
         Um, Pm = dm.solution()
-        Pc, Pc64 = Pm - Pm.mean(), P64 - P64.mean()
-        accuracy = {"dU_rel_l2_vs_plain_fp64": float(np.linalg.norm(Um - U64) / np.linalg.norm(U64)),
-                    "dP_rel_l2_vs_plain_fp64": float(np.linalg.norm(Pc - Pc64) / np.linalg.norm(Pc64))}
+        accuracy = solution_distance(Um, Pm, U64, P64)
+        if accuracy["dU_rel_l2_vs_plain_fp64"] > TARGET or accuracy["dP_rel_l2_vs_plain_fp64"] > TARGET:
+            raise SystemExit(f"learned + FP32-MG solution differs from the plain FP64 one by more than 1e-8: {accuracy}")
     ms = allmax(td, ms)
     clocks = clk.summary(dev)
     last = infos[-1]
-    # ---- operator rooflines: the finest-level FP32 apply (phase 1 k_stream_elem_f32 + phase 2
-    # k_node_gather_f32) and the double-float outer apply, both timed with CUDA events ----
+    # ---- operator rooflines: the double-float outer apply (the largest share of the learned solve)
+    # and the finest-level FP32 apply, timed with CUDA events on the library's stream ----
     ms_apply32 = dm.apply_timing(0, 1, 10)
     ms_apply_df = dm.apply_timing(0, 2, 10)
     hbm, peak_kind = peaks()
+    alg_df = algorithmic_apply_bytes(nel, ndof, nvnod, 8)
+    alg_32 = algorithmic_apply_bytes(nel, ndof, nvnod, 4)
     b32 = apply_bytes(nel, ndof, 4)
-    achieved = b32 / (ms_apply32 * 1e-3) / 1e9
-    # dominant kernel: with the learned smoother (2 finest FP32 applies per iteration) the one
-    # double-float outer apply per iteration takes the largest share; with Jacobi (6 FP32 applies
-    # per iteration) the FP32 apply does
     bdf = apply_bytes_df(nel, ndof)
     fp32 = {"kernel": "finest-level FP32 apply: k_stream_elem_f32 + k_node_gather_f32",
-            "achieved": achieved, "frac": achieved / hbm, "traffic": TRAFFIC_PER_ELEMENT_F32 * nel,
-            "bytes_per_apply": b32, "ms_per_apply": ms_apply32, "dof_per_s": ndof / (ms_apply32 * 1e-3)}
+            "bytes_per_apply": alg_32, "achieved": alg_32 / (ms_apply32 * 1e-3) / 1e9,
+            "traffic": TRAFFIC_PER_ELEMENT_F32 * nel, "ms_per_apply": ms_apply32, "dof_per_s": ndof / (ms_apply32 * 1e-3),
+            "stored_matrix": {"bytes_per_apply": b32, "achieved": b32 / (ms_apply32 * 1e-3) / 1e9}}
     df = {"kernel": "finest-level double-float outer apply: k_stream_rowlane<RlDF> + k_node_gather_f64",
-          "achieved": bdf / (ms_apply_df * 1e-3) / 1e9, "traffic": TRAFFIC_PER_ELEMENT_DF * nel,
-          "bytes_per_apply": bdf, "ms_per_apply": ms_apply_df, "dof_per_s": ndof / (ms_apply_df * 1e-3)}
-    df["frac"] = df["achieved"] / hbm
+          "bytes_per_apply": alg_df, "achieved": alg_df / (ms_apply_df * 1e-3) / 1e9,
+          "traffic": TRAFFIC_PER_ELEMENT_DF * nel, "ms_per_apply": ms_apply_df, "dof_per_s": ndof / (ms_apply_df * 1e-3),
+          "stored_matrix": {"bytes_per_apply": bdf, "achieved": bdf / (ms_apply_df * 1e-3) / 1e9}}
+    for k in (fp32, df):
+        k["frac"] = k["achieved"] / hbm
+        k["stored_matrix"]["frac"] = k["stored_matrix"]["achieved"] / hbm
     top, other = (df, fp32) if use_learned else (fp32, df)
     roofline = {"bound": "hbm", **top, "peak": hbm, "unit": "GB/s", "peak_kind": peak_kind,
+                "bytes_basis": "algorithmic bytes of a matrix-free apply (x, y, connectivity, class byte, vertex "
+                               "coordinates and viscosity); stored_matrix adds the resident element matrices it streams",
                 "traffic_source": "ncu dram__bytes_read+write of both kernels on the 491,520-element shell, "
                                   "scaled by element count",
                 "other_apply": other,
-                "fp64_apply_ms": fp64_apply_ms if plain else None,
-                "fp64_apply_gbs": apply_bytes(nel, ndof, 8) / (fp64_apply_ms * 1e-3) / 1e9 if plain else None}
+                "fp64_apply_ms": fp64_apply_ms if plain else None}
     learned = None
     if use_learned:
         learned = {"schedule": "one learned sweep per side on levels 0 and 1 (ml_schedule 1)",
@@ -258,7 +258,7 @@ def run_gb300(args, rank, ws, td):
                    "weights": "trained on the 130,662-DOF shell, 20 viscosity fields (contrast 1e2-1e5), ~2M pairs"}
     # ---- end-to-end through the public API with host buffers ----
     U = np.empty(ndof)
-    P = np.zeros(lv0["EL2NOD"][:, :4].max() + 1)
+    P = np.zeros(nvnod)
     t_e2e, einfo = None, {"rel_residual": None}
     if not args.skip_e2e:
         te = time.perf_counter()
@@ -269,10 +269,6 @@ def run_gb300(args, rank, ws, td):
     h2d = (w["visc"].nbytes + w["dens"].nbytes + 4 * len(w["ifix"]) + w["vfix"].nbytes + P.nbytes)
     d2h = U.nbytes + P.nbytes
     dm.close()
-    # ---- CPU baseline (rank 0, N=1): oracle on a bounded sample ----
-    cpu = None
-    if rank == 0 and ws == 1 and not args.skip_cpu:
-        cpu = cpu_baseline(w, plain["info"] if plain else last, args)
     out = {
         "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
@@ -300,13 +296,145 @@ def run_gb300(args, rank, ws, td):
                 "rel_residual": einfo["rel_residual"]},
         "gpu_launches": int(launches),
         "clocks": clocks,
-        "cpu_baseline": cpu,
         "mesh_build_s": t_mesh,
     }
+    # ---- the 130k-DOF shell: GPU solves beside the oracle's full CPU solve (rank 0, N=1) ----
+    if rank == 0 and not args.skip_c1:
+        out["c1"] = c1_leg(args, wfile)
+    out["cpu_baseline"] = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        out["cpu_baseline"] = cpu_baseline(args)
+        if out.get("c1"):
+            out["c1"]["cpu_oracle_s"] = out["cpu_baseline"]["value"]
+            out["c1"]["cpu_over_gpu_learned"] = out["cpu_baseline"]["value"] / out["c1"]["learned_fp32_s"]
     if rank == 0 and not args.skip_sl:
         out["advection"] = sl_rates(args)
+    if rank == 0 and not args.skip_c5:
+        out["c5"] = c5_leg(args, wfile)
     if rank == 0:
         print(json.dumps(out))
+
+
+def make_timed(dm, stream, td, _lib):
+    """Solve timer: warm-up solves, then `steps` device-resident solves bracketed by a barrier, a
+    synchronize and CUDA events on the library's stream."""
+    import torch
+
+    def timed(smoother, warmup, steps, clk=None):
+        for _ in range(warmup):
+            dm.step_device(smoother=smoother, **SOLVER_KW)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = _lib.launch_count()
+        barrier(td)
+        torch.cuda.synchronize()
+        with (clk if clk is not None else _Null()):
+            ev0.record(stream)
+            infos = [dm.step_device(smoother=smoother, **SOLVER_KW) for _ in range(steps)]
+            ev1.record(stream)
+            ev1.synchronize()
+        return ev0.elapsed_time(ev1) / steps, infos, _lib.launch_count() - n0
+    return timed
+
+
+def solution_distance(U, P, Uref, Pref):
+    Pc, Pcr = P - P.mean(), Pref - Pref.mean()
+    return {"dU_rel_l2_vs_plain_fp64": float(np.linalg.norm(U - Uref) / np.linalg.norm(Uref)),
+            "dP_rel_l2_vs_plain_fp64": float(np.linalg.norm(Pc - Pcr) / np.linalg.norm(Pcr))}
+
+
+def c1_leg(args, wfile):
+    """The 130,662-DOF shell (level 3 x 8 layers, 3 MG levels), the configuration the reference
+    runs on its CPU: learned + FP32-MG, Jacobi FP32-MG and plain FP64 solves to the 1e-8 coupled
+    residual, each the mean of 3 device-resident solves after one warm-up."""
+    import torch
+    from m3tet_sph_gb300 import _lib, learned as LS, stokes, workloads
+    w = workloads.make_workload("c1", seed=args.seed)
+    dm = stokes.DeviceMesh(w["levels"])
+    out = {"workload": "shell L3 x 8 layers, 30720 P2 tets, 130662 velocity DOF, 3 MG levels, isoviscous, free slip"}
+    try:
+        stream = torch.cuda.ExternalStream(dm.stream())
+        timed = make_timed(dm, stream, None, _lib)
+        dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=0)
+        ms, infos, _ = timed(0, 1, 3)
+        U64, P64 = dm.solution()
+        out["plain_fp64_s"] = ms / 1e3
+        dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
+        ms, infos, _ = timed(0, 1, 3)
+        out["jacobi_fp32_s"] = ms / 1e3
+        LS.set_params(dm, np.load(wfile), trained=True)
+        ms, infos, _ = timed(1, 1, 3)
+        out["learned_fp32_s"] = ms / 1e3
+        out["learned_rel_residual"] = infos[-1]["rel_residual"]
+        out["learned_its"] = infos[-1]["nitU"] + infos[-1]["nitZ"]
+        out.update(solution_distance(*dm.solution(), U64, P64))
+    finally:
+        dm.close()
+    return out
+
+
+def c5_leg(args, wfile):
+    """The 64M-DOF shell (level 6 x 64 layers, 15,728,640 curved P2 tets, 63,406,854 velocity DOF,
+    1e6 viscosity contrast x30 below 660 km, 12 plate caps): one learned + FP32-MG solve and one
+    plain-FP64 solve to the 1e-8 coupled residual, their distance, then device-resident time steps
+    (rock_prop -> Stokes at the reference's default tolerances -> calculate_dt -> PC2 + cubic
+    semi-Lagrangian advection of T) with each path."""
+    from m3tet_sph_gb300 import learned as LS, stokes, workloads
+    t0 = time.time()
+    w = workloads.make_workload("c5", seed=args.seed)
+    f = w["levels"][0]
+    dm = stokes.DeviceMesh(w["levels"])
+    t_mesh = time.time() - t0
+    nnod = f["nnod"]
+    out = {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {f['nel']} P2 tets, {3 * nnod} velocity DOF, "
+                       f"{w['nmg']} MG levels, eta contrast 1e6 x30 jump, 12 plate caps",
+           "mesh_build_s": t_mesh}
+    params = np.load(wfile)
+    rock = workloads.rock_params(1e6)
+    step_kw = dict(rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20)
+    try:
+        def setup(prec):
+            dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=prec)
+            if prec == 1:
+                LS.set_params(dm, params, trained=True)
+                dm.set_option("ml_schedule", 1)
+        setup(1)
+        il = dm.step_device(smoother=1, **SOLVER_KW)
+        Ul, Pl = dm.solution()
+        out["learned_fp32"] = {"s": (il["t_setup_ms"] + il["t_iter_ms"]) / 1e3, "its": il["nitU"] + il["nitZ"],
+                               "itPat": il["itPat"], "rel_residual": il["rel_residual"],
+                               "fallbacks": il["smoother_fallbacks"]}
+        if not args.c5_skip_plain:
+            setup(0)
+            ip = dm.step_device(**SOLVER_KW)
+            Up, Pp = dm.solution()
+            out["plain_fp64"] = {"s": (ip["t_setup_ms"] + ip["t_iter_ms"]) / 1e3, "its": ip["nitU"] + ip["nitZ"],
+                                 "itPat": ip["itPat"], "rel_residual": ip["rel_residual"]}
+            out["speedup_learned_vs_plain"] = out["plain_fp64"]["s"] / out["learned_fp32"]["s"]
+            out["accuracy"] = solution_distance(Ul, Pl, Up, Pp)
+        steps = {}
+        for name, prec, n in (("learned_fp32", 1, args.c5_steps), ("plain_fp64", 0, args.c5_plain_steps)):
+            if n <= 0:
+                continue
+            setup(prec)
+            dm.set_temperature(workloads.DT_K * w["T"])
+            infos = [dm.time_step(step_kw, slm=dict(method_BT="PC2", method_interp="cubic"), rock=rock,
+                                  smoother=prec, dt_adv_limit=0.005, dtmax=0.1) for _ in range(n)]
+            t_st = sum(i["t_stokes_ms"] for i in infos) / 1e3
+            t_ad = sum(i["t_advect_ms"] for i in infos) / 1e3
+            steps[name] = {"steps": n, "s_per_step": sum(i["t_total_ms"] for i in infos) / 1e3 / n,
+                           "stokes_solves_per_s": n / t_st, "departure_points_per_s": n * nnod / t_ad,
+                           "its_per_step": [i["stokes"]["nitU"] + i["stokes"]["nitZ"] for i in infos],
+                           "dt": [i["dt"] for i in infos], "locate_nties": sum(i["locate"]["nties"] for i in infos),
+                           "locate_ngap": sum(i["locate"]["ngap"] for i in infos),
+                           "locate_nlost": sum(i["locate"]["nlost"] for i in infos)}
+        if steps:
+            out["time_steps"] = steps
+            if "learned_fp32" in steps and "plain_fp64" in steps:
+                out["time_steps"]["solves_per_s_learned_over_plain"] = (steps["learned_fp32"]["stokes_solves_per_s"]
+                                                                        / steps["plain_fp64"]["stokes_solves_per_s"])
+    finally:
+        dm.close()
+    return out
 
 
 class _Null:
@@ -394,72 +522,34 @@ def run_operator_only(args, rank):
                           "gbs": None if b is None else b / (ms * 1e-3) / 1e9}))
 
 
-def cpu_baseline(w, gpu_info, args):
-    """FP64 oracle timed on the host: element matrices of a contiguous slice of the benchmark mesh
-    (scaled to all elements) plus MG-PCG iterations on the 3-level 130k-DOF shell (scaled per DOF
-    and by the iteration count the plain-FP64 GPU solve needed on the benchmark mesh)."""
-    from concurrent.futures import ThreadPoolExecutor
+def cpu_solve_c1(seed, nthreads):
+    """One full solve of the 130,662-DOF shell by the FP64 oracle on the host: element matrices,
+    assembly, rotation, Galerkin hierarchy and coarse Cholesky (StokesSystem), then Patera / MG-PCG
+    to the 1e-8 coupled residual with the sparse products on `nthreads` host threads. Returns
+    (seconds, info)."""
     from oracle import stokes_oracle as O
     from m3tet_sph_gb300 import workloads
-    lv0 = w["levels"][0]
-    nel = lv0["nel"]
-    S = args.cpu_sample_els
-    nth = host_threads()
-    # element matrices: the sample split into one block per host thread (numpy releases the GIL
-    # in its array kernels), like the reference's element blocks over MATLAB's worker threads
-    subs = [submesh(lv0, blk) for blk in np.array_split(np.arange(S), nth)]
-    with ThreadPoolExecutor(nth) as pool:
-        t = time.perf_counter()
-        list(pool.map(lambda sb: O.element_matrices(sb, w["visc"][sb["gnodes"]], w["dens"][sb["gnodes"]],
-                                                    **w["phys"]), subs))
-        t_el = (time.perf_counter() - t) / S
-    c1 = workloads.make_workload("c1", seed=args.seed)
-    sysm = O.StokesSystem(c1["levels"], c1["visc"], c1["dens"], c1["ifix"], c1["vfix"], c1["phys"])
-    # sparse products on threads only where that makes an MG-PCG iteration faster on this host (it
-    # depends on whether the installed scipy releases the GIL in its CSR product, and on other
-    # threads competing for the cores): time two iterations both ways
-    nth_mg, t_ser, t_thr = 1, None, None
-    if nth > 1:
-        bt = np.random.default_rng(1).standard_normal(len(sysm.ifree))
-        its = lambda: sysm.mg.solve(bt, np.zeros_like(bt), rtol=1e-30, itmax=2)
-        t_ser = best_time(its, reps=2)
-        sysm.mg.use_threads(nth)
-        t_thr = best_time(its, reps=2)
-        if t_thr < 0.95 * t_ser:
-            nth_mg = nth
-        else:
-            sysm.mg.use_serial()
-    rng = np.random.default_rng(0)
-    b = rng.standard_normal(len(sysm.ifree))
+    w = workloads.make_workload("c1", seed=seed)
     t = time.perf_counter()
-    _, it, _ = sysm.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=args.cpu_iters)
-    t_it = (time.perf_counter() - t) / it
-    nU1 = 3 * c1["levels"][0]["nnod"]
-    nU2 = 3 * lv0["nnod"]
-    iters = gpu_info["nitU"] + gpu_info["nitZ"]
-    est = t_el * nel + t_it * (nU2 / nU1) * iters
-    return {"value": est, "unit": "s", "cores": nth, "kind": "port",
-            "sample": f"oracle element matrices of {S} of {nel} elements of this mesh ({t_el * 1e3:.3f} ms/el) + "
-                      f"{it} MG-PCG iterations on the 130,662-DOF shell ({t_it:.2f} s/it; sparse products on "
-                      f"{nth_mg} thread(s){thr_note(t_ser, t_thr, nth)}) scaled by DOF x {iters} iterations of "
-                      f"the plain-FP64 solve"}
+    S = O.StokesSystem(w["levels"], w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"])
+    S.mg.use_threads(nthreads)
+    U, P, info = O.patera(S, target_rel_residual=TARGET, **{k: v for k, v in SOLVER_KW.items()
+                                                             if k != "target_rel_residual"})
+    t = time.perf_counter() - t
+    info = dict(info, rel_residual=float(S.residual(U, P)))
+    return t, info
 
 
-def best_time(f, reps=5):
-    """Shortest of `reps` timed calls of f (after one untimed call)."""
-    f()
-    best = float("inf")
-    for _ in range(reps):
-        t = time.perf_counter()
-        f()
-        best = min(best, time.perf_counter() - t)
-    return best
-
-
-def thr_note(t_ser, t_thr, nth):
-    if t_ser is None:
-        return ""
-    return f"; two iterations {t_ser:.2f} s on 1 thread, {t_thr:.2f} s on {nth}"
+def cpu_baseline(args):
+    """The FP64 oracle's full solve of the 130,662-DOF shell, timed on the host threads (not scaled
+    or extrapolated)."""
+    nth = host_threads()
+    t, info = cpu_solve_c1(args.seed, nth)
+    return {"value": t, "unit": "s", "cores": nth, "kind": "port",
+            "sample": f"one full FP64 oracle solve of the 130,662-DOF shell (set-up + Patera/MG-PCG to a "
+                      f"{info['rel_residual']:.1e} coupled residual, {info['nitU'] + info['nitZ']} MG-PCG iterations; "
+                      f"sparse products on {nth} OpenMP threads)",
+            "workload": "shell L3 x 8 layers, 30720 P2 tets, 130662 velocity DOF, 3 MG levels"}
 
 
 def host_threads():
@@ -470,37 +560,29 @@ def host_threads():
         return max(1, os.cpu_count() or 1)
 
 
-def submesh(lv, els):
-    """Elements `els` of a level with their nodes renumbered (for bounded oracle samples)."""
-    from m3tet_sph_gb300 import mesh as M
-    EL = lv["EL2NOD"][els]
-    g, inv = np.unique(EL, return_inverse=True)
-    iso_mask = np.isin(lv["els_iso"], els)
-    iso_new = np.searchsorted(els, lv["els_iso"][iso_mask]) if iso_mask.any() else np.zeros(0, np.int64)
-    return {"EL2NOD": inv.reshape(EL.shape), "GCOORD": lv["GCOORD"][:, g], "GCOORD_SPH": lv["GCOORD_SPH"][:, g],
-            "cls": lv["cls"][els], "els_iso": iso_new, "cubic_sph_rot": lv["cubic_sph_rot"][iso_mask],
-            "gnodes": g, "PointID": lv["PointID"][g]}
-
-
 def run_reference(args, rank, ws, td):
-    """CPU reference arm: the FP64 oracle on all host threads it can use, bounded per step."""
+    """CPU reference arm: the FP64 oracle restating the reference algorithm, on all host threads.
+    One step = one full solve of the 130,662-DOF shell (set-up included), timed."""
     if rank != 0:
         return
-    from m3tet_sph_gb300 import workloads
-    w = workloads.make_workload(args.workload, seed=args.seed)
-    fake_info = {"nitU": args.ref_iters // 2, "nitZ": args.ref_iters - args.ref_iters // 2}
+    nth = host_threads()
     for _ in range(args.warmup):
-        cpu_baseline(w, fake_info, argparse.Namespace(**{**vars(args), "cpu_sample_els": 2000, "cpu_iters": 1}))
-    vals = []
+        cpu_solve_c1(args.seed, nth)
+    ts, info = [], None
     for _ in range(args.steps):
-        vals.append(cpu_baseline(w, fake_info, args))
-    v = float(np.mean([c["value"] for c in vals]))
+        t, info = cpu_solve_c1(args.seed, nth)
+        ts.append(t)
+    v = float(np.mean(ts))
+    sample = (f"one full FP64 oracle solve per step of the 130,662-DOF shell (set-up + Patera/MG-PCG to a "
+              f"{info['rel_residual']:.1e} coupled residual, {info['nitU'] + info['nitZ']} MG-PCG iterations; sparse "
+              f"products on {nth} OpenMP threads)")
     out = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic", "impl": "reference",
-           "config": {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {w['levels'][0]['nel']} P2 tets"},
-           "cpu_baseline": {"value": v, "unit": "s", "cores": vals[-1]["cores"], "kind": "port",
-                            "sample": vals[-1]["sample"]},
+           "config": {"workload": "shell L3 x 8 layers, 30720 P2 tets, 130662 velocity DOF, 3 MG levels "
+                                  "(the configuration the reference runs on its CPU; the GPU arm reports its own "
+                                  "solves of this shell under c1)"},
+           "cpu_baseline": {"value": v, "unit": "s", "cores": nth, "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -518,11 +600,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--cpu-sample-els", type=int, default=20000)
-    ap.add_argument("--cpu-iters", type=int, default=3)
-    ap.add_argument("--ref-iters", type=int, default=988,
-                    help="MG-PCG iterations the reference arm charges per solve (nitU + nitZ of the "
-                         "plain-FP64 GPU solve of the 8M-DOF shell)")
+    ap.add_argument("--skip-c1", action="store_true", help="skip the GPU solves of the 130k-DOF shell")
+    ap.add_argument("--skip-c5", action="store_true", help="skip the 64M-DOF shell")
+    ap.add_argument("--c5-skip-plain", action="store_true", help="64M-DOF shell: no plain-FP64 1e-8 solve")
+    ap.add_argument("--c5-steps", type=int, default=3, help="64M-DOF time steps with the learned + FP32-MG solve")
+    ap.add_argument("--c5-plain-steps", type=int, default=1, help="64M-DOF time steps with the plain FP64 solve")
+    ap.add_argument("--jacobi-steps", type=int, default=3, help="timed Jacobi-smoothed comparison solves")
     ap.add_argument("--skip-learned", action="store_true", help="time the Jacobi-smoothed FP32 solve instead")
     ap.add_argument("--skip-jacobi", action="store_true", help="skip the Jacobi-smoothed comparison solve")
     ap.add_argument("--skip-e2e", action="store_true")

@@ -175,11 +175,30 @@ typedef struct m3sph_rock_params {
 M3SPH_API int m3sph_rock_prop(m3sph_mesh *mesh, const m3sph_rock_params *p, const double *T, double *Visc,
                               double *Dens);
 
+/* Thermal diffusion of diffusion3d_p (diffusion3d_p.m:1-121) with the reference's default element
+ * options (default_numerics_M3TET.m:94-121): linear elements on the 8-child split of every P2
+ * tetrahedron (tetmesh_p2_to_p1), double-Jacobian integrals with 4 points per element
+ * (assembly_diffusion_3d_double_jacobian.m), lumped capacity, theta scheme, the temperature of
+ * nodes ifix (1-based, TBC.ifix) prescribed to vfix, Jacobi-preconditioned CG (pcg_solver_p.m). */
+typedef struct m3sph_diffusion_opts {
+  double kappa;       /* PHYSICS.kappa (0: diffusion is skipped) */
+  double theta;       /* OPTS_D.theta: 1 implicit Euler (the default), 0.5 Crank-Nicolson */
+  double tol;         /* OPTS_D.tol, relative to the initial residual (<= 0: 1e-8) */
+  int32_t itmax;      /* OPTS_D.itmax (<= 0: 500) */
+  double theta_cone;  /* MESH.theta_cone in degrees for the split elements' classes (<= 0: 45) */
+} m3sph_diffusion_opts;
+M3SPH_API int m3sph_diffusion_setup(m3sph_mesh *mesh, const m3sph_diffusion_opts *opts, const int32_t *ifix,
+                                    const double *vfix, int32_t nfix);
+/* Replaces diffusion3d_p(T,kappa,MESH,COMM,SETTINGS,TBC,dt): T (nnod) diffused over dt in place;
+ * *nit receives the CG iterations (may be NULL). */
+M3SPH_API int m3sph_diffusion3d(m3sph_mesh *mesh, double *T, double dt, int32_t *nit);
+
 /* One time step of the reference's loop (M3TET_SPH_SOUTH_ATLANTIC_PLUME.m:213-296) on device-
  * resident fields: rock_prop (optional) -> flow3d_patera_sph (operator rebuild from the resident
  * viscosity/density and the boundary conditions of the last m3sph_stokes_setup, Patera solve
- * warm-started from the previous step's pressure) -> calculate_dt -> advect3d_slm_p_sph of the
- * resident temperature in the new velocity (search guesses carried between steps as WS_SLM).
+ * warm-started from the previous step's pressure) -> calculate_dt -> thermal_advdiff_3d_p of the
+ * resident temperature: optional diffusion half step, advect3d_slm_p_sph in the new velocity (search
+ * guesses carried between steps as WS_SLM), optional diffusion half step.
  * No counterpart call in the reference, whose loop calls the functions one by one from MATLAB. */
 typedef struct m3sph_step_opts {
   m3sph_opts stokes;          /* solver options (precision must match the set-up's) */
@@ -188,6 +207,8 @@ typedef struct m3sph_step_opts {
   m3sph_rock_params rock;
   double dt_adv_limit;        /* SETTINGS.dt_adv_limit (calculate_dt.m) */
   double dtmax;               /* SETTINGS.dtmax */
+  int32_t diffusion;          /* 1: diffusion half steps of dt/2 before and after the advection
+                                 (thermal_advdiff_3d_p.m:13-18,46-51) with m3sph_diffusion_setup's state */
 } m3sph_step_opts;
 
 typedef struct m3sph_step_info {
@@ -197,6 +218,8 @@ typedef struct m3sph_step_info {
   double time;                /* model time after the step */
   double t_rock_ms, t_stokes_ms, t_dt_ms, t_advect_ms, t_total_ms;
   int32_t status;
+  double t_diffusion_ms;      /* both diffusion half steps (inside t_advect_ms) */
+  int32_t diffusion_its;      /* CG iterations of both half steps */
 } m3sph_step_info;
 
 /* Upload the temperature T (nnod) that the time steps advect (and restart the step counter, the
@@ -204,6 +227,11 @@ typedef struct m3sph_step_info {
 M3SPH_API int m3sph_set_temperature(m3sph_mesh *mesh, const double *T, double time);
 M3SPH_API int m3sph_get_temperature(m3sph_mesh *mesh, double *T);
 M3SPH_API int m3sph_time_step(m3sph_mesh *mesh, const m3sph_step_opts *opts, m3sph_step_info *info);
+/* The resident nodal viscosity and density (VAR.Visc, VAR.Dens: nnod each; either may be NULL), for
+ * output and restart files (write_output_file.m, write_restart_file.m). */
+M3SPH_API int m3sph_get_properties(m3sph_mesh *mesh, double *Visc, double *Dens);
+/* Resume from a restart file: the pressure (nvnod) the next solve or time step starts from. */
+M3SPH_API int m3sph_set_pressure(m3sph_mesh *mesh, const double *P);
 
 /* Learned element smoother (no counterpart in the reference: M3TET_SPH smooths with weighted
  * Jacobi only). A 52-128-30 MLP (BF16 tensor cores, FP32 accumulation) replaces Jacobi sweeps on
@@ -305,6 +333,13 @@ M3SPH_API int m3sph_level_apply(m3sph_mesh *mesh, int32_t img, const double *x, 
 /* The FP32 operator of level img as used inside the V-cycle (streamed element apply on the finest
  * level, assembled blocks on coarse levels); needs a set-up with precision 1. */
 M3SPH_API int m3sph_level_apply32(m3sph_mesh *mesh, int32_t img, const float *x, float *y);
+/* Replaces intermesh_transfer_matrix(GCOORD,EL2NOD,GCOORD_c,EL2NOD_c,1) (intermesh_transfer_matrix.m:
+ * 1-62) for levels img (fine) and img+1: the scalar Ic2f (nnod(img) x nnod(img+1)) as 1-based
+ * (row, col, value) triplets of the handle's transfer operator, ready for MATLAB's sparse(). Call
+ * with rows/cols/vals NULL to get *nnz, then with arrays of that size. The vector form for ndof = 3
+ * is kron(Ic2f, eye(3)). */
+M3SPH_API int m3sph_transfer_matrix(const m3sph_mesh *mesh, int32_t img, int64_t *nnz, int32_t *rows, int32_t *cols,
+                                    double *vals);
 /* Ic2f{img} (intermesh_transfer_matrix): prolong x_c (3*nnod(img+1)) -> x_f (3*nnod(img)) and
  * restrict r_f -> r_c with Ic2f' (free-dof masked as in restrict_stiffmat.m:94-96). */
 M3SPH_API int m3sph_prolong(m3sph_mesh *mesh, int32_t img, const double *xc, double *xf);

@@ -68,16 +68,21 @@ class RockParams(C.Structure):
                                           "minDens", "maxDens", "minVisc", "maxVisc")]
 
 
+class DiffusionOpts(C.Structure):
+    _fields_ = [("kappa", C.c_double), ("theta", C.c_double), ("tol", C.c_double), ("itmax", C.c_int32),
+                ("theta_cone", C.c_double)]
+
+
 class StepOpts(C.Structure):
     _fields_ = [("stokes", Opts), ("slm", SlmOpts), ("rock_prop", C.c_int32), ("rock", RockParams),
-                ("dt_adv_limit", C.c_double), ("dtmax", C.c_double)]
+                ("dt_adv_limit", C.c_double), ("dtmax", C.c_double), ("diffusion", C.c_int32)]
 
 
 class StepInfo(C.Structure):
     _fields_ = [("stokes", Info), ("locate", LocateInfo), ("dt", C.c_double), ("dt_adv", C.c_double),
                 ("time", C.c_double), ("t_rock_ms", C.c_double), ("t_stokes_ms", C.c_double),
                 ("t_dt_ms", C.c_double), ("t_advect_ms", C.c_double), ("t_total_ms", C.c_double),
-                ("status", C.c_int32)]
+                ("status", C.c_int32), ("t_diffusion_ms", C.c_double), ("diffusion_its", C.c_int32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -106,6 +111,7 @@ SIGNATURES = {
     "m3sph_element_matrices": ([P, DP, DP, DP], C.c_int),
     "m3sph_level_apply32": ([P, C.c_int32, P, P], C.c_int),
     "m3sph_level_apply": ([P, C.c_int32, DP, DP], C.c_int),
+    "m3sph_transfer_matrix": ([P, C.c_int32, C.POINTER(C.c_int64), IP, IP, DP], C.c_int),
     "m3sph_prolong": ([P, C.c_int32, DP, DP], C.c_int),
     "m3sph_restrict": ([P, C.c_int32, DP, DP], C.c_int),
     "m3sph_vcycle": ([P, DP, DP], C.c_int),
@@ -113,9 +119,13 @@ SIGNATURES = {
     "m3sph_solution": ([P, DP, DP], C.c_int),
     "m3sph_calculate_dt": ([P, C.c_double, C.c_double, DP, DP], C.c_int),
     "m3sph_rock_prop": ([P, C.POINTER(RockParams), DP, DP, DP], C.c_int),
+    "m3sph_diffusion_setup": ([P, C.POINTER(DiffusionOpts), IP, DP, C.c_int32], C.c_int),
+    "m3sph_diffusion3d": ([P, DP, C.c_double, IP], C.c_int),
     "m3sph_set_temperature": ([P, DP, C.c_double], C.c_int),
     "m3sph_get_temperature": ([P, DP], C.c_int),
     "m3sph_time_step": ([P, C.POINTER(StepOpts), C.POINTER(StepInfo)], C.c_int),
+    "m3sph_get_properties": ([P, DP, DP], C.c_int),
+    "m3sph_set_pressure": ([P, DP], C.c_int),
     "m3sph_stream": ([P, C.POINTER(P)], C.c_int),
     "m3sph_tsearch_sph": ([P, DP, C.c_int32, IP, IP, DP, C.POINTER(LocateInfo)], C.c_int),
     "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),

@@ -182,6 +182,8 @@ int slm_advect_resident(m3sph_mesh *M, const double *U_soa, double *T, double dt
 int stokes_velocity_soa(m3sph_mesh *M, double *dst);
 int stokes_resident_solve(m3sph_mesh *M, const m3sph_opts *opts, bool zero_p, m3sph_info &inf);
 int stokes_calc_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv);
+int diffusion_resident(m3sph_mesh *M, double *T, double dt, int *nit);
+int stokes_set_pressure(m3sph_mesh *M, const double *P);
 int ml_build(m3sph_mesh *M);
 int ml_features(m3sph_mesh *M, const double *h_visc);
 template <typename T> int ml_sweep(m3sph_mesh *M, int j, const T *r0, const T *kd, const T *Dinv, T *tmp, T *d);
@@ -241,6 +243,8 @@ struct m3sph_mesh {
   double *Usoa = nullptr;             // [3][nnod] Cartesian velocity handed to the advection
   long long ts_steps = 0;             // time steps taken since the temperature was set
   double ts_time = 0.0;               // model time accumulated by the time steps
+  void *diff = nullptr;               // thermal-diffusion state
+  void (*diff_free)(void *) = nullptr;
   void *slm = nullptr;                // advection / point-location state
   void (*slm_free)(void *) = nullptr;
   double *red = nullptr;              // reduction partials

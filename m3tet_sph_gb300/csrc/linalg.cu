@@ -330,6 +330,21 @@ __global__ void k_dense_assemble(const T *__restrict__ K, const int *__restrict_
     if (gr != gc) atomicAdd(&A[(size_t)gc * n + gr], v);
   }
 }
+// dense matrix from the level's 3x3-block rows (blocks [9][nnzb]): every entry is written once, so
+// the result does not depend on the order in which threads run
+template <typename T>
+__global__ void k_dense_from_bsr(const int *__restrict__ ptr, const int *__restrict__ col, const T *__restrict__ B,
+                                 int nrow, size_t nnzb, int n, T *__restrict__ A) {
+  const int i = blockIdx.x;
+  if (i >= nrow) return;
+  for (int k = ptr[i] + threadIdx.x; k < ptr[i + 1]; k += blockDim.x) {
+    const int j = col[k];
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) A[(size_t)(3 * i + p) * n + 3 * j + q] = B[(size_t)(p * 3 + q) * nnzb + k];
+  }
+}
 template <typename T>
 __global__ void k_dense_fix_diag(T *A, const uint8_t *mask, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -359,10 +374,14 @@ __global__ void k_gj_update(T *A, int n, int k, const T *colk, const T *rowk) {
   A[(size_t)i * n + j] = v;
 }
 template <typename T>
-int dense_inverse(const Level &L, const T *K, T *A, T *work, cudaStream_t s) {
+int dense_inverse(const Level &L, const T *K, const T *B, T *A, T *work, cudaStream_t s) {
   const int n = L.ndof;
   M3_CUDA(cudaMemsetAsync(A, 0, sizeof(T) * (size_t)n * n, s));
-  k_dense_assemble<T><<<L.nel, 128, 0, s>>>(K, L.el2nod, L.nel, n, A); count_launch();
+  if (B)
+    k_dense_from_bsr<T><<<L.nnod, 64, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, (size_t)L.nnzb, n, A);
+  else
+    k_dense_assemble<T><<<L.nel, 128, 0, s>>>(K, L.el2nod, L.nel, n, A);
+  count_launch();
   k_dense_fix_diag<T><<<(n + 255) / 256, 256, 0, s>>>(A, L.freemask, n); count_launch();
   T *colk = work, *rowk = work + n;
   dim3 g((n + 255) / 256, n);
@@ -373,8 +392,8 @@ int dense_inverse(const Level &L, const T *K, T *A, T *work, cudaStream_t s) {
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
-template int dense_inverse<double>(const Level &, const double *, double *, double *, cudaStream_t);
-template int dense_inverse<float>(const Level &, const float *, float *, float *, cudaStream_t);
+template int dense_inverse<double>(const Level &, const double *, const double *, double *, double *, cudaStream_t);
+template int dense_inverse<float>(const Level &, const float *, const float *, float *, float *, cudaStream_t);
 
 // y = A x masked (one warp per row)
 template <typename T>

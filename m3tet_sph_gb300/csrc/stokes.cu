@@ -61,7 +61,7 @@ template <typename T> int jac_first(T w, const T *r0, const T *Di, T *d, size_t 
 template <typename T> int jac(T w, const T *r0, const T *Kd, const T *Di, T *d, size_t n, cudaStream_t s);
 template <typename T> int restrict_(const Level &F, const Level &C, const T *a, const T *b, T *out, cudaStream_t s);
 template <typename T> int prolong(const Level &F, const Level &C, const T *xc, const T *add, T *out, cudaStream_t s);
-template <typename T> int dense_inverse(const Level &L, const T *K, T *A, T *work, cudaStream_t s);
+template <typename T> int dense_inverse(const Level &L, const T *K, const T *B, T *A, T *work, cudaStream_t s);
 template <typename T> int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s);
 size_t element_setup_smem();
 
@@ -447,6 +447,7 @@ extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
   clear_graphs(M);
   if (M->wk && M->wk_free) M->wk_free(M->wk);
   if (M->slm && M->slm_free) M->slm_free(M->slm);
+  if (M->diff && M->diff_free) M->diff_free(M->diff);
   if (M->ml && M->ml_free) M->ml_free(M->ml);
   if (M->stream) cudaStreamDestroy(M->stream);
   delete M;
@@ -746,10 +747,10 @@ static int rebuild_operator(m3sph_mesh *M) {
   if (M->nmg > 1) {
     if (M->precision == 0) {
       if (!M->coarse.A64) M3_TRY(dalloc(&M->coarse.A64, (size_t)nc * nc));
-      M3_TRY(dense_inverse<double>(Lc, Lc.K64, M->coarse.A64, W->cwork64, s));
+      M3_TRY(dense_inverse<double>(Lc, Lc.K64, Lc.B64, M->coarse.A64, W->cwork64, s));
     } else {
       if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
-      M3_TRY(dense_inverse<float>(Lc, Lc.K32, M->coarse.A32, W->cwork32, s));
+      M3_TRY(dense_inverse<float>(Lc, Lc.K32, Lc.B32, M->coarse.A32, W->cwork32, s));
     }
   }
   return M3SPH_OK;
@@ -1516,6 +1517,12 @@ int stokes_resident_solve(m3sph_mesh *M, const m3sph_opts *opts, bool zero_p, m3
   return st;
 }
 int stokes_calc_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv);
+int stokes_set_pressure(m3sph_mesh *M, const double *P) {
+  Work *W = get_work(M);
+  M3_CUDA(cudaMemcpyAsync(W->pP, P, sizeof(double) * M->lev[0].nvnod, cudaMemcpyHostToDevice, M->stream));
+  M3_CUDA(cudaStreamSynchronize(M->stream));
+  return M3SPH_OK;
+}
 }  // namespace m3sph
 
 extern "C" int m3sph_calculate_dt(m3sph_mesh *M, double dt_adv_limit, double dtmax, double *dt, double *dt_adv) {
@@ -1711,6 +1718,39 @@ extern "C" int m3sph_ml_sweep32(m3sph_mesh *M, int32_t img, const float *r, cons
   M3_CUDA(cudaMemcpyAsync(d, W->d32[img], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
   return ml_check(M);
+}
+
+extern "C" int m3sph_transfer_matrix(const m3sph_mesh *M, int32_t img, int64_t *nnz, int32_t *rows, int32_t *cols,
+                                     double *vals) {
+  if (!M || !nnz || img < 0 || img + 1 >= M->nmg) {
+    set_error("m3sph_transfer_matrix: bad arguments or level out of range");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  const Level &F = M->lev[img];
+  std::vector<int> ptr(F.nnod + 1);
+  M3_CUDA(cudaMemcpy(ptr.data(), F.P_ptr, sizeof(int) * ptr.size(), cudaMemcpyDeviceToHost));
+  const int64_t n = ptr[F.nnod];
+  if (!rows || !cols || !vals) {   // first call: the number of entries
+    *nnz = n;
+    return M3SPH_OK;
+  }
+  if (*nnz < n) {
+    set_error("m3sph_transfer_matrix: arrays hold fewer entries than the matrix has");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  std::vector<int> col(n);
+  std::vector<float> w(n);
+  M3_CUDA(cudaMemcpy(col.data(), F.P_col, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  M3_CUDA(cudaMemcpy(w.data(), F.P_w, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < F.nnod; ++i)
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      rows[k] = i + 1;
+      cols[k] = col[k] + 1;
+      vals[k] = (double)w[k];   // multiples of 1/8: exact in FP32
+    }
+  *nnz = n;
+  return M3SPH_OK;
 }
 
 extern "C" int m3sph_prolong(m3sph_mesh *M, int32_t img, const double *xc, double *xf) {

@@ -4,6 +4,8 @@
 // 24 B of coordinates read, 16 B written per node). The time step chains the hot-path calls of the
 // reference's time loop (M3TET_SPH_SOUTH_ATLANTIC_PLUME.m:213-296) without leaving the device:
 // rock_prop -> Stokes (operator rebuild + Patera) -> calculate_dt -> semi-Lagrangian advection.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <string>
 
@@ -133,6 +135,30 @@ extern "C" int m3sph_get_temperature(m3sph_mesh *M, double *T) {
   return M3SPH_OK;
 }
 
+extern "C" int m3sph_get_properties(m3sph_mesh *M, double *Visc, double *Dens) {
+  if (!M || !M->have_operator) {
+    set_error("m3sph_get_properties: call m3sph_stokes_setup first");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  const size_t n = M->lev[0].nnod;
+  if (Visc) M3_CUDA(cudaMemcpyAsync(Visc, M->fin.visc, n * sizeof(double), cudaMemcpyDeviceToHost, M->stream));
+  if (Dens) M3_CUDA(cudaMemcpyAsync(Dens, M->fin.dens, n * sizeof(double), cudaMemcpyDeviceToHost, M->stream));
+  M3_CUDA(cudaStreamSynchronize(M->stream));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_set_pressure(m3sph_mesh *M, const double *P) {
+  if (!M || !P || !M->have_operator) {
+    set_error("m3sph_set_pressure: call m3sph_stokes_setup first");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  M3_TRY(stokes_set_pressure(M, P));
+  M->ts_steps = std::max<long long>(M->ts_steps, 1);   // the next time step starts from this pressure
+  return M3SPH_OK;
+}
+
 extern "C" int m3sph_time_step(m3sph_mesh *M, const m3sph_step_opts *o, m3sph_step_info *info) {
   if (!M || !o) {
     set_error("m3sph_time_step: bad arguments");
@@ -169,11 +195,24 @@ extern "C" int m3sph_time_step(m3sph_mesh *M, const m3sph_step_opts *o, m3sph_st
   // CALCULATE TIME STEP
   M3_TRY(stokes_calc_dt(M, o->dt_adv_limit, o->dtmax, &inf.dt, &inf.dt_adv));
   M3_CUDA(cudaEventRecord(ev[3], s));
-  // THERMAL ADVECTION in the new velocity
+  // THERMAL ADVECTION-DIFFUSION in the new velocity (thermal_advdiff_3d_p.m)
+  double t_diff = 0.0;
+  auto half_step = [&](void) -> int {
+    if (!o->diffusion) return M3SPH_OK;
+    const auto h0 = std::chrono::steady_clock::now();
+    int it = 0;
+    const int r = diffusion_resident(M, M->T, 0.5 * inf.dt, &it);
+    inf.diffusion_its += it;
+    t_diff += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
+    return r;
+  };
+  M3_TRY(half_step());
   M3_TRY(stokes_velocity_soa(M, M->Usoa));
   M3_TRY(slm_advect_resident(M, M->Usoa, M->T, inf.dt, &o->slm, M->ts_steps == 0, &inf.locate));
+  M3_TRY(half_step());
   M3_CUDA(cudaEventRecord(ev[4], s));
   M3_CUDA(cudaEventSynchronize(ev[4]));
+  inf.t_diffusion_ms = t_diff;
   M3_TRY(elapsed(ev[0], ev[1], inf.t_rock_ms));
   M3_TRY(elapsed(ev[1], ev[2], inf.t_stokes_ms));
   M3_TRY(elapsed(ev[2], ev[3], inf.t_dt_ms));

@@ -130,6 +130,18 @@ class DeviceMesh:
         L.check(L.lib().m3sph_level_apply32(self.h, img, L.fptr(x), L.fptr(y)))
         return y
 
+    def transfer_matrix(self, img):
+        """intermesh_transfer_matrix of levels img -> img+1 as a scipy CSR matrix (scalar Ic2f)."""
+        import scipy.sparse as sp
+        nnz = C.c_int64()
+        L.check(L.lib().m3sph_transfer_matrix(self.h, img, C.byref(nnz), None, None, None))
+        r = np.empty(nnz.value, np.int32)
+        c = np.empty(nnz.value, np.int32)
+        v = np.empty(nnz.value)
+        L.check(L.lib().m3sph_transfer_matrix(self.h, img, C.byref(nnz), L.iptr(r), L.iptr(c), L.dptr(v)))
+        return sp.csr_matrix((v, (r - 1, c - 1)), shape=(self.levels[img]['GCOORD'].shape[1],
+                                                          self.levels[img + 1]['GCOORD'].shape[1]))
+
     def prolong(self, img, xc):
         y = np.empty(3 * self.levels[img]['GCOORD'].shape[1])
         L.check(L.lib().m3sph_prolong(self.h, img, L.dptr(np.ascontiguousarray(xc, dtype=np.float64)), L.dptr(y)))
@@ -207,6 +219,15 @@ class DeviceMesh:
         L.check(L.lib().m3sph_rock_prop(self.h, C.byref(rp), L.dptr(T), L.dptr(V), L.dptr(D)))
         return V, D
 
+    def properties(self):
+        """Resident (Visc, Dens), nnod each."""
+        V, D = np.empty(self.nnod), np.empty(self.nnod)
+        L.check(L.lib().m3sph_get_properties(self.h, L.dptr(V), L.dptr(D)))
+        return V, D
+
+    def set_pressure(self, P):
+        L.check(L.lib().m3sph_set_pressure(self.h, L.dptr(np.ascontiguousarray(P, dtype=np.float64))))
+
     def set_temperature(self, T, time=0.0):
         L.check(L.lib().m3sph_set_temperature(self.h, L.dptr(np.ascontiguousarray(T, dtype=np.float64)), float(time)))
 
@@ -215,8 +236,23 @@ class DeviceMesh:
         L.check(L.lib().m3sph_get_temperature(self.h, L.dptr(T)))
         return T
 
+    def diffusion_setup(self, kappa, ifix, vfix, theta=1.0, tol=1e-8, itmax=500, theta_cone=45.0):
+        """Thermal diffusion state (diffusion3d_p's operator): ifix 0-based node ids of TBC."""
+        o = L.DiffusionOpts(kappa=float(kappa), theta=float(theta), tol=float(tol), itmax=int(itmax),
+                            theta_cone=float(theta_cone))
+        fx = np.ascontiguousarray(np.asarray(ifix, dtype=np.int32) + 1)
+        vf = np.ascontiguousarray(vfix, dtype=np.float64)
+        L.check(L.lib().m3sph_diffusion_setup(self.h, C.byref(o), L.iptr(fx), L.dptr(vf), len(fx)))
+
+    def diffusion(self, T, dt):
+        """diffusion3d_p on the GPU: (T diffused over dt, CG iterations)."""
+        T = np.ascontiguousarray(T, dtype=np.float64).copy()
+        nit = C.c_int32()
+        L.check(L.lib().m3sph_diffusion3d(self.h, L.dptr(T), float(dt), C.byref(nit)))
+        return T, nit.value
+
     def time_step(self, stokes_kw=None, slm=None, rock=None, dt_adv_limit=0.005, dtmax=0.1, smoother=0,
-                  r_cmb=3480.0, r_surf=6371.0, allow_not_converged=False):
+                  r_cmb=3480.0, r_surf=6371.0, diffusion=False, allow_not_converged=False):
         """One device-resident time step (rock_prop if `rock` is given -> Stokes -> calculate_dt ->
         semi-Lagrangian advection of the resident T). Returns the step info as a dict."""
         kw = dict(rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20, target_rel_residual=0.0)
@@ -233,6 +269,7 @@ class DeviceMesh:
             o.rock = rock_params_struct(rock)
         o.dt_adv_limit = dt_adv_limit
         o.dtmax = dtmax
+        o.diffusion = 1 if diffusion else 0
         info = L.StepInfo()
         code = L.lib().m3sph_time_step(self.h, C.byref(o), C.byref(info))
         return self._finish(code, info.as_dict(), allow_not_converged)
@@ -310,3 +347,16 @@ def rock_prop(VAR, PHYSICS, NUMSCALE, MESH, SETTINGS=None):
     VAR = dict(VAR)
     VAR['Visc'], VAR['Dens'] = dm.rock_prop(VAR['T'], p)
     return VAR
+
+
+def diffusion3d_p(T, kappa, MESH, COMM, SETTINGS, TBC, dt):
+    """Mirror of diffusion3d_p.m:1 (T = diffusion3d_p(T,kappa,MESH,COMM,SETTINGS,TBC,dt)) on the GPU
+    with the default element options; TBC: dict with 'ifix' (1-based nodes) and 'vfix'."""
+    dm = MESH.get('device_mesh')
+    if dm is None:
+        dm = DeviceMesh(MESH['levels'])
+        MESH['device_mesh'] = dm
+    D = (SETTINGS or {}).get('OPTS_D', {})
+    dm.diffusion_setup(kappa, np.asarray(TBC['ifix']) - 1, TBC['vfix'], theta=D.get('theta', 1.0),
+                       tol=D.get('tol', 1e-8), itmax=D.get('itmax', 500))
+    return dm.diffusion(T, dt)[0]

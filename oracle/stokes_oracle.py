@@ -341,27 +341,43 @@ class CoarseChol:
         self.c = sla.cho_factor(K.toarray() if sp.issparse(K) else K, lower=True)
 
     def solve(self, r):
-        return sla.cho_solve(self.c, r)
+        return sla.cho_solve(self.c, r, check_finite=False)
 
 
-class ThreadedCSR:
-    """y = A @ x with the rows of a CSR matrix split into one block per thread. The reference's own
-    product (mgpcg_solver_p.m:728-733, MUTILS spmv) runs on several threads the same way; each row
-    is still summed in the same order, so the result is bit-identical to ``A @ x``."""
+class OmpCSR:
+    """y = A @ x on `nthreads` host threads through the oracle's OpenMP product (oracle/csr_omp.c).
+    The reference's own product (mgpcg_solver_p.m:728-733, MUTILS spmv) is multi-threaded too. Each
+    row is summed in the same order with separate multiply and add, so the result is bit-identical
+    to scipy's ``A @ x``."""
 
-    def __init__(self, A, pool, nthreads):
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            import ctypes as C
+            from oracle import build_oracle
+            L = C.CDLL(str(build_oracle.build()))
+            L.csr_matvec.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+            L.csr_matvec.restype = None
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, A, nthreads):
         A = A.tocsr()
+        A.sort_indices()
         self.shape = A.shape
-        self.bounds = np.linspace(0, A.shape[0], nthreads + 1).astype(np.int64)
-        self.blocks = [A[self.bounds[i]:self.bounds[i + 1]] for i in range(nthreads)]
-        self.pool = pool
+        self.ptr = np.ascontiguousarray(A.indptr, dtype=np.int64)
+        self.col = np.ascontiguousarray(A.indices, dtype=np.int32)
+        self.val = np.ascontiguousarray(A.data, dtype=np.float64)
+        self.nthreads = int(nthreads)
+        self.lib()
 
     def __matmul__(self, x):
-        y = np.empty(self.shape[0], dtype=np.result_type(self.blocks[0].dtype, x.dtype))
-
-        def one(i):
-            y[self.bounds[i]:self.bounds[i + 1]] = self.blocks[i] @ x
-        list(self.pool.map(one, range(len(self.blocks))))
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.shape[0])
+        self._lib.csr_matvec(self.shape[0], self.ptr.ctypes.data, self.col.ctypes.data, self.val.ctypes.data,
+                             x.ctypes.data, y.ctypes.data, self.nthreads)
         return y
 
 
@@ -382,14 +398,13 @@ class MGPCG:
 
     def use_threads(self, nthreads):
         """Run the sparse products on `nthreads` host threads (the CPU baseline's timing mode)."""
-        from concurrent.futures import ThreadPoolExecutor
-        pool = ThreadPoolExecutor(nthreads)
         if not hasattr(self, "_serial"):
             self._serial = (self.K1, list(self.KK), list(self.P), list(self.PT))
-        self.K1 = ThreadedCSR(self.K1, pool, nthreads)
-        self.KK = [self.KK[0]] + [ThreadedCSR(K, pool, nthreads) for K in self.KK[1:]]
-        self.PT = [ThreadedCSR(P.T, pool, nthreads) for P in self.P]
-        self.P = [ThreadedCSR(P, pool, nthreads) for P in self.P]
+        K1, KK, P = self._serial[0], self._serial[1], self._serial[2]
+        self.K1 = OmpCSR(K1, nthreads)
+        self.KK = [KK[0]] + [OmpCSR(K, nthreads) for K in KK[1:]]
+        self.PT = [OmpCSR(p.T, nthreads) for p in P]
+        self.P = [OmpCSR(p, nthreads) for p in P]
 
     def use_serial(self):
         """Back to the serial products after use_threads."""
@@ -529,8 +544,11 @@ class StokesSystem:
 
 
 def patera(sysm, P0=None, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmax_U=20, itmin_Pat=3,
-           verbose=False):
-    """Patera pressure CG around MG-PCG (flow3d_patera_mg_sph_p.m:386-632)."""
+           verbose=False, target_rel_residual=0.0):
+    """Patera pressure CG around MG-PCG (flow3d_patera_mg_sph_p.m:386-632). With a target coupled
+    residual (the library's extension): when the pressure tolerance is met but the coupled FP64
+    residual is above the target, both tolerances are cut by 10, the velocity is solved for the
+    current pressure, the pressure residual is replaced by the true -G'U and CG restarts."""
     s = sysm
     ifree = s.ifree
     nU = s.nU
@@ -587,6 +605,17 @@ def patera(sysm, P0=None, rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmax_U=20,
         if verbose:
             print(itPat, norm_rP, nit)
         if norm_rP < tol_Pat and itPat >= itmin_Pat:
+            if target_rel_residual > 0 and s.residual(U, P) > target_rel_residual:
+                tol_Pat *= 0.1
+                rtol_U *= 0.1
+                tol_U_restart = rtol_U * tol_Pat
+                Rhs = (s.Fb + s.GG @ P - s.bc_rhs)[ifree]
+                U[ifree], nit, _ = s.mg.solve(Rhs, U[ifree], tol=tol_U_restart, itmax=itmax_U)
+                info['nitU'] += nit
+                r = rm0space(-(s.GG.T @ U))
+                norm_rP = normdf(r)
+                restart = True
+                continue
             break
         if norm_rP < rtol_restart * norm_rP0 or norm_rP > 10 * norm_rP0:
             Rhs = (s.Fb + s.GG @ P - s.bc_rhs)[ifree]

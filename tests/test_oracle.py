@@ -127,3 +127,21 @@ def test_locator_independent_of_batch_and_neighbour_count():
     e3 = np.concatenate([L1.locate(P[:, :1000])[0], L1.locate(P[:, 1000:])[0]])
     assert np.array_equal(e1, e3)
     assert i1['nlost'] == 0 and i1['nties'] >= 1000
+
+
+def test_diffusion_oracle_identities(tiny):
+    """Conductivity rows sum to zero (constants do not diffuse); the capacities add up to the shell
+    volume times 6 (ip_tetrahedron's weights sum to 1, not to the reference tetrahedron's 1/6, in
+    both matrices alike); the implicit step keeps a constant field."""
+    import numpy as np
+    from m3tet_sph_gb300 import mesh as M
+    from oracle import thermal_oracle as TO
+    f = tiny['levels'][0]
+    EL1 = M.split_p2(f['GCOORD'], f['EL2NOD'])[0]
+    fix = np.nonzero(f['PointID'] > 0)[0]
+    D = TO.Diffusion(f['GCOORD'], f['GCOORD_SPH'], EL1, 31.6, fix)
+    assert np.abs(np.asarray(D.C.sum(axis=1))).max() < 1e-12 * np.abs(D.C).max()
+    vol = 4.0 / 3.0 * np.pi * (6371.0 ** 3 - 3480.0 ** 3)
+    assert abs(D.ML.sum() / (6 * vol) - 1) < 2e-2
+    T, nit = D.step(np.full(f['nnod'], 5.0), 100.0, np.full(len(fix), 5.0))
+    assert np.abs(T - 5.0).max() < 1e-12

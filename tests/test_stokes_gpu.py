@@ -271,3 +271,16 @@ def test_streamed_fp32_variants_bit_identical(built_lib):
             dm2.set_option("stream_f32_variant", 0)
     finally:
         dm2.close()
+
+
+def test_transfer_matrix_equals_oracle(case):
+    """m3sph_transfer_matrix returns intermesh_transfer_matrix's Ic2f (intermesh_transfer_matrix.m:
+    1-62) as the oracle builds it from the straight-edged coordinates of both levels."""
+    w, S, dm = case
+    lv = w['levels']
+    Xs_c = O.p2_straight(lv[1]['GCOORD'], lv[1]['EL2NOD'])
+    Xs_f = O.straight_coords(Xs_c, lv[0]['EL2NOD'])
+    ref = O.intermesh_transfer_matrix(Xs_f, lv[0]['EL2NOD'], Xs_c, lv[1]['EL2NOD'])
+    got = dm.transfer_matrix(0)
+    assert got.shape == ref.shape
+    assert abs(got - ref).max() < 1e-15

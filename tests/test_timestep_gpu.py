@@ -60,9 +60,11 @@ def _setup(dm, w, visc, dens, precision):
 
 
 def test_time_step_equals_the_calls_one_by_one(plates):
-    """Two device-resident steps give bit-identical temperature, time step and velocity to the same
-    hot-path calls made one by one through the C ABI with host arrays (rock_prop, stokes_setup +
-    stokes_solve from the previous pressure, calculate_dt, advect_slm with the WS_SLM guesses)."""
+    """Two device-resident steps give the temperature, time step and velocity of the same hot-path
+    calls made one by one through the C ABI with host arrays (rock_prop, stokes_setup + stokes_solve
+    from the previous pressure, calculate_dt, advect_slm with the WS_SLM guesses). They agree to
+    rounding rather than bit for bit: the element set-up sums the right-hand side of the nonzero
+    prescribed velocities with shared-memory atomics, whose order varies between set-ups."""
     from m3tet_sph_gb300 import advection as A, stokes, workloads
     w = plates
     rock = workloads.rock_params(1e3)
@@ -84,11 +86,14 @@ def test_time_step_equals_the_calls_one_by_one(plates):
             _setup(dm2, w, V, D, 1)
             U, P, info = dm2.solve(P0=P, **kw)
             dt, adv = dm2.calculate_dt(0.01, 50.0)
-            assert dt == steps[k]['dt'] and adv == steps[k]['dt_adv']
+            assert dt == pytest.approx(steps[k]['dt'], rel=1e-12)
+            assert adv == pytest.approx(steps[k]['dt_adv'], rel=1e-12)
             T, WS = A.advect3d_slm_p_sph(MESH, None, U[0::3], U[1::3], U[2::3], T, dt,
                                          dict(method_BT='PC2', method_interp='cubic'), WS)
-        assert np.array_equal(U, U_dev) and np.array_equal(P, P_dev)
-        assert np.array_equal(T, T_dev)
+            assert np.array_equal(WS['els_INTERP'] > 0, np.ones(len(T), bool))
+        assert np.linalg.norm(U - U_dev) <= 1e-12 * np.linalg.norm(U)
+        assert np.linalg.norm((P - P.mean()) - (P_dev - P_dev.mean())) <= 1e-12 * np.linalg.norm(P - P.mean())
+        assert np.max(np.abs(T - T_dev)) <= 1e-12 * np.max(np.abs(T0))
         assert steps[1]['time'] == steps[0]['dt'] + steps[1]['dt']
         for st in steps:
             assert st['status'] == 0 and st['locate']['nlost'] == 0 and st['dt'] > 0
@@ -151,3 +156,32 @@ def test_time_steps_with_learned_smoother_c1(built_lib):
         assert T.min() >= T0.min() - 1e-9 and T.max() <= T0.max() + 1e-9
     finally:
         dm.close()
+
+
+def test_restart_file_resumes_the_time_series(plates, tmp_path):
+    """Two steps in one handle; the same series written to a restart file after step 1 and resumed
+    in a fresh handle gives the same step 2 (write_restart_file.m / load_restart_data.m)."""
+    from m3tet_sph_gb300 import restart as R, stokes, workloads
+    w = plates
+    rock = workloads.rock_params(1e3)
+    kw = dict(rtol_Pat=1e-6, rtol_U=5e-3, itmax_Pat=200, itmax_U=40, target_rel_residual=1e-8)
+    T0 = 2500.0 * w['T']
+    dm, dm2 = stokes.DeviceMesh(w['levels']), stokes.DeviceMesh(w['levels'])
+    try:
+        _setup(dm, w, w['visc'], w['dens'], 1)
+        dm.set_temperature(T0)
+        s1 = dm.time_step(kw, rock=rock, dt_adv_limit=0.01, dtmax=50.0)
+        path = R.write_restart_file({'outdir': str(tmp_path)}, R.var_from_device(dm), None, 2, 1, s1['time'],
+                                    s1['dt'], 1)
+        s2 = dm.time_step(kw, rock=rock, dt_adv_limit=0.01, dtmax=50.0)
+        T2 = dm.get_temperature()
+        VAR, time, istep, iplot = R.load_restart_file(path)
+        assert time == s1['time'] and istep == 2
+        _setup(dm2, w, VAR['Visc'], VAR['Dens'], 1)
+        R.restore_device(dm2, VAR, time)
+        r2 = dm2.time_step(kw, rock=rock, dt_adv_limit=0.01, dtmax=50.0)
+        assert r2['time'] == pytest.approx(s2['time'], rel=1e-12)
+        assert np.max(np.abs(dm2.get_temperature() - T2)) <= 1e-12 * np.max(np.abs(T0))
+    finally:
+        dm.close()
+        dm2.close()
