@@ -248,6 +248,11 @@ M3SPH_API int m3sph_ml_get_params(m3sph_mesh *mesh, float *params);
  * the features of r and its local values of e. */
 M3SPH_API int m3sph_ml_reserve(m3sph_mesh *mesh, int64_t capacity);
 M3SPH_API int m3sph_ml_collect(m3sph_mesh *mesh, uint64_t seed, int32_t n_iterates, int32_t stride, int64_t *count);
+/* Append the pairs of caller vectors: residual r and error e (3*nnod each, rotated frame, fixed dofs
+ * ignored), every `stride`-th element from `offset` -- e.g. the residuals and errors of the iterates
+ * of a plain multigrid solve. */
+M3SPH_API int m3sph_ml_add_pairs(m3sph_mesh *mesh, const double *r, const double *e, int32_t stride, int32_t offset,
+                                 int64_t *count);
 /* One Adam epoch over the shuffled samples (batch a multiple of 64); mse = mean squared error. */
 M3SPH_API int m3sph_ml_train_epoch(m3sph_mesh *mesh, int32_t batch, float lr, uint64_t seed, double *mse);
 /* Gradient of the MSE loss (flat layout, same as the parameters) and forward outputs on caller
@@ -269,7 +274,10 @@ M3SPH_API int m3sph_ml_sweep32(m3sph_mesh *mesh, int32_t img, const float *r, co
  * sweep per side, default; per handle), "ml_omega_pct" (relaxation weight of the learned correction
  * in percent, 10-300, default 100; per handle), "ml_infer" (learned sweep kernels: 1 fused tcgen05 sweep, default;
  * 0 WMMA tile kernel), "stream_f32_variant" (slot-ring depth / gather warps of the streamed FP32
- * kernel, 0-3, default 0). */
+ * kernel, 0-3, default 0), "coarse_f64_direct_max" (plain FP64 path: coarsest levels up to this many
+ * dofs get an FP64 dense inverse, larger ones the FP32 inverse refined against the FP64 coarsest
+ * operator in every coarse solve; default 6000; takes effect at the next set-up), "coarse_refine_sweeps"
+ * (refinement steps of that solve, default 3). */
 M3SPH_API int m3sph_set_option(m3sph_mesh *mesh, const char *name, int32_t value);
 /* Cumulative number of CUDA kernels this library has launched (all handles). */
 M3SPH_API int m3sph_launch_count(unsigned long long *count);

@@ -138,6 +138,7 @@ SIGNATURES = {
     "m3sph_ml_reserve": ([P, C.c_int64], C.c_int),
     "m3sph_ml_collect": ([P, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_int64)], C.c_int),
     "m3sph_ml_train_epoch": ([P, C.c_int32, C.c_float, C.c_uint64, DP], C.c_int),
+    "m3sph_ml_add_pairs": ([P, DP, DP, C.c_int32, C.c_int32, C.POINTER(C.c_int64)], C.c_int),
     "m3sph_ml_gradients": ([P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float), DP], C.c_int),
     "m3sph_ml_forward": ([P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float)], C.c_int),
     "m3sph_ml_sweep32": ([P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),

@@ -156,6 +156,9 @@ struct Coarse {
   int n = 0;                          // dofs of the coarsest level
   double *A64 = nullptr;              // dense inverse (n x n)
   float *A32 = nullptr;
+  bool refine64 = false;              // FP64 path: FP32 inverse + iterative refinement against B64
+  float *B32tmp = nullptr;            // [9][nnzb] FP32 copy of the coarsest FP64 blocks (refinement)
+  double *t64 = nullptr;              // [n] refinement residual
 };
 
 struct SetupArgs {

@@ -314,22 +314,6 @@ template int prolong<float>(const Level &, const Level &, const float *, const f
 // ---------------------------------------------------------------------------------------
 // coarsest level: dense assembly, in-place Gauss-Jordan inverse (SPD, no pivoting), GEMV
 // ---------------------------------------------------------------------------------------
-template <typename T>
-__global__ void k_dense_assemble(const T *__restrict__ K, const int *__restrict__ el2nod, int nel, int n,
-                                 T *__restrict__ A) {
-  const int e = blockIdx.x;
-  for (int q = threadIdx.x; q < NPACK; q += blockDim.x) {
-    int cc = 0, rem = q;
-    while (rem >= 30 - cc) { rem -= 30 - cc; ++cc; }
-    const int rr = cc + rem;
-    const int gr = 3 * el2nod[(size_t)(rr / 3) * nel + e] + rr % 3;
-    const int gc = 3 * el2nod[(size_t)(cc / 3) * nel + e] + cc % 3;
-    const T v = K[kidx<T>(q, e, nel)];
-    if (v == T(0)) continue;
-    atomicAdd(&A[(size_t)gr * n + gc], v);
-    if (gr != gc) atomicAdd(&A[(size_t)gc * n + gr], v);
-  }
-}
 // dense matrix from the level's 3x3-block rows (blocks [9][nnzb]): every entry is written once, so
 // the result does not depend on the order in which threads run
 template <typename T>
@@ -350,50 +334,186 @@ __global__ void k_dense_fix_diag(T *A, const uint8_t *mask, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && !mask[i]) A[(size_t)i * n + i] = T(1);
 }
+// ---------------------------------------------------------------------------------------
+// blocked Gauss-Jordan inverse of the SPD coarsest matrix, 128-wide panels (no pivoting):
+// per panel k, with D = A_kk, C = A_:k (saved) and R = D^-1 A_k: :
+//   A_ij -= C_i R_j (i, j outside panel k), A_kj = R_j, A_ik = -C_i D^-1, A_kk = D^-1.
+// Three launches per panel; the rank-128 update is a 128x128-tile GEMM in shared memory with an
+// 8x8 register block per thread. The inner dimension runs in chunks of GJK(T) (32 FP32, 16 FP64)
+// so that the two staged tiles stay near 33 KB.
+// ---------------------------------------------------------------------------------------
+constexpr int GJB = 128;
+template <typename T> struct GjChunk { static constexpr int K = sizeof(T) == 4 ? 32 : 16; };
+
+// D^-1 of the nb x nb diagonal block (one CTA, unblocked Gauss-Jordan in dynamic shared memory:
+// GJB x (GJB+1) values + two pivot vectors)
 template <typename T>
-__global__ void k_gj_save(const T *A, int n, int k, T *colk, T *rowk) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const T piv = A[(size_t)k * n + k];
-  colk[i] = A[(size_t)i * n + k];
-  rowk[i] = A[(size_t)k * n + i] / piv;
+__global__ void __launch_bounds__(256) k_gjb_diag(const T *__restrict__ A, int n, int kb, int nb, T *__restrict__ Dinv) {
+  extern __shared__ __align__(16) unsigned char gj_smem[];
+  T(*a)[GJB + 1] = reinterpret_cast<T(*)[GJB + 1]>(gj_smem);
+  T *colp = reinterpret_cast<T *>(gj_smem) + GJB * (GJB + 1), *rowp = colp + GJB;
+  for (int t = threadIdx.x; t < GJB * GJB; t += blockDim.x) {
+    const int r = t / GJB, c = t % GJB;
+    a[r][c] = (r < nb && c < nb) ? A[(size_t)(kb + r) * n + kb + c] : (r == c ? T(1) : T(0));
+  }
+  __syncthreads();
+  for (int p = 0; p < GJB; ++p) {
+    if (threadIdx.x < GJB) {
+      colp[threadIdx.x] = a[threadIdx.x][p];
+      rowp[threadIdx.x] = a[p][threadIdx.x] / a[p][p];
+    }
+    __syncthreads();
+    const T piv = colp[p];
+    for (int t = threadIdx.x; t < GJB * GJB; t += blockDim.x) {
+      const int r = t / GJB, c = t % GJB;
+      T v;
+      if (r == p) v = (c == p) ? T(1) / piv : rowp[c];
+      else if (c == p) v = -colp[r] / piv;
+      else v = a[r][c] - colp[r] * rowp[c];
+      a[r][c] = v;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < GJB * GJB; t += blockDim.x) Dinv[t] = a[t / GJB][t % GJB];
 }
-template <typename T>
-__global__ void k_gj_update(T *A, int n, int k, const T *colk, const T *rowk) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y;
-  if (j >= n) return;
-  const T piv = colk[k];
-  T v;
-  if (i == k)
-    v = (j == k) ? T(1) / piv : rowk[j];
-  else if (j == k)
-    v = -colk[i] / piv;
-  else
-    v = A[(size_t)i * n + j] - colk[i] * rowk[j];
-  A[(size_t)i * n + j] = v;
+
+// 128x128 tile product acc = X (rows i0.., inner dimension 0..127) * Y (inner, cols j0..), X and Y
+// read through the loaders; 256 threads, thread (ty, tx) owns rows ty + 16a, cols tx + 16b
+template <typename T, typename LX, typename LY>
+__device__ __forceinline__ void gj_tile_mma(T (&acc)[8][8], LX loadx, LY loady) {
+  constexpr int KC = GjChunk<T>::K;
+  __shared__ T xs[GJB][KC + 1];
+  __shared__ T ys[KC][GJB + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc[a][b] = T(0);
+  for (int k0 = 0; k0 < GJB; k0 += KC) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < GJB * KC; q += blockDim.x) {
+      const int r = q / KC, m = q % KC;
+      xs[r][m] = loadx(r, k0 + m);
+      const int ym = q / GJB, c = q % GJB;
+      ys[ym][c] = loady(k0 + ym, c);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int m = 0; m < KC; ++m) {
+      T xv[8], yv[8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) xv[a] = xs[ty + 16 * a][m];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) yv[b] = ys[m][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] += xv[a] * yv[b];
+    }
+  }
 }
+
+// column panel C (n x 128, saved before the update overwrites it) and row panel R = D^-1 A_k:
+// (128 x n); block x handles columns [128x, 128x+128) of R and rows [128x, 128x+128) of C
 template <typename T>
-int dense_inverse(const Level &L, const T *K, const T *B, T *A, T *work, cudaStream_t s) {
-  const int n = L.ndof;
-  M3_CUDA(cudaMemsetAsync(A, 0, sizeof(T) * (size_t)n * n, s));
-  if (B)
-    k_dense_from_bsr<T><<<L.nnod, 64, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, (size_t)L.nnzb, n, A);
-  else
-    k_dense_assemble<T><<<L.nel, 128, 0, s>>>(K, L.el2nod, L.nel, n, A);
-  count_launch();
-  k_dense_fix_diag<T><<<(n + 255) / 256, 256, 0, s>>>(A, L.freemask, n); count_launch();
-  T *colk = work, *rowk = work + n;
-  dim3 g((n + 255) / 256, n);
-  for (int k = 0; k < n; ++k) {
-    k_gj_save<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, k, colk, rowk); count_launch();
-    k_gj_update<T><<<g, 256, 0, s>>>(A, n, k, colk, rowk); count_launch();
+__global__ void __launch_bounds__(256) k_gjb_panels(const T *__restrict__ A, int n, int kb, int nb,
+                                                    const T *__restrict__ Dinv, T *__restrict__ R, T *__restrict__ Cc) {
+  const int j0 = blockIdx.x * GJB;
+  for (int q = threadIdx.x; q < GJB * GJB; q += blockDim.x) {
+    const int r = q / GJB, c = q % GJB;
+    const int i = j0 + r;
+    if (i < n) Cc[(size_t)i * GJB + c] = c < nb ? A[(size_t)i * n + kb + c] : T(0);
+  }
+  T acc[8][8];
+  gj_tile_mma<T>(
+      acc, [&](int r, int m) { return Dinv[r * GJB + m]; },
+      [&](int m, int c) { return (m < nb && j0 + c < n) ? A[(size_t)(kb + m) * n + j0 + c] : T(0); });
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int j = j0 + tx + 16 * b;
+      if (j < n) R[(size_t)(ty + 16 * a) * n + j] = acc[a][b];
+    }
+}
+
+// the update of one 128x128 tile (by, bx): outside panel k A -= C R; row panel R; column panel
+// -C D^-1; diagonal block D^-1
+template <typename T>
+__global__ void __launch_bounds__(256) k_gjb_update(T *__restrict__ A, int n, int kblk, int nb,
+                                                    const T *__restrict__ Dinv, const T *__restrict__ R,
+                                                    const T *__restrict__ Cc) {
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  const int i0 = bi * GJB, j0 = bj * GJB, kb = kblk * GJB;
+  const bool rowk = bi == kblk, colk = bj == kblk;
+  if (rowk && colk) {
+    for (int q = threadIdx.x; q < GJB * GJB; q += blockDim.x) {
+      const int r = q / GJB, c = q % GJB;
+      if (r < nb && c < nb) A[(size_t)(kb + r) * n + kb + c] = Dinv[q];
+    }
+    return;
+  }
+  if (rowk) {
+    for (int q = threadIdx.x; q < GJB * GJB; q += blockDim.x) {
+      const int r = q / GJB, c = q % GJB;
+      if (r < nb && j0 + c < n) A[(size_t)(kb + r) * n + j0 + c] = R[(size_t)r * n + j0 + c];
+    }
+    return;
+  }
+  T acc[8][8];
+  gj_tile_mma<T>(
+      acc, [&](int r, int m) { return (i0 + r < n) ? Cc[(size_t)(i0 + r) * GJB + m] : T(0); },
+      [&](int m, int c) {
+        return colk ? -Dinv[m * GJB + c] : ((j0 + c < n) ? R[(size_t)m * n + j0 + c] : T(0));
+      });
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int i = i0 + ty + 16 * a;
+    if (i >= n) continue;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int j = j0 + tx + 16 * b;
+      if (j >= n) continue;
+      if (colk) {
+        if (j - kb < nb) A[(size_t)i * n + j] = acc[a][b];            // -C D^-1
+      } else {
+        A[(size_t)i * n + j] -= acc[a][b];                           // A - C R
+      }
+    }
+  }
+}
+
+// in-place inverse of the n x n SPD matrix A; work holds GJB*GJB + 2*GJB*n values
+template <typename T>
+int gj_blocked_inverse(T *A, int n, T *work, cudaStream_t s) {
+  T *Dinv = work, *R = work + GJB * GJB, *Cc = R + (size_t)GJB * n;
+  const int nbk = (n + GJB - 1) / GJB;
+  const size_t dsmem = sizeof(T) * ((size_t)GJB * (GJB + 1) + 2 * GJB);
+  M3_CUDA(cudaFuncSetAttribute(k_gjb_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+  for (int k = 0; k < nbk; ++k) {
+    const int kb = k * GJB, nb = std::min(GJB, n - kb);
+    k_gjb_diag<T><<<1, 256, dsmem, s>>>(A, n, kb, nb, Dinv); count_launch();
+    k_gjb_panels<T><<<nbk, 256, 0, s>>>(A, n, kb, nb, Dinv, R, Cc); count_launch();
+    k_gjb_update<T><<<dim3(nbk, nbk), 256, 0, s>>>(A, n, k, nb, Dinv, R, Cc); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
-template int dense_inverse<double>(const Level &, const double *, const double *, double *, double *, cudaStream_t);
-template int dense_inverse<float>(const Level &, const float *, const float *, float *, float *, cudaStream_t);
+
+// dense coarse matrix (from the level's block rows) and its blocked Gauss-Jordan inverse; with a
+// `lowp` target the FP64 matrix is rounded to FP32 first and A receives nothing
+template <typename T>
+int dense_inverse_blocked(const Level &L, const T *B, T *A, T *work, cudaStream_t s) {
+  const int n = L.ndof;
+  M3_CUDA(cudaMemsetAsync(A, 0, sizeof(T) * (size_t)n * n, s));
+  k_dense_from_bsr<T><<<L.nnod, 64, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, (size_t)L.nnzb, n, A); count_launch();
+  k_dense_fix_diag<T><<<(n + 255) / 256, 256, 0, s>>>(A, L.freemask, n); count_launch();
+  return gj_blocked_inverse<T>(A, n, work, s);
+}
+template int dense_inverse_blocked<double>(const Level &, const double *, double *, double *, cudaStream_t);
+template int dense_inverse_blocked<float>(const Level &, const float *, float *, float *, cudaStream_t);
 
 // y = A x masked (one warp per row)
 template <typename T>
@@ -408,6 +528,51 @@ __global__ void k_dense_gemv(const T *__restrict__ A, int n, const T *__restrict
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) y[row] = mask[row] ? s : T(0);
 }
+// y (FP64) = A (FP32) x (FP64) masked, FP64 accumulation: the refined FP64 coarse solve
+__global__ void k_dense_gemv_mixed(const float *__restrict__ A, int n, const double *__restrict__ x,
+                                   const uint8_t *__restrict__ mask, double *__restrict__ y, int accumulate) {
+  const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  for (int j = lane; j < n; j += 32) s += (double)A[(size_t)row * n + j] * x[j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[row] = mask[row] ? (accumulate ? y[row] + s : s) : 0.0;
+}
+__global__ void k_sub_masked(const double *a, const double *b, const uint8_t *mask, double *out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = mask[i] ? a[i] - b[i] : 0.0;
+}
+template <typename T> int bsr_apply(const Level &L, const T *B, const T *x, T *y, cudaStream_t s);
+
+// FP64 coarse solve d = A^-1 r from the FP32 inverse A32 and the FP64 operator B64 of the coarsest
+// level: d = A32 r, then `sweeps` steps of iterative refinement d += A32 (r - A d)
+int coarse_refined(const Level &L, const float *A32, const double *B64, const double *r, double *d, double *t,
+                   int sweeps, cudaStream_t s) {
+  const int n = L.ndof;
+  const unsigned g = (unsigned)((n + 7) / 8);
+  k_dense_gemv_mixed<<<g, 256, 0, s>>>(A32, n, r, L.freemask, d, 0); count_launch();
+  for (int k = 0; k < sweeps; ++k) {
+    M3_TRY(bsr_apply<double>(L, B64, d, t, s));
+    k_sub_masked<<<(n + 255) / 256, 256, 0, s>>>(r, t, L.freemask, t, n); count_launch();
+    k_dense_gemv_mixed<<<g, 256, 0, s>>>(A32, n, t, L.freemask, d, 1); count_launch();
+  }
+  M3_CUDA(cudaGetLastError());
+  return M3SPH_OK;
+}
+
+__global__ void k_d2f_n(const double *a, float *b, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+// FP32 inverse of the FP64 coarsest operator (its blocks rounded to FP32)
+int dense_inverse_from64(const Level &L, const double *B64, float *B32tmp, float *A, float *work, cudaStream_t s) {
+  const size_t nb = 9 * (size_t)L.nnzb;
+  k_d2f_n<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B64, B32tmp, nb); count_launch();
+  return dense_inverse_blocked<float>(L, B32tmp, A, work, s);
+}
+
 template <typename T>
 int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s) {
   k_dense_gemv<T><<<(n + 7) / 8, 256, 0, s>>>(A, n, x, mask, y); count_launch();

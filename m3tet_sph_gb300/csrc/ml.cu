@@ -27,6 +27,22 @@ constexpr int NPARAM = HID * INP + HID + OUTP * HID + OUTP;   // flat FP32 param
 constexpr int OFF_W1 = 0, OFF_B1 = HID * INP, OFF_W2 = OFF_B1 + HID, OFF_B2 = OFF_W2 + OUTP * HID;
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU with erf from Abramowitz & Stegun, Handbook of Mathematical Functions, 7.1.26:
+// erf(z) = 1 - (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5) exp(-z^2), t = 1/(1 + p z), z >= 0,
+// |error| <= 1.5e-7. With z = |x|/sqrt(2) and q = x/2 * poly(t) * exp(-x^2/2):
+// GELU(x) = x - q for x >= 0 and q for x < 0. The fused inference sweep uses it (its hidden
+// activations are rounded to BF16, 2^-8 relative, right after); training keeps erff.
+__device__ __forceinline__ float gelu_as(float x) {
+  const float z = fabsf(x) * 0.70710678118654752f;
+  const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+  float p = fmaf(1.061405429f, t, -1.453152027f);
+  p = fmaf(p, t, 1.421413741f);
+  p = fmaf(p, t, -0.284496736f);
+  p = fmaf(p, t, 0.254829592f);
+  p = p * t;
+  const float q = 0.5f * x * p * __expf(-0.5f * x * x);
+  return x >= 0.0f ? x - q : q;
+}
 __device__ __forceinline__ float gelu_grad(float x) {
   return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
@@ -480,8 +496,8 @@ __global__ void __launch_bounds__(tc::THREADS, 2) k_ml_sweep_tc(FeatLevel L, Mlp
           uint32_t gv[8];
 #pragma unroll
           for (int q = 0; q < 8; ++q)
-            gv[q] = tc_pack(gelu(h[16 * half + 2 * q] + sb1[16 * c + 2 * q]),
-                            gelu(h[16 * half + 2 * q + 1] + sb1[16 * c + 2 * q + 1]));
+            gv[q] = tc_pack(gelu_as(h[16 * half + 2 * q] + sb1[16 * c + 2 * q]),
+                            gelu_as(h[16 * half + 2 * q + 1] + sb1[16 * c + 2 * q + 1]));
           const uint32_t atom = sbase + OFF_G + (c >> 2) * ATOM;
           tc_st16(atom + tc_sw(t, 2 * (c & 3)), gv[0], gv[1], gv[2], gv[3]);
           tc_st16(atom + tc_sw(t, 2 * (c & 3) + 1), gv[4], gv[5], gv[6], gv[7]);

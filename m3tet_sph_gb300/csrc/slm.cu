@@ -49,7 +49,7 @@ struct SlmMesh {
   const double *SX;      // [3][nnod]  X-90 frame of all nodes
   const int *v2e_ptr;    // [nvnod+1]
   const int *v2e;        // vertex -> elements
-  const uint8_t *iface;  // [nel] 1 if an element sharing a vertex has another frame or iso-ness
+  const uint8_t *iface;  // [nel] bit k: face k has a vertex shared with an element of another frame or iso-ness
   const float *S0f, *SZf, *SXf;   // FP32 copies of S0, SZ, SX (the FP32 part of the walk)
   // start grid for walks without a guess: cells equal in cos(theta), phi and r
   const int *grid;       // [gnr][gnt][gnp] element id
@@ -203,16 +203,6 @@ __device__ __forceinline__ void bary_minmax(const double *lc, double &mn, double
 __device__ __forceinline__ int frame_rank(int cls) { return cls >= M3SPH_IN_CONE_NO_ISO ? 0 : (cls == 0 ? 1 : 2); }
 
 // candidate flags: bit 0 isoparametric, bits 1-2 frame rank, bit 3 point at one of its vertices
-struct CandList {
-  int n = 0, overflow = 0;
-  int id[MAX_CAND];
-  uint8_t fl[MAX_CAND];
-  __device__ void add(int e, uint8_t f) {
-    for (int k = 0; k < n; ++k)
-      if (id[k] == e) return;
-    if (n < MAX_CAND) { id[n] = e; fl[n] = f; ++n; } else overflow = 1;
-  }
-};
 
 // rule 1 over n candidates; *ambiguous: neither the iso drop nor the shared-vertex drop applied and
 // the remaining candidates span frames (the reference's error('no good'), tsearch2_sph.m:387-392)
@@ -261,7 +251,10 @@ struct GapBest {
   __device__ int pick() const { return non >= 0 ? non : iso; }
 };
 
-__device__ __forceinline__ void eval_candidate(const SlmMesh &m, int e, const PointFrames &f, CandList &C, GapBest &G) {
+// one element of a ring or of the brute-force set: a candidate (within the tie band, appended to the
+// warp's shared list; the rule does not depend on the order) or a gap contender
+__device__ __forceinline__ void eval_shared(const SlmMesh &m, int e, const PointFrames &f, int *ids, uint8_t *fl,
+                                            int *n, GapBest &G) {
   double lc[3], mn, mx;
   int am;
   const double step = local_coords(m, e, f, lc);
@@ -270,61 +263,154 @@ __device__ __forceinline__ void eval_candidate(const SlmMesh &m, int e, const Po
   const int cls = m.cls[e];
   const bool iso = cls == M3SPH_IN_CONE_ISO;
   if (need <= TIE_BAND) {
-    C.add(e, (uint8_t)((iso ? 1 : 0) | (frame_rank(cls) << 1) | (mx >= 1.0 - TIE_BAND ? 8 : 0)));
+    const int slot = atomicAdd(n, 1);
+    if (slot < MAX_CAND) {
+      ids[slot] = e;
+      fl[slot] = (uint8_t)((iso ? 1 : 0) | (frame_rank(cls) << 1) | (mx >= 1.0 - TIE_BAND ? 8 : 0));
+    }
   } else if (need <= (GAP_QMAX + 1) * GAP_STEP) {
     G.add(e, (int)ceil(need / GAP_STEP - 1e-9), iso, step);
   }
 }
 
-// Apply the rule over the elements sharing a vertex with e0 (depth 1) or with any of those
-// (depth 2, for points the walk could not place). Returns the element (or -1) and sets kind bits:
-// 2 tie, 4 gap, 32 ambiguous for the reference, 64 candidate list overflow.
-__device__ __noinline__ int resolve_ring(const SlmMesh &m, int e0, int depth, const PointFrames &f, double *lc_out, int &kind) {
-  CandList C;
+// warp reduction of the gap choice: the smallest step count, then at that count the smallest
+// non-isoparametric id and the isoparametric element of the smallest Newton step (then id)
+__device__ __forceinline__ int gap_reduce(const GapBest &G, int &q) {
+  q = G.q;
+  for (int o = 16; o > 0; o >>= 1) q = min(q, __shfl_xor_sync(0xffffffffu, q, o));
+  int non = (G.q == q) ? G.non : -1;
+  int iso_e = (G.q == q) ? G.iso : -1;
+  double iso_s = (G.q == q) ? G.iso_step : 1e300;
+  for (int o = 16; o > 0; o >>= 1) {
+    const int on = __shfl_xor_sync(0xffffffffu, non, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, iso_e, o);
+    const double os = __shfl_xor_sync(0xffffffffu, iso_s, o);
+    if (on >= 0 && (non < 0 || on < non)) non = on;
+    if (oi >= 0 && (iso_e < 0 || os < iso_s || (os == iso_s && oi < iso_e))) { iso_e = oi; iso_s = os; }
+  }
+  return non >= 0 ? non : iso_e;
+}
+
+// rule 1 / rule 2 on the warp's shared candidate list (duplicates removed first), by lane 0;
+// writes the point's element, local coordinates and status (base_status: 1 placed by a ring, 16 by
+// the brute force)
+__device__ void finish_point(const SlmMesh &m, const PointFrames &f, int i, int npt, int *ids, uint8_t *fl, int nc,
+                             int gap_e, int q, int base_status, int adjust, int *els, double *lc_out, uint8_t *status) {
+  int kind = nc > MAX_CAND ? 64 : 0;
+  nc = min(nc, MAX_CAND);
+  int u = 0;
+  for (int a = 0; a < nc; ++a) {
+    bool dup = false;
+    for (int b = 0; b < u; ++b) dup |= ids[b] == ids[a];
+    if (!dup) {
+      ids[u] = ids[a];
+      fl[u] = fl[a];
+      ++u;
+    }
+  }
+  int e = -1;
+  if (u > 0) {
+    int amb = 0;
+    e = tie_rule(ids, fl, u, &amb);
+    kind |= base_status | (u >= 2 ? 2 : 0) | (amb ? 32 : 0);
+  } else if (q <= GAP_QMAX && gap_e >= 0) {
+    e = gap_e;
+    kind |= (base_status & 16) | 4;
+  }
+  if (e < 0) {
+    status[i] = (uint8_t)(8 | (kind & 64));
+    return;
+  }
+  double lc[3];
+  local_coords(m, e, f, lc);
+  if (adjust) {   // adjust_local_coords (locate_points_interp_vars_3d_sph.m:180-198)
+    for (int k = 0; k < 3; ++k) lc[k] = fmin(fmax(lc[k], 0.0), 1.0);
+    const double sm = lc[0] + lc[1] + lc[2];
+    if (sm > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= sm;
+  }
+  els[i] = e;
+  lc_out[i] = lc[0];
+  lc_out[npt + i] = lc[1];
+  lc_out[2 * npt + i] = lc[2];
+  status[i] = (uint8_t)kind;
+}
+
+// Rules 1-2 for the points k_locate listed: one warp per point over the elements sharing a vertex
+// with the walk's element (placed points) or with any of those (points the walk could not place).
+constexpr int RING_WARPS = 8;
+constexpr int RING_VTAB = 256;   // open-addressing table of the 1-ring's vertices (2-ring search)
+__global__ void __launch_bounds__(RING_WARPS * 32) k_resolve_ring(SlmMesh m, const double *__restrict__ P, int npt,
+                                                                 const int *__restrict__ todo, int ntodo,
+                                                                 int *__restrict__ els, double *__restrict__ lc_out,
+                                                                 uint8_t *__restrict__ status, int adjust) {
+  __shared__ int s_id[RING_WARPS][MAX_CAND];
+  __shared__ uint8_t s_fl[RING_WARPS][MAX_CAND];
+  __shared__ int s_n[RING_WARPS];
+  __shared__ int s_vt[RING_WARPS][RING_VTAB];
+  const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * RING_WARPS + wl;
+  if (w >= ntodo) return;
+  const int i = todo[w];
+  const int e0 = els[i];
+  const int depth = (status[i] & 1) ? 1 : 2;
+  if (lane == 0) s_n[wl] = 0;
+  PointFrames f;
+  point_frames(P[i], P[npt + i], P[2 * npt + i], f);
+  int v0[4], len[4];
+  for (int k = 0; k < 4; ++k) {
+    v0[k] = m.el2nod[(size_t)k * m.nel + e0];
+    len[k] = m.v2e_ptr[v0[k] + 1] - m.v2e_ptr[v0[k]];
+  }
+  const int tot = len[0] + len[1] + len[2] + len[3];
   GapBest G;
+  __syncwarp();
   if (depth == 1) {
-    for (int i = 0; i < 4; ++i) {
-      const int v = m.el2nod[(size_t)i * m.nel + e0];
-      for (int k = m.v2e_ptr[v]; k < m.v2e_ptr[v + 1]; ++k) eval_candidate(m, m.v2e[k], f, C, G);
+    for (int t = lane; t < tot; t += 32) {
+      int k = 0, o = t;
+      while (o >= len[k]) o -= len[k++];
+      eval_shared(m, m.v2e[m.v2e_ptr[v0[k]] + o], f, s_id[wl], s_fl[wl], &s_n[wl], G);
     }
   } else {
-    int verts[MAX_RING_VERTS];
-    int nv = 0;
-    for (int i = 0; i < 4; ++i) {
-      const int v = m.el2nod[(size_t)i * m.nel + e0];
-      for (int k = m.v2e_ptr[v]; k < m.v2e_ptr[v + 1]; ++k) {
-        const int e1 = m.v2e[k];
-        for (int j = 0; j < 4; ++j) {
-          const int w = m.el2nod[(size_t)j * m.nel + e1];
-          bool seen = false;
-          for (int a = 0; a < nv; ++a) seen |= verts[a] == w;
-          if (!seen && nv < MAX_RING_VERTS) verts[nv++] = w;
+    // vertices of the 1-ring, deduplicated in a shared hash table (-1 = empty)
+    for (int t = lane; t < RING_VTAB; t += 32) s_vt[wl][t] = -1;
+    __syncwarp();
+    for (int t = lane; t < tot; t += 32) {
+      int k = 0, o = t;
+      while (o >= len[k]) o -= len[k++];
+      const int e1 = m.v2e[m.v2e_ptr[v0[k]] + o];
+      for (int j = 0; j < 4; ++j) {
+        const int v = m.el2nod[(size_t)j * m.nel + e1];
+        int h = (int)(((unsigned)v * 2654435761u) % RING_VTAB);
+        for (int probe = 0; probe < RING_VTAB; ++probe) {
+          const int old = atomicCAS(&s_vt[wl][h], -1, v);
+          if (old == -1 || old == v) break;
+          h = (h + 1) % RING_VTAB;
         }
       }
     }
-    for (int a = 0; a < nv; ++a)
-      for (int k = m.v2e_ptr[verts[a]]; k < m.v2e_ptr[verts[a] + 1]; ++k) eval_candidate(m, m.v2e[k], f, C, G);
+    __syncwarp();
+    for (int slot = 0; slot < RING_VTAB; ++slot) {
+      const int v = s_vt[wl][slot];
+      if (v < 0) continue;
+      for (int k = m.v2e_ptr[v] + lane; k < m.v2e_ptr[v + 1]; k += 32)
+        eval_shared(m, m.v2e[k], f, s_id[wl], s_fl[wl], &s_n[wl], G);
+    }
   }
-  int e = -1;
-  kind = C.overflow ? 64 : 0;
-  if (C.n > 0) {
-    int amb = 0;
-    e = tie_rule(C.id, C.fl, C.n, &amb);
-    kind |= (C.n >= 2 ? 2 : 0) | (amb ? 32 : 0);
-  } else {
-    e = G.pick();
-    if (e >= 0) kind |= 4;
-  }
-  if (e >= 0) local_coords(m, e, f, lc_out);
-  return e;
+  __syncwarp();
+  int q;
+  const int gap_e = gap_reduce(G, q);
+  if (lane != 0) return;
+  finish_point(m, f, i, npt, s_id[wl], s_fl[wl], s_n[wl], gap_e, q, 1, adjust, els, lc_out, status);
 }
 
-// one thread per point: walk from the guess to the containing element, then the rule above.
+// one thread per point: walk from the guess to the containing element; points that may tie and
+// points the walk could not place are listed for k_resolve_ring.
 // status bits: 1 placed, 2 tie, 4 gap (tolerance), 8 not placed yet (brute force next), 16 placed by
-// brute force, 32 ambiguous for the reference, 64 candidate list overflow
+// brute force, 32 ambiguous for the reference, 64 candidate list overflow, 128 ring resolution pending
 __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const int *__restrict__ guess,
                          const int *__restrict__ node_guess, int *__restrict__ els, double *__restrict__ lc_out,
-                         uint8_t *__restrict__ status, int adjust) {
+                         uint8_t *__restrict__ status, int adjust, int *__restrict__ ring_todo,
+                         int *__restrict__ ring_count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npt) return;
   PointFrames f;
@@ -401,29 +487,27 @@ __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const
   }
   if (found >= 0) {
     st = 1;
-    double mn, mx;
-    int am;
-    bary_minmax(lc, mn, mx, am);
-    if (mn < TIE_TRIGGER || mx > 1.0 - TIE_TRIGGER || (m.iface[found] && mn < IFACE_TRIGGER)) {
-      int kind = 0;
-      const int r = resolve_ring(m, found, 1, f, lc, kind);
-      if (r >= 0) found = r;
-      st |= kind;
+    // the point may tie with other elements (within the band of a face, edge or vertex, or inside a
+    // face that borders another frame or an isoparametric element, where the own-frame shapes
+    // overlap): the ring is resolved by k_resolve_ring, one warp per such point
+    const double b[4] = {lc[0], lc[1], lc[2], 1.0 - lc[0] - lc[1] - lc[2]};
+    bool trig = false;
+    const uint8_t fmask = m.iface[found];
+    for (int k = 0; k < 4; ++k)
+      trig |= b[k] < TIE_TRIGGER || b[k] > 1.0 - TIE_TRIGGER || (((fmask >> k) & 1) && b[k] < IFACE_TRIGGER);
+    if (trig) {
+      st = 1 | 128;
+      ring_todo[atomicAdd(ring_count, 1)] = i;
     }
   } else {
-    int kind = 0;
-    const int r = resolve_ring(m, e, 2, f, lc, kind);
-    if (r >= 0) {
-      found = r;
-      st = (kind & 4) ? kind : (1 | kind);
-    } else {
-      st = 8 | kind;
-    }
+    found = e;                   // the walk's last element: centre of the 2-ring search
+    st = 128;
+    ring_todo[atomicAdd(ring_count, 1)] = i;
   }
-  if (adjust && found >= 0) {   // adjust_local_coords (locate_points_interp_vars_3d_sph.m:180-198)
-    for (int k = 0; k < 3; ++k) lc[k] = fmin(fmax(lc[k], 0.0), 1.0);
-    const double s = lc[0] + lc[1] + lc[2];
-    if (s > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= s;
+  if (st & 128) {                // resolved later from the centre element stored in els
+    els[i] = found;
+    status[i] = st;
+    return;
   }
   els[i] = found;
   lc_out[i] = lc[0];
@@ -432,9 +516,8 @@ __global__ void k_locate(SlmMesh m, const double *__restrict__ P, int npt, const
   status[i] = st;
 }
 
-// brute force over all elements for points the walk could not place (status 8): one warp per point,
-// the same rule over every element. Candidates within the tie band go to a per-warp list in shared
-// memory (the rule does not depend on their order); the gap choice is reduced across the warp.
+// brute force over all elements for points no ring could place (status 8): one warp per point, the
+// same rule over every element
 constexpr int BRUTE_WARPS = 8;
 __global__ void __launch_bounds__(BRUTE_WARPS * 32) k_locate_brute(SlmMesh m, const double *__restrict__ P, int npt,
                                                                   const int *__restrict__ todo, int ntodo,
@@ -446,69 +529,19 @@ __global__ void __launch_bounds__(BRUTE_WARPS * 32) k_locate_brute(SlmMesh m, co
   const int wl = threadIdx.x >> 5;
   const int w = blockIdx.x * BRUTE_WARPS + wl;
   const int lane = threadIdx.x & 31;
+  if (w >= ntodo) return;
   if (lane == 0) s_n[wl] = 0;
   __syncwarp();
-  if (w >= ntodo) return;
   const int i = todo[w];
   PointFrames f;
   point_frames(P[i], P[npt + i], P[2 * npt + i], f);
   GapBest G;
-  for (int e = lane; e < m.nel; e += 32) {
-    double lc[3], mn, mx;
-    int am;
-    const double step = local_coords(m, e, f, lc);
-    bary_minmax(lc, mn, mx, am);
-    const double need = fmax(-mn, mx - 1.0);
-    const int cls = m.cls[e];
-    const bool iso = cls == M3SPH_IN_CONE_ISO;
-    if (need <= TIE_BAND) {
-      const int slot = atomicAdd(&s_n[wl], 1);
-      if (slot < MAX_CAND) {
-        s_id[wl][slot] = e;
-        s_fl[wl][slot] = (uint8_t)((iso ? 1 : 0) | (frame_rank(cls) << 1) | (mx >= 1.0 - TIE_BAND ? 8 : 0));
-      }
-    } else if (need <= (GAP_QMAX + 1) * GAP_STEP) {
-      G.add(e, (int)ceil(need / GAP_STEP - 1e-9), iso, step);
-    }
-  }
+  for (int e = lane; e < m.nel; e += 32) eval_shared(m, e, f, s_id[wl], s_fl[wl], &s_n[wl], G);
   __syncwarp();
-  // warp reduction of the gap choice: smallest q, then the per-kind bests at that q
-  int q = G.q;
-  for (int o = 16; o > 0; o >>= 1) q = min(q, __shfl_xor_sync(0xffffffffu, q, o));
-  int non = (G.q == q) ? G.non : -1;
-  int iso_e = (G.q == q) ? G.iso : -1;
-  double iso_s = (G.q == q) ? G.iso_step : 1e300;
-  for (int o = 16; o > 0; o >>= 1) {
-    const int on = __shfl_xor_sync(0xffffffffu, non, o);
-    const int oi = __shfl_xor_sync(0xffffffffu, iso_e, o);
-    const double os = __shfl_xor_sync(0xffffffffu, iso_s, o);
-    if (on >= 0 && (non < 0 || on < non)) non = on;
-    if (oi >= 0 && (iso_e < 0 || os < iso_s || (os == iso_s && oi < iso_e))) { iso_e = oi; iso_s = os; }
-  }
+  int q;
+  const int gap_e = gap_reduce(G, q);
   if (lane != 0) return;
-  const int nc = s_n[wl];
-  int e = -1, kind = nc > MAX_CAND ? 64 : 0;
-  if (nc > 0) {
-    int amb = 0;
-    e = tie_rule(s_id[wl], s_fl[wl], min(nc, MAX_CAND), &amb);
-    kind |= (nc >= 2 ? 2 : 0) | (amb ? 32 : 0);
-  } else if (q <= GAP_QMAX) {
-    e = non >= 0 ? non : iso_e;
-    kind |= 4;
-  }
-  if (e < 0) return;
-  double lc[3];
-  local_coords(m, e, f, lc);
-  if (adjust) {   // adjust_local_coords (locate_points_interp_vars_3d_sph.m:180-198)
-    for (int k = 0; k < 3; ++k) lc[k] = fmin(fmax(lc[k], 0.0), 1.0);
-    const double sm = lc[0] + lc[1] + lc[2];
-    if (sm > 1.0) for (int k = 0; k < 3; ++k) lc[k] /= sm;
-  }
-  els[i] = e;
-  lc_out[i] = lc[0];
-  lc_out[npt + i] = lc[1];
-  lc_out[2 * npt + i] = lc[2];
-  status[i] = (uint8_t)(16 | kind);
+  finish_point(m, f, i, npt, s_id[wl], s_fl[wl], s_n[wl], gap_e, q, 16, adjust, els, lc_out, status);
 }
 
 // P2 interpolation (interp3d_tet.m:39-69): V is [nvar][nnod], out [nvar][npt]
@@ -759,6 +792,7 @@ struct SlmState {
   int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr, *grid = nullptr;
   float *S0f = nullptr, *SZf = nullptr, *SXf = nullptr;
   uint8_t *cls = nullptr, *iface = nullptr;
+  int *ring_count = nullptr;          // points listed for k_resolve_ring
   double *S0 = nullptr, *SZ = nullptr, *SX = nullptr;
   // work
   double *P = nullptr, *lc = nullptr, *V = nullptr, *out = nullptr, *upu = nullptr, *rpu = nullptr, *U = nullptr;
@@ -802,7 +836,7 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
                     (void *)S->wel, (void *)S->gn, (void *)S->wn, (void *)S->Xc, (void *)S->kk, (void *)S->acc,
                     (void *)S->els, (void *)S->guess,
                     (void *)S->todo, (void *)S->status, (void *)S->grid, (void *)S->S0f, (void *)S->SZf,
-                    (void *)S->SXf, (void *)S->iface})
+                    (void *)S->SXf, (void *)S->iface, (void *)S->ring_count})
       if (q) cudaFree(q);
     delete S;
   };
@@ -913,6 +947,8 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
   std::vector<uint8_t> cls(f0.elclass, f0.elclass + nel);
   // interface elements: some element sharing a vertex has another frame or another iso-ness (the
   // own-frame shapes of such neighbours overlap or leave gaps)
+  // (face k, opposite local vertex k, borders another frame or iso-ness if one of its vertices is
+  // shared with such an element: bit k of iface)
   std::vector<uint8_t> vmask(nv, 0), iface(nel, 0);
   auto key = [&](int e) { const int c = cls[e]; return (c >= 2 ? 0 : (c == 0 ? 1 : 2)) * 2 + (c == 3 ? 1 : 0); };
   for (int e = 0; e < nel; ++e)
@@ -920,7 +956,9 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
   for (int e = 0; e < nel; ++e)
     for (int i = 0; i < 4; ++i) {
       const uint8_t mk = vmask[el[(size_t)e * 10 + i]];
-      if (mk & (mk - 1)) iface[e] = 1;
+      if (mk & (mk - 1))
+        for (int k = 0; k < 4; ++k)
+          if (k != i) iface[e] |= (uint8_t)(1u << k);
     }
   int st;
   if ((st = sl_upload(&S->el2nod, soa.data(), soa.size(), s)) || (st = sl_upload(&S->nbr, nbr.data(), nbr.size(), s)) ||
@@ -929,7 +967,7 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
       (st = sl_upload(&S->cls, cls.data(), cls.size(), s)) || (st = sl_upload(&S->S0, S0.data(), S0.size(), s)) ||
       (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)) ||
       (st = sl_upload(&S->grid, grid.data(), grid.size(), s)) ||
-      (st = sl_upload(&S->iface, iface.data(), iface.size(), s)))
+      (st = sl_upload(&S->iface, iface.data(), iface.size(), s)) || (st = sl_alloc(&S->ring_count, 1)))
     return st;
   const std::vector<float> S0f(S0.begin(), S0.end()), SZf(SZ.begin(), SZ.end()), SXf(SX.begin(), SX.end());
   if ((st = sl_upload(&S->S0f, S0f.data(), S0f.size(), s)) || (st = sl_upload(&S->SZf, SZf.data(), SZf.size(), s)) ||
@@ -973,10 +1011,20 @@ static int slm_reserve(SlmState *S, size_t npt, int nel, int nnod, int nv) {
 static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool node_guess, bool adjust,
                       m3sph_locate_info *info) {
   cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemsetAsync(S->ring_count, 0, sizeof(int), s));
   k_locate<<<(npt + 127) / 128, 128, 0, s>>>(S->view, S->P, npt, use_guess ? S->guess : nullptr,
                                               node_guess ? S->node_guess : nullptr, S->els, S->lc, S->status,
-                                              adjust ? 1 : 0); count_launch();
+                                              adjust ? 1 : 0, S->todo, S->ring_count); count_launch();
   M3_CUDA(cudaGetLastError());
+  int nring = 0;
+  M3_CUDA(cudaMemcpyAsync(&nring, S->ring_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  if (nring > 0) {
+    k_resolve_ring<<<(nring + RING_WARPS - 1) / RING_WARPS, RING_WARPS * 32, 0, s>>>(S->view, S->P, npt, S->todo, nring,
+                                                                                     S->els, S->lc, S->status,
+                                                                                     adjust ? 1 : 0); count_launch();
+    M3_CUDA(cudaGetLastError());
+  }
   std::vector<uint8_t> hs(npt);
   M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));

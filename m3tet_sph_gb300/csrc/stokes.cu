@@ -61,7 +61,10 @@ template <typename T> int jac_first(T w, const T *r0, const T *Di, T *d, size_t 
 template <typename T> int jac(T w, const T *r0, const T *Kd, const T *Di, T *d, size_t n, cudaStream_t s);
 template <typename T> int restrict_(const Level &F, const Level &C, const T *a, const T *b, T *out, cudaStream_t s);
 template <typename T> int prolong(const Level &F, const Level &C, const T *xc, const T *add, T *out, cudaStream_t s);
-template <typename T> int dense_inverse(const Level &L, const T *K, const T *B, T *A, T *work, cudaStream_t s);
+template <typename T> int dense_inverse_blocked(const Level &L, const T *B, T *A, T *work, cudaStream_t s);
+int dense_inverse_from64(const Level &L, const double *B64, float *B32tmp, float *A, float *work, cudaStream_t s);
+int coarse_refined(const Level &L, const float *A32, const double *B64, const double *r, double *d, double *t,
+                   int sweeps, cudaStream_t s);
 template <typename T> int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s);
 size_t element_setup_smem();
 
@@ -635,8 +638,9 @@ static int alloc_work(m3sph_mesh *M) {
     M3_TRY(dalloc(&W->t64[i], n)); M3_TRY(dalloc(&W->t32[i], n));
   }
   const size_t nc = M->lev[nmg - 1].ndof;
-  M3_TRY(dalloc(&W->cwork64, 2 * nc));
-  M3_TRY(dalloc(&W->cwork32, 2 * nc));
+  // blocked Gauss-Jordan: the 128x128 diagonal inverse and the 128-wide row and column panels
+  M3_TRY(dalloc(&W->cwork64, 128 * 128 + 2 * 128 * nc));
+  M3_TRY(dalloc(&W->cwork32, 128 * 128 + 2 * 128 * nc));
   const size_t n0 = M->lev[0].ndof, np = M->lev[0].nvnod;
   M3_TRY(dalloc(&W->r, n0)); M3_TRY(dalloc(&W->d, n0)); M3_TRY(dalloc(&W->q, n0));
   M3_TRY(dalloc(&W->Kq, n0)); M3_TRY(dalloc(&W->tmp, n0));
@@ -671,6 +675,10 @@ __global__ void k_recip(const double *a, double *b, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = 1.0 / a[i];
 }
+
+// FP64 coarsest levels up to this many dofs are inverted in FP64; larger ones are refined
+static int g_coarse_f64_direct_max = 6000;
+static int g_coarse_refine_sweeps = 3;
 
 // element operator, force vector, Galerkin hierarchy and coarse inverse from the device-resident
 // viscosity, density and boundary conditions (assembly_stokes_sph_3d_double_jacobian +
@@ -736,21 +744,32 @@ static int rebuild_operator(m3sph_mesh *M) {
       M3_TRY(bsr_assemble<float>(C, C.K32, C.B32, s));
     }
   }
-  // coarsest dense inverse (stands in for cholesky_factorization)
+  // coarsest-level solve (stands in for cholesky_factorization / cholesky_solve): the dense
+  // inverse by blocked Gauss-Jordan (128-wide panels), applied as one GEMV per V-cycle. FP32 V-cycle: FP32 inverse.
+  // Plain FP64 path: the FP64 inverse up to g_coarse_f64_direct_max dofs; above, the FP32 inverse
+  // of the FP64 operator refined against it to FP64 rounding in every coarse solve (an FP64 dense
+  // inverse costs 2 n^3 FP64 flops, ~10 s at n = 17,334 on this part's FP64 rate).
   Level &Lc = M->lev[M->nmg - 1];
   const int nc = Lc.ndof;
-  if (nc > 12000) {
-    set_error("coarsest level too large for the dense coarse solve; add a multigrid level");
+  if (nc > 40000) {
+    set_error("coarsest level too large for the dense coarse solve (more than 40,000 dofs); add a multigrid level");
     return M3SPH_ERR_BAD_INPUT;
   }
   M->coarse.n = nc;
+  M->coarse.refine64 = false;
   if (M->nmg > 1) {
-    if (M->precision == 0) {
+    if (M->precision == 0 && nc <= g_coarse_f64_direct_max) {
       if (!M->coarse.A64) M3_TRY(dalloc(&M->coarse.A64, (size_t)nc * nc));
-      M3_TRY(dense_inverse<double>(Lc, Lc.K64, Lc.B64, M->coarse.A64, W->cwork64, s));
+      M3_TRY(dense_inverse_blocked<double>(Lc, Lc.B64, M->coarse.A64, W->cwork64, s));
+    } else if (M->precision == 0) {
+      M->coarse.refine64 = true;
+      if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
+      if (!M->coarse.B32tmp) M3_TRY(dalloc(&M->coarse.B32tmp, 9 * (size_t)Lc.nnzb));
+      if (!M->coarse.t64) M3_TRY(dalloc(&M->coarse.t64, (size_t)nc));
+      M3_TRY(dense_inverse_from64(Lc, Lc.B64, M->coarse.B32tmp, M->coarse.A32, W->cwork32, s));
     } else {
       if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
-      M3_TRY(dense_inverse<float>(Lc, Lc.K32, Lc.B32, M->coarse.A32, W->cwork32, s));
+      M3_TRY(dense_inverse_blocked<float>(Lc, Lc.B32, M->coarse.A32, W->cwork32, s));
     }
   }
   return M3SPH_OK;
@@ -898,6 +917,18 @@ static int level_op_jac(const Level &L, int img, T w, const T *r, T *d, T *kd, c
   return jac<T>(w, r, kd, levDi<T>(L), d, L.ndof, s);
 }
 
+// the coarsest-level solve of the V-cycle: one GEMV with the dense inverse, or on the plain FP64
+// path with a large coarsest level the FP32 inverse refined against the FP64 operator
+template <typename T>
+static int coarse_solve(m3sph_mesh *M, const T *Ainv, const T *r, T *d) {
+  const Level &Lc = M->lev[M->nmg - 1];
+  if constexpr (std::is_same<T, double>::value) {
+    if (M->coarse.refine64)
+      return coarse_refined(Lc, M->coarse.A32, Lc.B64, r, d, M->coarse.t64, g_coarse_refine_sweeps, M->stream);
+  }
+  return dense_gemv<T>(Ainv, M->coarse.n, r, Lc.freemask, d, M->stream);
+}
+
 template <typename T>
 static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std::vector<T *> &kd,
                     std::vector<T *> &tmp, const T *Ainv) {
@@ -933,7 +964,7 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     }
     M3_TRY(restrict_<T>(L, M->lev[j + 1], r[j], kd[j], r[j + 1], s));
   }
-  M3_TRY(dense_gemv<T>(Ainv, M->coarse.n, r[nm - 1], M->lev[nm - 1].freemask, d[nm - 1], s));
+  M3_TRY(coarse_solve<T>(M, Ainv, r[nm - 1], d[nm - 1]));
   for (int j = nm - 2; j >= 0; --j) {
     const Level &L = M->lev[j];
     const double *w = j == 0 ? WU0 : WUc;
@@ -1906,6 +1937,18 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
     M->use_graphs = value != 0;
   } else if (n == "df_outer") {
     M->df_outer = value != 0;
+  } else if (n == "coarse_f64_direct_max") {
+    if (value < 0) {
+      set_error("coarse_f64_direct_max must be >= 0");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    g_coarse_f64_direct_max = value;
+  } else if (n == "coarse_refine_sweeps") {
+    if (value < 0 || value > 20) {
+      set_error("coarse_refine_sweeps must be in 0..20");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    g_coarse_refine_sweeps = value;
   } else {
     set_error("unknown option " + n);
     return M3SPH_ERR_BAD_INPUT;
@@ -1961,6 +2004,27 @@ extern "C" int m3sph_ml_collect(m3sph_mesh *M, uint64_t seed, int32_t n_iterates
   }
   M3_CUDA(cudaStreamSynchronize(s));
   M->smoother_active = act;
+  if (count) *count = ml_count(M);
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_ml_add_pairs(m3sph_mesh *M, const double *r, const double *e, int32_t stride, int32_t offset,
+                                  int64_t *count) {
+  M3_TRY(need_op(M));
+  if (!r || !e || stride < 1 || offset < 0) {
+    set_error("m3sph_ml_add_pairs: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Work *W = get_work(M);
+  Level &L0 = M->lev[0];
+  cudaStream_t s = M->stream;
+  const size_t n = L0.ndof;
+  M3_CUDA(cudaMemcpyAsync(W->r, r, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_CUDA(cudaMemcpyAsync(W->tmp, e, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  M3_TRY(apply_mask(W->r, L0.freemask, n, s));
+  M3_TRY(apply_mask(W->tmp, L0.freemask, n, s));
+  M3_TRY(ml_add_samples(M, W->r, W->tmp, stride, offset % stride));
+  M3_CUDA(cudaStreamSynchronize(s));
   if (count) *count = ml_count(M);
   return M3SPH_OK;
 }

@@ -76,10 +76,31 @@ def collect(dm, seed, n_iterates=4, stride=1):
     return n.value
 
 
+def collect_mg_pairs(dm, seed, n_rhs, n_iterates, stride):
+    """(residual, error) pairs of plain multigrid iterates: for seeded right-hand sides b on the
+    free dofs, x* from a tight MG-PCG solve, then the iterates x_k after k = 1..n_iterates MG-PCG
+    iterations from zero with r_k = b - K x_k and e_k = x* - x_k (the operator and V-cycle of the
+    current set-up, Jacobi smoothing)."""
+    rng = np.random.default_rng(seed)
+    count = C.c_int64()
+    for i in range(n_rhs):
+        b = rng.standard_normal(dm.ndof)
+        x_star, _, _ = dm.mgpcg(b, np.zeros(dm.ndof), 1e-12, is_abs_tol=False, itmax=300)
+        for k in range(1, n_iterates + 1):
+            x_k, _, _ = dm.mgpcg(b, np.zeros(dm.ndof), 1e-30, is_abs_tol=False, itmax=k)
+            r_k = b - dm.apply(x_k)
+            e_k = np.ascontiguousarray(x_star - x_k)
+            L.check(L.lib().m3sph_ml_add_pairs(dm.h, L.dptr(np.ascontiguousarray(r_k)), L.dptr(e_k), int(stride),
+                                                int((seed + i * n_iterates + k) % stride), C.byref(count)))
+    return count.value
+
+
 def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_000, n_iterates=4, epochs=12,
-                   batch=4096, lr=2e-3, seed=0, precision=1, log=None):
+                   batch=4096, lr=2e-3, seed=0, precision=1, log=None, pairs="noise"):
     """Collect pairs over `n_fields` seeded viscosity fields on the mesh of workload `w`, train,
-    and leave the trained weights loaded in `dm`. Returns (params, history)."""
+    and leave the trained weights loaded in `dm`. pairs: "noise" -- (K e, e) for white-noise errors
+    e; "mg" -- residuals and errors of plain multigrid iterates (collect_mg_pairs). Returns
+    (params, history)."""
     rng = np.random.default_rng(seed)
     nel = w['levels'][0]['nel']
     per_field = samples / n_fields
@@ -92,7 +113,10 @@ def train_smoother(dm, w, n_fields=20, contrast_range=(1e2, 1e5), samples=2_000_
         T = workloads.temperature(w['levels'], seed + 1000 + i)
         visc = workloads.viscosity(w['levels'], T, c, 30.0)
         dm.setup(visc, workloads.density(T), w['ifix'], w['vfix'], w['phys'], precision=precision)
-        count = collect(dm, seed * 7919 + i, n_iterates, stride)
+        if pairs == "mg":
+            count = collect_mg_pairs(dm, seed * 7919 + i, 1, n_iterates, stride)
+        else:
+            count = collect(dm, seed * 7919 + i, n_iterates, stride)
         if log:
             log(f"field {i}: contrast {c:.3g}, samples {count}")
     t_collect = time.time() - t0
@@ -145,13 +169,15 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--schedule", type=int, default=1, help="0: learned-Jacobi-learned per side, 1: one learned sweep")
+    ap.add_argument("--pairs", default="noise", choices=["noise", "mg"],
+                    help="training pairs: white-noise (K e, e) or plain-multigrid iterates")
     a = ap.parse_args(argv)
     w = workloads.make_workload(a.workload, seed=a.seed)
     dm = stokes.DeviceMesh(w['levels'])
     try:
         if a.cmd == "train":
             p, h = train_smoother(dm, w, n_fields=a.fields, samples=a.samples, epochs=a.epochs, seed=a.seed,
-                                  log=lambda m: print(m, flush=True))
+                                  log=lambda m: print(m, flush=True), pairs=a.pairs)
             np.save(a.weights, p)
             print(json.dumps({"mse": h["mse"], "t_collect_s": h["t_collect"], "t_train_s": h["t_train"],
                               "stride": h["stride"]}))

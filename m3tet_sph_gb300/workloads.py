@@ -7,8 +7,10 @@ spherical-Voronoi caps with random Euler poles. Units follow the reference's 'ma
 * ``shell_c1``: level-3 icosahedral surface, 8 layers, 3 MG levels; isoviscous 1e21 Pa s;
   T = linear conductive profile + 0.05 Re Y_4^3 + U(-1e-3, 1e-3); free slip at both boundaries
   with the rigid-rotation pins of the reference's commented-out recipe (SETUP_TEST/bc_sph.m:569-594).
-* ``shell_c2``: level-5 surface, 32 layers; eta = eta0 exp(-gamma T) (contrast 1e4) x 30 below
-  660 km depth; 12 seeded plate caps (|v| <= 10 cm/yr) at the surface, free slip at the CMB.
+* ``shell_c2``: level-5 surface, 32 layers, 4 MG levels (coarsest 17,334 DOF); eta = eta0 exp(-gamma T)
+  (contrast 1e4) x 30 below 660 km depth; 12 seeded plate caps (|v| <= 10 cm/yr) at the surface,
+  free slip at the CMB.
+* ``shell_c5``: level-6 surface, 64 layers, 5 MG levels (coarsest 17,334 DOF), contrast 1e6.
 """
 from __future__ import annotations
 
@@ -22,6 +24,8 @@ SCALE['U0'] = SCALE['L0'] / SCALE['t0']
 SCALE['Bscale'] = SCALE['L0'] ** 2 / (SCALE['Visc0'] * SCALE['U0'])
 R_CMB, R_SURF = 3480.0, 6371.0
 ALPHA, DT_K = 3e-5, 2500.0
+# thermal diffusivity 1e-6 m^2/s in km^2/Myr (model_parameters_sph_south_atlantic_plume.m:483-487)
+KAPPA = 1e-6 / (SCALE['L0'] ** 2 / SCALE['t0'])
 
 
 def physics():
@@ -132,9 +136,9 @@ def make_workload(name, seed=0, nmg=None, level=None, nlayer=None):
     if name == 'c1':
         L, n, g, contrast, jump, bc = 3, 8, 3, 1.0, 1.0, 'free_slip'
     elif name == 'c2':
-        L, n, g, contrast, jump, bc = 5, 32, 5, 1e4, 30.0, 'plates'
+        L, n, g, contrast, jump, bc = 5, 32, 4, 1e4, 30.0, 'plates'
     elif name == 'c5':
-        L, n, g, contrast, jump, bc = 6, 64, 6, 1e6, 30.0, 'plates'
+        L, n, g, contrast, jump, bc = 6, 64, 5, 1e6, 30.0, 'plates'
     elif name == 'mid':
         # 1/8 of the 8M-DOF shell (level 4, 16 layers): the profiling case (> L2, a few GB on device)
         L, n, g, contrast, jump, bc = 4, 16, 4, 1e4, 30.0, 'plates'

@@ -190,8 +190,10 @@ def gap_rule(ids, iso, q, step):
 
 class Locator:
     """Point location by the explicit rule of the module docstring. Candidate elements come from
-    the k nearest element centroids; an element that places the point near its boundary has its
-    vertex neighbours added (every other element within the tie band shares a vertex with it),
+    the k nearest element centroids; an element that places the point near its boundary (within
+    TIE_TRIGGER, or within IFACE_TRIGGER of a face that borders another frame or an isoparametric
+    element, where own-frame shapes overlap) has its vertex neighbours added (every other element
+    within the tie band shares a vertex with it),
     and a point outside all of them is tested against every element whose centroid lies within
     1.5 circumradii."""
 
@@ -214,7 +216,9 @@ class Locator:
         kmax = np.full(nv, -1)
         np.minimum.at(kmin, EL4.ravel(), np.repeat(key, 4))
         np.maximum.at(kmax, EL4.ravel(), np.repeat(key, 4))
-        self.iface = (kmin[EL4] != kmax[EL4]).any(1)
+        multi = (kmin != kmax)[EL4]                            # (nel,4): vertex shared across frames / iso-ness
+        # face k (opposite vertex k) borders another frame or iso-ness if one of its vertices does
+        self.iface_face = np.stack([multi[:, [i for i in range(4) if i != k]].any(1) for k in range(4)], 1)
         V = X[:, EL4]                                           # (3,nel,4)
         self.cent = V.mean(axis=2).T
         self.rad = np.sqrt(((V - self.cent.T[:, :, None]) ** 2).sum(0)).max()
@@ -299,8 +303,10 @@ class Locator:
         lcs = lc[:, r, j].copy()
         kind = np.ones(n, np.int32)
         found = need[r, j] <= TIE_BAND
-        mnb, mxb = mn[r, j], mx[r, j]
-        trig = found & ((mnb < TIE_TRIGGER) | (mxb > 1 - TIE_TRIGGER) | (self.iface[best] & (mnb < IFACE_TRIGGER)))
+        lb = lcs
+        bary = np.vstack([lb, 1 - lb.sum(0)]).T                  # (n,4): barycentric k <-> face k
+        trig = found & ((bary < TIE_TRIGGER) | (bary > 1 - TIE_TRIGGER)
+                        | (self.iface_face[best] & (bary < IFACE_TRIGGER))).any(1)
         for sel, lists in ((np.nonzero(trig)[0], None), (np.nonzero(~found)[0], None)):
             if len(sel) == 0:
                 continue

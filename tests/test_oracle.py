@@ -145,3 +145,21 @@ def test_diffusion_oracle_identities(tiny):
     assert abs(D.ML.sum() / (6 * vol) - 1) < 2e-2
     T, nit = D.step(np.full(f['nnod'], 5.0), 100.0, np.full(len(fix), 5.0))
     assert np.abs(T - 5.0).max() < 1e-12
+
+
+def test_gelu_erf_approximation_bound():
+    """The fused inference sweep's GELU uses Abramowitz & Stegun 7.1.26 for erf (|error| <= 1.5e-7);
+    the same formula and constants, evaluated in FP64 here, stay within that bound of erf and
+    within 1.5e-7 |x| / 2 of the exact GELU."""
+    import numpy as np
+    from scipy.special import erf
+    x = np.linspace(-12.0, 12.0, 200001)
+    z = np.abs(x) / np.sqrt(2.0)
+    t = 1.0 / (1.0 + 0.3275911 * z)
+    poly = t * (0.254829592 + t * (-0.284496736 + t * (1.421413741 + t * (-1.453152027 + t * 1.061405429))))
+    erf_as = 1.0 - poly * np.exp(-z * z)
+    assert np.max(np.abs(erf_as - erf(z))) <= 1.5e-7
+    q = 0.5 * x * poly * np.exp(-0.5 * x * x)
+    gelu_as = np.where(x >= 0, x - q, q)
+    gelu = 0.5 * x * (1.0 + erf(x / np.sqrt(2.0)))
+    assert np.all(np.abs(gelu_as - gelu) <= 0.5 * 1.5e-7 * np.abs(x) + 1e-15)
