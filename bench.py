@@ -170,6 +170,7 @@ def run_gb300(args, rank, ws, td):
     nel, ndof = lv0["nel"], 3 * lv0["nnod"]
     nvnod = int(lv0["EL2NOD"][:, :4].max()) + 1
     dm = stokes.DeviceMesh(w["levels"], device=dev)
+    dm.set_option("fp32_operator", args.fp32_operator)
     torch.cuda.set_device(dev)
     wfile = ROOT / "m3tet_sph_gb300" / "smoother_c1.npy"
     use_learned = not args.skip_learned
@@ -277,6 +278,8 @@ def run_gb300(args, rank, ws, td):
                    "nmg": w["nmg"], "solves_per_s": ws * 1e3 / ms,
                    "smoother": "learned (one sweep per side, levels 0-1) + Jacobi below" if use_learned
                    else "weighted Jacobi",
+                   "fp32_operator": "partially assembled (per-point geometric factors)" if args.fp32_operator
+                   else "streamed stored element matrices",
                    "l2": f"working set (element matrices {nel * 7440 / 1e9:.0f} GB) > L2; no flush needed",
                    "parallelism": f"replicas x{ws}"},
         "solve": {"itPat": last["itPat"], "nitU": last["nitU"], "nitZ": last["nitZ"], "nvcycle": last["nvcycle"],
@@ -351,6 +354,7 @@ def c1_leg(args, wfile):
     from m3tet_sph_gb300 import _lib, learned as LS, stokes, workloads
     w = workloads.make_workload("c1", seed=args.seed)
     dm = stokes.DeviceMesh(w["levels"])
+    dm.set_option("fp32_operator", args.fp32_operator)
     out = {"workload": "shell L3 x 8 layers, 30720 P2 tets, 130662 velocity DOF, 3 MG levels, isoviscous, free slip"}
     try:
         stream = torch.cuda.ExternalStream(dm.stream())
@@ -384,6 +388,7 @@ def c5_leg(args, wfile):
     w = workloads.make_workload("c5", seed=args.seed)
     f = w["levels"][0]
     dm = stokes.DeviceMesh(w["levels"])
+    dm.set_option("fp32_operator", args.fp32_operator)
     t_mesh = time.time() - t0
     nnod = f["nnod"]
     out = {"workload": f"shell L{w['level']} x {w['nlayer']} layers, {f['nel']} P2 tets, {3 * nnod} velocity DOF, "
@@ -543,12 +548,12 @@ def run_operator_only(args, rank):
     w = workloads.make_workload(args.workload, seed=args.seed, nmg=args.nmg)
     lv0 = w["levels"][0]
     dm = stokes.DeviceMesh(w["levels"])
-    t = time.perf_counter()
-    dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
-    t_setup = time.perf_counter() - t
     for kv in args.set_option:
         k, v = kv.split("=")
         dm.set_option(k, int(v))
+    t = time.perf_counter()
+    dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
+    t_setup = time.perf_counter() - t
     ms = dm.apply_timing(args.op_level, args.op_precision, args.op_reps)
     nc = dm.ncolors(args.op_level)
     dm.close()
@@ -571,7 +576,7 @@ def cpu_solve_c1(seed, nthreads):
     from m3tet_sph_gb300 import workloads
     w = workloads.make_workload("c1", seed=seed)
     t = time.perf_counter()
-    S = O.StokesSystem(w["levels"], w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"])
+    S = O.StokesSystem(w["levels"], w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], nthreads=nthreads)
     S.mg.use_threads(nthreads)
     U, P, info = O.patera(S, target_rel_residual=TARGET, **{k: v for k, v in SOLVER_KW.items()
                                                              if k != "target_rel_residual"})
@@ -654,6 +659,8 @@ def main():
     ap.add_argument("--sl-workload", default="c1", help="mesh of the semi-Lagrangian measurements")
     ap.add_argument("--skip-sl", action="store_true")
     ap.add_argument("--sweep-points", type=int, default=16_000_000)
+    ap.add_argument("--fp32-operator", type=int, default=0, choices=[0, 1],
+                    help="finest-level FP32 V-cycle operator: 0 streamed stored matrices, 1 partially assembled")
     ap.add_argument("--op-only", action="store_true", help="time one level operator only (profiling)")
     ap.add_argument("--diff-only", action="store_true", help="time thermal-diffusion half steps only (profiling)")
     ap.add_argument("--op-level", type=int, default=0)

@@ -130,6 +130,13 @@ struct Level {
   int *g_ptr = nullptr;               // [nnod + 1] node -> incident (element, local node) entries
   int *g_idx = nullptr;               // [10 nel] offsets e * 30 + 3 * local node into Ye, element order
   int *sa_err = nullptr;              // bounded waits of the streamed apply that gave up (bit mask)
+  // partially assembled FP32 operator (finest level): per integration point the 3x3 factor
+  // sqrt(w eta) d xi / d x, [NIP][9][nel]; per element the free-dof bits; per node RR's angles
+  float *pa32 = nullptr;
+  int pa_ld = 0;                      // row stride of pa32 (floats, multiple of 4)
+  uint32_t *pa_emask = nullptr;       // [nel] bit 3 n + c set when dof c of local node n is free
+  float4 *pa_trig = nullptr;          // [nnod] (cos theta, sin theta, cos phi, sin phi)
+  bool pa_ready = false;              // pa32 / pa_emask written by the last operator set-up
   // host copies needed at set-up
   std::vector<int> h_el2nod_orig;     // [nel][10] original order, 0-based
 };
@@ -174,6 +181,9 @@ struct SetupArgs {
   double g, Bscale, Dens0, minVisc, maxVisc;
   double *K64; float *K32; double *G64; double *M64; double *Fbe;
   float *KL32;              // low FP32 part of K64 - K32 (double-float outer operator) or nullptr
+  float *PA32;              // [NIP * 9][pa_ld] partially assembled factors or nullptr
+  int pa_ld;
+  uint32_t *emask;          // [nel] free-dof bits or nullptr
   const double *ufix;       // [3*nnod] prescribed values (rotated frame) or nullptr
   double *BCe;              // [30][nel] element K_unmasked * ufix (when ufix != nullptr)
   int *err;

@@ -370,7 +370,9 @@ int diffusion_resident(m3sph_mesh *M, double *T, double dt, int *nit) {
   const double tol = D->tol * norm_r;
   int it = 0;
   double rd = 0.0;
-  if (!(norm_r < tol)) {
+  // an exactly zero initial residual (a field the step leaves unchanged, e.g. a constant one) is
+  // converged: pcg_solver_p.m would test 0 < 0 and go on to alpha = 0/0
+  if (!(norm_r < tol) && norm_r > 0.0) {
     for (it = 1; it <= D->itmax; ++it) {
       k_diff_jacobi<<<g, 256, 0, s>>>(n, D->ML, D->Cdiag, c, D->fixmask, D->r, D->d); count_launch();
       double beta = 0.0;

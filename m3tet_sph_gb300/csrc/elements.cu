@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
     }
     sMask[el] = mask;
     sCls[el] = cls;
+    if (a.emask && e < nel) a.emask[e] = (uint32_t)mask;
     for (int q = 0; q < 30; ++q) sBC[q * EB + el] = 0.0;
   }
   __syncthreads();
@@ -199,6 +200,25 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_element_setup(SetupArgs a) {
     if (!(visc > 0.0)) atomicOr(a.err, 4);
     sW[ip * EB + el] = w;
     sW2[ip * EB + el] = w * visc;
+    if (a.PA32) {
+      // sqrt(w eta) d xi_j / d x_c in global Cartesian components: frame = R_cls global, so
+      // d xi / d x_global = R_cls^T Jd (Z-180: diag(-1,-1,1); X-90: frame (x, -z, y))
+      const double sq = sqrt(w * visc);
+      for (int j = 0; j < 3; ++j) {
+        double g0 = Jd[0][j], g1 = Jd[1][j], g2 = Jd[2][j];
+        if (cls == M3SPH_OUT_CONE_CROSS_2PI) {
+          g0 = -g0;
+          g1 = -g1;
+        } else if (cls != M3SPH_OUT_CONE_NO_CROSS_2PI) {
+          const double t1 = g1;
+          g1 = Jd[2][j];
+          g2 = -t1;
+        }
+        a.PA32[((size_t)ip * 9 + 0 * 3 + j) * a.pa_ld + e] = (float)(sq * g0);
+        a.PA32[((size_t)ip * 9 + 1 * 3 + j) * a.pa_ld + e] = (float)(sq * g1);
+        a.PA32[((size_t)ip * 9 + 2 * 3 + j) * a.pa_ld + e] = (float)(sq * g2);
+      }
+    }
     sW3[ip * EB + el] = w / visc;
     sFG[ip * EB + el] = w * a.g * a.Bscale * (dens - a.Dens0);
     sDIR[(ip * 3 + 0) * EB + el] = st * cp;

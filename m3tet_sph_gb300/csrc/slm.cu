@@ -365,10 +365,17 @@ __global__ void __launch_bounds__(RING_WARPS * 32) k_resolve_ring(SlmMesh m, con
   GapBest G;
   __syncwarp();
   if (depth == 1) {
+    // an element of the 1-ring is visited once: from the first of e0's vertices it contains
     for (int t = lane; t < tot; t += 32) {
       int k = 0, o = t;
       while (o >= len[k]) o -= len[k++];
-      eval_shared(m, m.v2e[m.v2e_ptr[v0[k]] + o], f, s_id[wl], s_fl[wl], &s_n[wl], G);
+      const int e1 = m.v2e[m.v2e_ptr[v0[k]] + o];
+      bool dup = false;
+      for (int j = 0; j < 4; ++j) {
+        const int v = m.el2nod[(size_t)j * m.nel + e1];
+        for (int kk = 0; kk < k; ++kk) dup |= v == v0[kk];
+      }
+      if (!dup) eval_shared(m, e1, f, s_id[wl], s_fl[wl], &s_n[wl], G);
     }
   } else {
     // vertices of the 1-ring, deduplicated in a shared hash table (-1 = empty)
@@ -389,11 +396,29 @@ __global__ void __launch_bounds__(RING_WARPS * 32) k_resolve_ring(SlmMesh m, con
       }
     }
     __syncwarp();
+    // an element of the 2-ring is visited once: from the vertex in the table's lowest slot
     for (int slot = 0; slot < RING_VTAB; ++slot) {
       const int v = s_vt[wl][slot];
       if (v < 0) continue;
-      for (int k = m.v2e_ptr[v] + lane; k < m.v2e_ptr[v + 1]; k += 32)
-        eval_shared(m, m.v2e[k], f, s_id[wl], s_fl[wl], &s_n[wl], G);
+      for (int k = m.v2e_ptr[v] + lane; k < m.v2e_ptr[v + 1]; k += 32) {
+        const int e1 = m.v2e[k];
+        bool dup = false;
+        for (int j = 0; j < 4 && !dup; ++j) {
+          const int vj = m.el2nod[(size_t)j * m.nel + e1];
+          if (vj == v) continue;
+          int h = (int)(((unsigned)vj * 2654435761u) % RING_VTAB);
+          for (int probe = 0; probe < RING_VTAB; ++probe) {
+            const int tv = s_vt[wl][h];
+            if (tv < 0) break;
+            if (tv == vj) {
+              dup = h < slot;
+              break;
+            }
+            h = (h + 1) % RING_VTAB;
+          }
+        }
+        if (!dup) eval_shared(m, e1, f, s_id[wl], s_fl[wl], &s_n[wl], G);
+      }
     }
   }
   __syncwarp();

@@ -36,6 +36,11 @@ int stream_apply_jac_f32(const Level &L, const float *K, float w, const float *r
 int stream_apply_df(const Level &L, const float *Kh, const float *Kl, const double *x, double *y, cudaStream_t s);
 int stream_apply_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
 int stream_check(const Level &L, cudaStream_t s);
+int pa_upload_tables();
+int pa_row_stride(int nel);
+int pa_build_trig(const double *RR, int nnod, float4 *trig, cudaStream_t s);
+int pa_apply_f32(const Level &L, const float *x, float *y, cudaStream_t s);
+int pa_apply_jac_f32(const Level &L, float w, const float *r, const float *Di, float *d, cudaStream_t s);
 int stream_set_outer_warps(int n);
 int stream_set_f32_variant(int v);
 int scatter_elvec(const Level &L, const double *V, int nq, int per_node, double *out, size_t nout, cudaStream_t s);
@@ -422,7 +427,7 @@ static void free_level(Level &L) {
                   (void *)L.P_ptr, (void *)L.P_col, (void *)L.P_w, (void *)L.R_ptr, (void *)L.R_col, (void *)L.R_w,
                   (void *)L.bsr_ptr, (void *)L.bsr_col, (void *)L.bsr_cptr, (void *)L.bsr_contrib, (void *)L.B64,
                   (void *)L.B32, (void *)L.chunk_conn, (void *)L.ye32, (void *)L.g_ptr, (void *)L.g_idx, (void *)L.sa_err,
-                  (void *)L.chunk_conn8, (void *)L.ye64})
+                  (void *)L.chunk_conn8, (void *)L.ye64, (void *)L.pa32, (void *)L.pa_emask, (void *)L.pa_trig})
     dfree(p);
   L = Level();
 }
@@ -479,6 +484,8 @@ extern "C" int m3sph_mesh_create(int32_t nmg, const m3sph_level *levels, int32_t
   };
   if (cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(M3SPH_ERR_CUDA);
   st = upload_shape_tables();
+  if (st) return fail(st);
+  st = pa_upload_tables();
   if (st) return fail(st);
   M->lev.resize(nmg);
   for (int i = 0; i < nmg; ++i) {
@@ -677,6 +684,9 @@ __global__ void k_recip(const double *a, double *b, int n) {
 }
 
 // FP64 coarsest levels up to this many dofs are inverted in FP64; larger ones are refined
+// FP32 V-cycle operator of the finest level: false = streamed stored matrices (K32), true =
+// partially assembled (per-point geometric factors, product formed on the fly)
+static bool g_pa_apply = false;
 static int g_coarse_f64_direct_max = 6000;
 static int g_coarse_refine_sweeps = 3;
 
@@ -697,11 +707,29 @@ static int rebuild_operator(m3sph_mesh *M) {
   a.ufix = nullptr;
   a.BCe = nullptr;
   a.KL32 = L0.KL32;
+  a.PA32 = nullptr;
+  a.emask = nullptr;
+  L0.pa_ready = false;
+  if (M->precision == 1 && g_pa_apply) {
+    if (!L0.pa32) {
+      L0.pa_ld = pa_row_stride(L0.nel);
+      M3_TRY(dalloc(&L0.pa32, (size_t)NIP * 9 * L0.pa_ld));
+    }
+    if (!L0.pa_emask) M3_TRY(dalloc(&L0.pa_emask, (size_t)L0.nel));
+    if (!L0.pa_trig) {
+      M3_TRY(dalloc(&L0.pa_trig, (size_t)L0.nnod));
+      M3_TRY(pa_build_trig(M->fin.RR, L0.nnod, L0.pa_trig, s));
+    }
+    a.PA32 = L0.pa32;
+    a.pa_ld = L0.pa_ld;
+    a.emask = L0.pa_emask;
+  }
   if (M->has_nonzero_fix) {
     a.ufix = M->Ufix;
     a.BCe = M->fin.BCe;
   }
   M3_TRY(launch_element_setup(a, s));
+  L0.pa_ready = a.PA32 != nullptr;
   int herr[4];
   M3_CUDA(cudaMemcpyAsync(herr, M->fin.err, sizeof(herr), cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
@@ -896,6 +924,9 @@ static int stream_apply_T(const Level &L, const double *K, const double *x, doub
 template <typename T>
 static int level_op(const Level &L, int img, const T *x, T *y, cudaStream_t s) {
   if (img > 0 && levB<T>(L)) return bsr_apply<T>(L, levB<T>(L), x, y, s);
+  if constexpr (std::is_same<T, float>::value) {
+    if (img == 0 && g_pa_apply && L.pa_ready) return pa_apply_f32(L, x, y, s);
+  }
   if ((std::is_same<T, float>::value ? g_stream_apply : g_stream_outer) && L.nchunk && levK<T>(L))
     return stream_apply_T(L, levK<T>(L), x, y, s);
   if (g_split_apply) return split_apply_T(L, levK<T>(L), x, y, s);
@@ -911,6 +942,7 @@ template <> const float *levDi<float>(const Level &L) { return L.Dinv32; }
 template <typename T>
 static int level_op_jac(const Level &L, int img, T w, const T *r, T *d, T *kd, cudaStream_t s) {
   if constexpr (std::is_same<T, float>::value) {
+    if (img == 0 && g_pa_apply && L.pa_ready) return pa_apply_jac_f32(L, w, r, L.Dinv32, d, s);
     if (img == 0 && g_stream_apply && L.nchunk && L.K32) return stream_apply_jac_f32(L, L.K32, w, r, L.Dinv32, d, s);
   }
   M3_TRY(level_op<T>(L, img, d, kd, s));
@@ -1910,6 +1942,12 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
   const std::string n(name);
   if (n == "stream_apply") {
     g_stream_apply = value != 0;
+  } else if (n == "fp32_operator") {
+    if (value < 0 || value > 1) {
+      set_error("fp32_operator must be 0 (stored element matrices) or 1 (partially assembled)");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    g_pa_apply = value == 1;
   } else if (n == "ml_schedule") {
     if (value < 0 || value > 1) {
       set_error("ml_schedule must be 0 or 1");

@@ -218,6 +218,33 @@ def element_matrices(mesh, visc, dens, g=-9.81, Bscale=1.0, Dens0=0.0, minVisc=N
     return K, G, Mm, Fb
 
 
+def element_matrices_threaded(mesh, visc, dens, nthreads, **phys):
+    """element_matrices over contiguous blocks of elements on `nthreads` host threads (numpy
+    releases the GIL inside its kernels); the same per-element arithmetic as one call."""
+    EL = mesh['EL2NOD']
+    nel = len(EL)
+    if nthreads <= 1 or nel < 4096:
+        return element_matrices(mesh, visc, dens, **phys)
+    from concurrent.futures import ThreadPoolExecutor
+    iso_pos = {e: i for i, e in enumerate(mesh['els_iso'])}
+    bounds = np.linspace(0, nel, nthreads + 1).astype(np.int64)
+
+    def block(k):
+        lo, hi = int(bounds[k]), int(bounds[k + 1])
+        sub = dict(mesh)
+        sub['EL2NOD'] = EL[lo:hi]
+        sub['cls'] = mesh['cls'][lo:hi]
+        els = [e for e in mesh['els_iso'] if lo <= e < hi]
+        sub['els_iso'] = np.array([e - lo for e in els], dtype=np.int64)
+        sub['cubic_sph_rot'] = mesh['cubic_sph_rot'][[iso_pos[e] for e in els]] if els else \
+            mesh['cubic_sph_rot'][:0]
+        return element_matrices(sub, visc, dens, **phys)
+
+    with ThreadPoolExecutor(nthreads) as ex:
+        parts = list(ex.map(block, range(nthreads)))
+    return tuple(np.concatenate([p[i] for p in parts]) for i in range(4))
+
+
 # ----------------------------------------------------------------------------------------
 # assembly, rotation, boundary conditions
 # ----------------------------------------------------------------------------------------
@@ -335,13 +362,19 @@ def normdf(x):
 
 
 class CoarseChol:
-    """Dense Cholesky of the coarsest operator (cholesky_factorization / cholesky_solve)."""
+    """Sparse factorisation of the coarsest operator with a minimum-degree ordering, no pivoting
+    (cholesky_factorization.m:227-237: AMD + sparse L L^T; cholesky_solve.m:265-281: two
+    triangular solves). SuperLU in symmetric mode with the diagonal pivots forced factors the SPD
+    matrix as L D L^T-equivalent L U."""
 
     def __init__(self, K):
-        self.c = sla.cho_factor(K.toarray() if sp.issparse(K) else K, lower=True)
+        import scipy.sparse.linalg as spla
+        K = sp.csc_matrix(K)
+        self.lu = spla.splu(K, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0,
+                            options=dict(SymmetricMode=True))
 
     def solve(self, r):
-        return sla.cho_solve(self.c, r, check_finite=False)
+        return self.lu.solve(np.asarray(r, dtype=np.float64))
 
 
 class OmpCSR:
@@ -475,10 +508,10 @@ def rm0space(a):
 class StokesSystem:
     """Rotated, BC-reduced Stokes system + MG hierarchy (flow3d_patera_mg_sph_p.m:182-384)."""
 
-    def __init__(self, levels, visc, dens, ifix, vfix, phys=None):
+    def __init__(self, levels, visc, dens, ifix, vfix, phys=None, nthreads=1):
         phys = phys or {}
         f = levels[0]
-        K, G, Mm, Fb = element_matrices(f, visc, dens, **phys)
+        K, G, Mm, Fb = element_matrices_threaded(f, visc, dens, nthreads, **phys)
         KK, GG, MM, FF = assemble(f, K, G, Mm, Fb)
         RR = rotation_matrix(f['GCOORD'])
         K1 = (RR.T @ KK @ RR).tocsr()

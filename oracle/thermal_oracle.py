@@ -111,7 +111,8 @@ def pcg_diag(A, b, x, tol=1e-8, itmax=500):
     r = b - A @ x
     normdf = lambda v: np.linalg.norm(v) / np.sqrt(len(v))
     tol = tol * normdf(r)
-    if normdf(r) < tol:
+    if normdf(r) < tol or normdf(r) == 0.0:
+        # zero initial residual: converged (pcg_solver_p.m would go on to alpha = 0/0)
         return x, 0
     rd = q = rlast = None
     it = 0
