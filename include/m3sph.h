@@ -270,8 +270,11 @@ M3SPH_API int m3sph_ml_sweep32(m3sph_mesh *mesh, int32_t img, const float *r, co
  * "stream_outer_variant" (warp layout of the double-float kernel, 0-7, default 4),
  * "split_apply" (4-warp per-colour kernels when streaming is off, default 1), "graphs" (CUDA-graph
  * replay of MG-PCG iterations, default 1), "df_outer" (double-float outer operator on the mixed
- * path, default 1), "ml_schedule" (learned smoothing: 0 learned-Jacobi-learned, 1 one learned
- * sweep per side, default; per handle), "ml_omega_pct" (relaxation weight of the learned correction
+ * path, default 1), "ml_schedule" (learned smoothing on the two finest levels: 0 learned-Jacobi-
+ * learned, 1 one learned sweep per side (default), 3 learned + one Jacobi sweep per side; 2 one
+ * learned sweep per side on the finest level only; per handle), "fp32_operator" (finest-level FP32
+ * V-cycle operator: 1 partially assembled, default; 0 streamed stored matrices; takes effect at the
+ * next set-up), "ml_omega_pct" (relaxation weight of the learned correction
  * in percent, 10-300, default 100; per handle), "ml_infer" (learned sweep kernels: 1 fused tcgen05 sweep, default;
  * 0 WMMA tile kernel), "stream_f32_variant" (slot-ring depth / gather warps of the streamed FP32
  * kernel, 0-3, default 0), "coarse_f64_direct_max" (plain FP64 path: coarsest levels up to this many

@@ -339,7 +339,8 @@ __global__ void k_dense_fix_diag(T *A, const uint8_t *mask, int n) {
 // per panel k, with D = A_kk, C = A_:k (saved) and R = D^-1 A_k: :
 //   A_ij -= C_i R_j (i, j outside panel k), A_kj = R_j, A_ik = -C_i D^-1, A_kk = D^-1.
 // Three launches per panel; the rank-128 update is a 128x128-tile GEMM in shared memory with an
-// 8x8 register block per thread. The inner dimension runs in chunks of GJK(T) (32 FP32, 16 FP64)
+// 8x8 register block per thread (16-byte shared loads, K chunks copied with cp.async one chunk
+// ahead of the FMAs). The inner dimension runs in chunks of GJK(T) (32 FP32, 16 FP64)
 // so that the two staged tiles stay near 33 KB.
 // ---------------------------------------------------------------------------------------
 constexpr int GJB = 128;
@@ -378,63 +379,113 @@ __global__ void __launch_bounds__(256) k_gjb_diag(const T *__restrict__ A, int n
 }
 
 // 128x128 tile product acc = X (rows i0.., inner dimension 0..127) * Y (inner, cols j0..), X and Y
-// read through the loaders; 256 threads, thread (ty, tx) owns rows ty + 16a, cols tx + 16b
+// read through the loaders (row / column index fastest across threads, so global reads coalesce
+// and shared stores do not conflict). 256 threads; thread (ty, tx) owns rows 4ty..4ty+3 and
+// 64+4ty..64+4ty+3 and the same columns with tx, read from shared memory as 16-byte vectors
+// (a quarter-warp's vectors are consecutive: no bank conflicts).
+template <typename T> struct GjVec;
+template <> struct GjVec<float> {
+  static __device__ __forceinline__ void ld4(const float *p, float *v) {
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  }
+};
+template <> struct GjVec<double> {
+  static __device__ __forceinline__ void ld4(const double *p, double *v) {
+    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+};
+constexpr int GJ_LD = GJB + 4;       // shared row stride (16-byte aligned rows)
+__device__ __forceinline__ int gj_row(int t, int a) { return (a < 4 ? 0 : 64) + 4 * t + (a & 3); }
+
+// asynchronous 4- or 8-byte global -> shared copies (cp.async), grouped per K chunk
+template <typename T>
+__device__ __forceinline__ void gj_cp(T *dst, const T *src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void gj_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void gj_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// dynamic shared memory of the tile product: two buffers of X and Y chunks
+template <typename T> constexpr size_t gj_tile_smem() { return sizeof(T) * 2 * 2 * GjChunk<T>::K * GJ_LD; }
+
+// the loaders return the source address of an operand element, or nullptr for a zero; chunks of
+// the inner dimension are copied asynchronously one chunk ahead of the FMAs (double buffer)
 template <typename T, typename LX, typename LY>
-__device__ __forceinline__ void gj_tile_mma(T (&acc)[8][8], LX loadx, LY loady) {
-  constexpr int KC = GjChunk<T>::K;
-  __shared__ T xs[GJB][KC + 1];
-  __shared__ T ys[KC][GJB + 1];
+__device__ __forceinline__ void gj_tile_mma(T (&acc)[8][8], LX srcx, LY srcy) {
+  constexpr int KC = GjChunk<T>::K, NCH = GJB / KC;
+  extern __shared__ __align__(16) unsigned char gj_tile_raw[];
+  T(*xs)[KC][GJ_LD] = reinterpret_cast<T(*)[KC][GJ_LD]>(gj_tile_raw);               // [2][KC][GJ_LD]
+  T(*ys)[KC][GJ_LD] = reinterpret_cast<T(*)[KC][GJ_LD]>(gj_tile_raw + sizeof(T) * 2 * KC * GJ_LD);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
 #pragma unroll
   for (int a = 0; a < 8; ++a)
 #pragma unroll
     for (int b = 0; b < 8; ++b) acc[a][b] = T(0);
-  for (int k0 = 0; k0 < GJB; k0 += KC) {
-    __syncthreads();
+  auto issue = [&](int ch) {
+    const int buf = ch & 1, k0 = ch * KC;
     for (int q = threadIdx.x; q < GJB * KC; q += blockDim.x) {
-      const int r = q / KC, m = q % KC;
-      xs[r][m] = loadx(r, k0 + m);
-      const int ym = q / GJB, c = q % GJB;
-      ys[ym][c] = loady(k0 + ym, c);
+      const int r = q % GJB, m = q / GJB;
+      const T *px = srcx(r, k0 + m), *py = srcy(k0 + m, r);
+      if (px) gj_cp(&xs[buf][m][r], px); else xs[buf][m][r] = T(0);
+      if (py) gj_cp(&ys[buf][m][r], py); else ys[buf][m][r] = T(0);
+    }
+    gj_commit();
+  };
+  issue(0);
+  for (int ch = 0; ch < NCH; ++ch) {
+    if (ch + 1 < NCH) {
+      issue(ch + 1);
+      gj_wait<1>();
+    } else {
+      gj_wait<0>();
     }
     __syncthreads();
+    const int buf = ch & 1;
 #pragma unroll 4
     for (int m = 0; m < KC; ++m) {
       T xv[8], yv[8];
-#pragma unroll
-      for (int a = 0; a < 8; ++a) xv[a] = xs[ty + 16 * a][m];
-#pragma unroll
-      for (int b = 0; b < 8; ++b) yv[b] = ys[m][tx + 16 * b];
+      GjVec<T>::ld4(&xs[buf][m][4 * ty], xv);
+      GjVec<T>::ld4(&xs[buf][m][64 + 4 * ty], xv + 4);
+      GjVec<T>::ld4(&ys[buf][m][4 * tx], yv);
+      GjVec<T>::ld4(&ys[buf][m][64 + 4 * tx], yv + 4);
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int b = 0; b < 8; ++b) acc[a][b] += xv[a] * yv[b];
     }
+    __syncthreads();                     // buffer `buf` is refilled by the next issue
   }
 }
 
-// column panel C (n x 128, saved before the update overwrites it) and row panel R = D^-1 A_k:
-// (128 x n); block x handles columns [128x, 128x+128) of R and rows [128x, 128x+128) of C
+// column panel C (n x 128, saved transposed as Ct [128][n] before the update overwrites it) and
+// row panel R = D^-1 A_k: (128 x n); block x handles columns [128x, 128x+128) of R and rows
+// [128x, 128x+128) of C
 template <typename T>
 __global__ void __launch_bounds__(256) k_gjb_panels(const T *__restrict__ A, int n, int kb, int nb,
                                                     const T *__restrict__ Dinv, T *__restrict__ R, T *__restrict__ Cc) {
   const int j0 = blockIdx.x * GJB;
   for (int q = threadIdx.x; q < GJB * GJB; q += blockDim.x) {
-    const int r = q / GJB, c = q % GJB;
+    const int r = q % GJB, c = q / GJB;
     const int i = j0 + r;
-    if (i < n) Cc[(size_t)i * GJB + c] = c < nb ? A[(size_t)i * n + kb + c] : T(0);
+    if (i < n) Cc[(size_t)c * n + i] = c < nb ? A[(size_t)i * n + kb + c] : T(0);
   }
   T acc[8][8];
   gj_tile_mma<T>(
-      acc, [&](int r, int m) { return Dinv[r * GJB + m]; },
-      [&](int m, int c) { return (m < nb && j0 + c < n) ? A[(size_t)(kb + m) * n + j0 + c] : T(0); });
+      acc, [&](int r, int m) -> const T * { return Dinv + r * GJB + m; },
+      [&](int m, int c) -> const T * { return (m < nb && j0 + c < n) ? A + (size_t)(kb + m) * n + j0 + c : nullptr; });
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
 #pragma unroll
   for (int a = 0; a < 8; ++a)
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
-      const int j = j0 + tx + 16 * b;
-      if (j < n) R[(size_t)(ty + 16 * a) * n + j] = acc[a][b];
+      const int j = j0 + gj_row(tx, b);
+      if (j < n) R[(size_t)gj_row(ty, a) * n + j] = acc[a][b];
     }
 }
 
@@ -463,21 +514,21 @@ __global__ void __launch_bounds__(256) k_gjb_update(T *__restrict__ A, int n, in
   }
   T acc[8][8];
   gj_tile_mma<T>(
-      acc, [&](int r, int m) { return (i0 + r < n) ? Cc[(size_t)(i0 + r) * GJB + m] : T(0); },
-      [&](int m, int c) {
-        return colk ? -Dinv[m * GJB + c] : ((j0 + c < n) ? R[(size_t)m * n + j0 + c] : T(0));
+      acc, [&](int r, int m) -> const T * { return (i0 + r < n) ? Cc + (size_t)m * n + i0 + r : nullptr; },
+      [&](int m, int c) -> const T * {
+        return colk ? Dinv + m * GJB + c : ((j0 + c < n) ? R + (size_t)m * n + j0 + c : nullptr);
       });
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
 #pragma unroll
   for (int a = 0; a < 8; ++a) {
-    const int i = i0 + ty + 16 * a;
+    const int i = i0 + gj_row(ty, a);
     if (i >= n) continue;
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
-      const int j = j0 + tx + 16 * b;
+      const int j = j0 + gj_row(tx, b);
       if (j >= n) continue;
       if (colk) {
-        if (j - kb < nb) A[(size_t)i * n + j] = acc[a][b];            // -C D^-1
+        if (j - kb < nb) A[(size_t)i * n + j] = -acc[a][b];           // -C D^-1
       } else {
         A[(size_t)i * n + j] -= acc[a][b];                           // A - C R
       }
@@ -492,11 +543,13 @@ int gj_blocked_inverse(T *A, int n, T *work, cudaStream_t s) {
   const int nbk = (n + GJB - 1) / GJB;
   const size_t dsmem = sizeof(T) * ((size_t)GJB * (GJB + 1) + 2 * GJB);
   M3_CUDA(cudaFuncSetAttribute(k_gjb_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+  M3_CUDA(cudaFuncSetAttribute(k_gjb_panels<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gj_tile_smem<T>()));
+  M3_CUDA(cudaFuncSetAttribute(k_gjb_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gj_tile_smem<T>()));
   for (int k = 0; k < nbk; ++k) {
     const int kb = k * GJB, nb = std::min(GJB, n - kb);
     k_gjb_diag<T><<<1, 256, dsmem, s>>>(A, n, kb, nb, Dinv); count_launch();
-    k_gjb_panels<T><<<nbk, 256, 0, s>>>(A, n, kb, nb, Dinv, R, Cc); count_launch();
-    k_gjb_update<T><<<dim3(nbk, nbk), 256, 0, s>>>(A, n, k, nb, Dinv, R, Cc); count_launch();
+    k_gjb_panels<T><<<nbk, 256, gj_tile_smem<T>(), s>>>(A, n, kb, nb, Dinv, R, Cc); count_launch();
+    k_gjb_update<T><<<dim3(nbk, nbk), 256, gj_tile_smem<T>(), s>>>(A, n, k, nb, Dinv, R, Cc); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;

@@ -686,7 +686,7 @@ __global__ void k_recip(const double *a, double *b, int n) {
 // FP64 coarsest levels up to this many dofs are inverted in FP64; larger ones are refined
 // FP32 V-cycle operator of the finest level: false = streamed stored matrices (K32), true =
 // partially assembled (per-point geometric factors, product formed on the fly)
-static bool g_pa_apply = false;
+static bool g_pa_apply = true;
 static int g_coarse_f64_direct_max = 6000;
 static int g_coarse_refine_sweeps = 3;
 
@@ -971,16 +971,25 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     return M3SPH_OK;
   }
   const bool ml = M->smoother_active;
+  // learned levels: the two finest (schedules 0, 1, 3) or the finest only (schedule 2)
+  const int nml = M->ml_schedule == 2 ? 1 : 2;
+  const bool one = M->ml_schedule == 1 || M->ml_schedule == 2;
   for (int j = 0; j < nm - 1; ++j) {
     const Level &L = M->lev[j];
     const double *w = j == 0 ? WD0 : WDc;
     const size_t n = L.ndof;
-    if (ml && j < 2 && M->ml_schedule == 1) {
+    if (ml && j < nml && one) {
       // one learned sweep from zero, then the residual for the restriction
       M3_CUDA(cudaMemsetAsync(d[j], 0, sizeof(T) * n, s));
       M3_TRY(ml_sweep<T>(M, j, r[j], nullptr, levDi<T>(L), tmp[j], d[j]));
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
-    } else if (ml && j < 2) {
+    } else if (ml && j < nml && M->ml_schedule == 3) {
+      // learned sweep from zero, one weighted Jacobi sweep, residual
+      M3_CUDA(cudaMemsetAsync(d[j], 0, sizeof(T) * n, s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], nullptr, levDi<T>(L), tmp[j], d[j]));
+      M3_TRY(level_op_jac<T>(L, j, (T)w[2], r[j], d[j], kd[j], s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+    } else if (ml && j < nml) {
       // learned sweep, weighted Jacobi sweep, learned sweep
       M3_CUDA(cudaMemsetAsync(d[j], 0, sizeof(T) * n, s));
       M3_TRY(ml_sweep<T>(M, j, r[j], nullptr, levDi<T>(L), tmp[j], d[j]));
@@ -1002,10 +1011,14 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
     const double *w = j == 0 ? WU0 : WUc;
     const size_t n = L.ndof;
     M3_TRY(prolong<T>(L, M->lev[j + 1], d[j + 1], d[j], d[j], s));
-    if (ml && j < 2 && M->ml_schedule == 1) {
+    if (ml && j < nml && one) {
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
       M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
-    } else if (ml && j < 2) {
+    } else if (ml && j < nml && M->ml_schedule == 3) {
+      M3_TRY(level_op_jac<T>(L, j, (T)w[0], r[j], d[j], kd[j], s));
+      M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
+      M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
+    } else if (ml && j < nml) {
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
       M3_TRY(ml_sweep<T>(M, j, r[j], kd[j], levDi<T>(L), tmp[j], d[j]));
       M3_TRY(level_op<T>(L, j, d[j], kd[j], s));
@@ -1949,8 +1962,8 @@ extern "C" int m3sph_set_option(m3sph_mesh *M, const char *name, int32_t value) 
     }
     g_pa_apply = value == 1;
   } else if (n == "ml_schedule") {
-    if (value < 0 || value > 1) {
-      set_error("ml_schedule must be 0 or 1");
+    if (value < 0 || value > 3) {
+      set_error("ml_schedule must be 0..3");
       return M3SPH_ERR_BAD_INPUT;
     }
     M->ml_schedule = value;

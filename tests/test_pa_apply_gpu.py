@@ -24,7 +24,7 @@ def _apply_both(dm, x):
         dm.set_option("fp32_operator", 0)
         yst = dm.level_apply32(0, x)
     finally:
-        dm.set_option("fp32_operator", 0)
+        dm.set_option("fp32_operator", 1)        # the default
     return ys, yst
 
 
@@ -56,7 +56,6 @@ def test_partially_assembled_apply(wl):
         ys2, _ = _apply_both(dm, x2)
         assert np.array_equal(ys2[0], ys[0])
     finally:
-        dm.set_option("fp32_operator", 0)
         dm.close()
 
 
@@ -80,7 +79,7 @@ def test_solve_with_partially_assembled_vcycle(built_lib, smoother):
             U, P, info = dm.solve(**kw)
             res[op] = (U, P - P.mean(), info)
     finally:
-        dm.set_option("fp32_operator", 0)
+        dm.set_option("fp32_operator", 1)
         dm.close()
     (U0, P0, i0), (U1, P1, i1) = res[0], res[1]
     its0, its1 = i0['nitU'] + i0['nitZ'], i1['nitU'] + i1['nitZ']

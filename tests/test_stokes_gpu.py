@@ -209,6 +209,7 @@ def test_streamed_fp32_apply(case):
     from m3tet_sph_gb300 import stokes
     dm2 = stokes.DeviceMesh(w['levels'])
     try:
+        dm2.set_option("fp32_operator", 0)      # the streamed stored matrices
         dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
         rng = np.random.default_rng(11)
         x = np.zeros(S.nU, np.float32)
@@ -220,6 +221,7 @@ def test_streamed_fp32_apply(case):
         assert np.linalg.norm(ys[0] - y_split) < 1e-6 * np.linalg.norm(y_split)
         assert np.linalg.norm(ys[0] - y_ref) < 1e-5 * np.linalg.norm(y_ref)
     finally:
+        dm2.set_option("fp32_operator", 1)
         dm2.close()
 
 
@@ -229,6 +231,7 @@ def test_streamed_fp32_apply_many_chunks(built_lib):
     w = workloads.make_workload('c1')
     dm2 = stokes.DeviceMesh(w['levels'])
     try:
+        dm2.set_option("fp32_operator", 0)      # the streamed stored matrices
         dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
         rng = np.random.default_rng(12)
         x = rng.standard_normal(3 * w['levels'][0]['nnod']).astype(np.float32)
@@ -250,6 +253,7 @@ def test_streamed_fp32_apply_many_chunks(built_lib):
         assert np.linalg.norm(ys[0] - y_split) < 1e-6 * np.linalg.norm(y_split)
         assert np.linalg.norm(ys[0] - y64) < 1e-5 * np.linalg.norm(y64)
     finally:
+        dm2.set_option("fp32_operator", 1)
         dm2.close()
 
 
@@ -260,6 +264,7 @@ def test_streamed_fp32_variants_bit_identical(built_lib):
     w = workloads.make_workload('c1')
     dm2 = stokes.DeviceMesh(w['levels'])
     try:
+        dm2.set_option("fp32_operator", 0)      # the streamed stored matrices
         dm2.setup(w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'], precision=1)
         x = np.random.default_rng(13).standard_normal(3 * w['levels'][0]['nnod']).astype(np.float32)
         y0 = dm2.level_apply32(0, x)
@@ -270,6 +275,7 @@ def test_streamed_fp32_variants_bit_identical(built_lib):
         finally:
             dm2.set_option("stream_f32_variant", 0)
     finally:
+        dm2.set_option("fp32_operator", 1)
         dm2.close()
 
 
