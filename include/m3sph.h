@@ -262,6 +262,15 @@ M3SPH_API int m3sph_ml_forward(m3sph_mesh *mesh, const float *X, int32_t n, floa
 /* One learned sweep of level img (0 or 1) in FP32 as the V-cycle runs it: d += the partition-of-
  * unity sum of the network's element corrections for the residual r - kd (kd may be NULL: r).
  * Host vectors of 3*nnod(img); needs a set-up with precision 1 and parameters loaded. */
+/* Inverse diagonal of the FP32 level-img operator (host, ndof of the level; 0 on fixed dofs): the
+ * scaling of the weighted-Jacobi sweeps (mgpcg_solver_p.m:397-437). */
+M3SPH_API int m3sph_level_inverse_diag32(m3sph_mesh *mesh, int32_t img, float *dinv);
+/* Inputs of the learned smoother on level img (0 or 1) for a Jacobi-scaled residual z (host, FP32,
+ * 3 nnod of that level): X (host, nel x 52, original element order) = the 30 local values of z
+ * divided by their norm, the 10 standardised log-viscosities and the 12 geometry factors;
+ * s_norm (host, nel) = the norms. No reference counterpart (the learned part is new); used to
+ * check the fused sweep's features against a CPU restatement. */
+M3SPH_API int m3sph_ml_features(m3sph_mesh *mesh, int32_t img, const float *z, float *X, float *s_norm);
 M3SPH_API int m3sph_ml_sweep32(m3sph_mesh *mesh, int32_t img, const float *r, const float *kd, float *d);
 
 /* Kernel-variant switches for measurement and tests (per process, results equal to rounding):

@@ -142,6 +142,8 @@ SIGNATURES = {
     "m3sph_ml_gradients": ([P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float), DP], C.c_int),
     "m3sph_ml_forward": ([P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float)], C.c_int),
     "m3sph_ml_sweep32": ([P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
+    "m3sph_level_inverse_diag32": ([P, C.c_int32, C.POINTER(C.c_float)], C.c_int),
+    "m3sph_ml_features": ([P, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
     "m3sph_set_option": ([P, C.c_char_p, C.c_int32], C.c_int),
     "m3sph_launch_count": ([C.POINTER(C.c_ulonglong)], C.c_int),
     "m3sph_apply_timing": ([P, C.c_int32, C.c_int32, C.c_int32, DP], C.c_int),

@@ -161,6 +161,9 @@ struct Finest {
 
 struct Coarse {
   int n = 0;                          // dofs of the coarsest level
+  int nf = 0;                         // its free dofs: the dense inverse is nf x nf
+  int *fidx = nullptr;                // [nf] compact -> level dof
+  int *cmap = nullptr;                // [n] level dof -> compact index, -1 for a fixed dof
   double *A64 = nullptr;              // dense inverse (n x n)
   float *A32 = nullptr;
   bool refine64 = false;              // FP64 path: FP32 inverse + iterative refinement against B64

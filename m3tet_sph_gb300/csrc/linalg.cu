@@ -316,23 +316,26 @@ template int prolong<float>(const Level &, const Level &, const float *, const f
 // ---------------------------------------------------------------------------------------
 // dense matrix from the level's 3x3-block rows (blocks [9][nnzb]): every entry is written once, so
 // the result does not depend on the order in which threads run
+// rows and columns of fixed dofs are left out: the matrix is the free-dof block, nf x nf, through
+// the compact map cmap (-1 for a fixed dof)
 template <typename T>
 __global__ void k_dense_from_bsr(const int *__restrict__ ptr, const int *__restrict__ col, const T *__restrict__ B,
-                                 int nrow, size_t nnzb, int n, T *__restrict__ A) {
+                                 int nrow, size_t nnzb, const int *__restrict__ cmap, int nf, T *__restrict__ A) {
   const int i = blockIdx.x;
   if (i >= nrow) return;
   for (int k = ptr[i] + threadIdx.x; k < ptr[i + 1]; k += blockDim.x) {
     const int j = col[k];
 #pragma unroll
-    for (int p = 0; p < 3; ++p)
+    for (int p = 0; p < 3; ++p) {
+      const int a = cmap[3 * i + p];
+      if (a < 0) continue;
 #pragma unroll
-      for (int q = 0; q < 3; ++q) A[(size_t)(3 * i + p) * n + 3 * j + q] = B[(size_t)(p * 3 + q) * nnzb + k];
+      for (int q = 0; q < 3; ++q) {
+        const int b = cmap[3 * j + q];
+        if (b >= 0) A[(size_t)a * nf + b] = B[(size_t)(p * 3 + q) * nnzb + k];
+      }
+    }
   }
-}
-template <typename T>
-__global__ void k_dense_fix_diag(T *A, const uint8_t *mask, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && !mask[i]) A[(size_t)i * n + i] = T(1);
 }
 // ---------------------------------------------------------------------------------------
 // blocked Gauss-Jordan inverse of the SPD coarsest matrix, 128-wide panels (no pivoting):
@@ -557,41 +560,43 @@ int gj_blocked_inverse(T *A, int n, T *work, cudaStream_t s) {
 
 // dense coarse matrix (from the level's block rows) and its blocked Gauss-Jordan inverse; with a
 // `lowp` target the FP64 matrix is rounded to FP32 first and A receives nothing
+// free-dof inverse of the level matrix: A (nf x nf) = (K restricted to the free dofs)^-1
 template <typename T>
-int dense_inverse_blocked(const Level &L, const T *B, T *A, T *work, cudaStream_t s) {
-  const int n = L.ndof;
-  M3_CUDA(cudaMemsetAsync(A, 0, sizeof(T) * (size_t)n * n, s));
-  k_dense_from_bsr<T><<<L.nnod, 64, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, (size_t)L.nnzb, n, A); count_launch();
-  k_dense_fix_diag<T><<<(n + 255) / 256, 256, 0, s>>>(A, L.freemask, n); count_launch();
-  return gj_blocked_inverse<T>(A, n, work, s);
+int dense_inverse_blocked(const Level &L, const T *B, T *A, T *work, const int *cmap, int nf, cudaStream_t s) {
+  M3_CUDA(cudaMemsetAsync(A, 0, sizeof(T) * (size_t)nf * nf, s));
+  k_dense_from_bsr<T><<<L.nnod, 64, 0, s>>>(L.bsr_ptr, L.bsr_col, B, L.nnod, (size_t)L.nnzb, cmap, nf, A); count_launch();
+  return gj_blocked_inverse<T>(A, nf, work, s);
 }
-template int dense_inverse_blocked<double>(const Level &, const double *, double *, double *, cudaStream_t);
-template int dense_inverse_blocked<float>(const Level &, const float *, float *, float *, cudaStream_t);
+template int dense_inverse_blocked<double>(const Level &, const double *, double *, double *, const int *, int,
+                                           cudaStream_t);
+template int dense_inverse_blocked<float>(const Level &, const float *, float *, float *, const int *, int,
+                                          cudaStream_t);
 
-// y = A x masked (one warp per row)
+// y[fidx[row]] = sum_j A[row][j] x[fidx[j]] over the nf free dofs (one warp per row); the fixed
+// entries of y are zeroed beforehand
 template <typename T>
-__global__ void k_dense_gemv(const T *__restrict__ A, int n, const T *__restrict__ x, const uint8_t *__restrict__ mask,
+__global__ void k_dense_gemv(const T *__restrict__ A, int nf, const int *__restrict__ fidx, const T *__restrict__ x,
                              T *__restrict__ y) {
   const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (row >= n) return;
+  if (row >= nf) return;
   T s = 0;
-  for (int j = lane; j < n; j += 32) s += A[(size_t)row * n + j] * x[j];
+  for (int j = lane; j < nf; j += 32) s += A[(size_t)row * nf + j] * x[fidx[j]];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) y[row] = mask[row] ? s : T(0);
+  if (lane == 0) y[fidx[row]] = s;
 }
-// y (FP64) = A (FP32) x (FP64) masked, FP64 accumulation: the refined FP64 coarse solve
-__global__ void k_dense_gemv_mixed(const float *__restrict__ A, int n, const double *__restrict__ x,
-                                   const uint8_t *__restrict__ mask, double *__restrict__ y, int accumulate) {
+// the same with A in FP32 and x, y in FP64 (FP64 accumulation): the refined FP64 coarse solve
+__global__ void k_dense_gemv_mixed(const float *__restrict__ A, int nf, const int *__restrict__ fidx,
+                                   const double *__restrict__ x, double *__restrict__ y, int accumulate) {
   const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (row >= n) return;
+  if (row >= nf) return;
   double s = 0.0;
-  for (int j = lane; j < n; j += 32) s += (double)A[(size_t)row * n + j] * x[j];
+  for (int j = lane; j < nf; j += 32) s += (double)A[(size_t)row * nf + j] * x[fidx[j]];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) y[row] = mask[row] ? (accumulate ? y[row] + s : s) : 0.0;
+  if (lane == 0) y[fidx[row]] = accumulate ? y[fidx[row]] + s : s;
 }
 __global__ void k_sub_masked(const double *a, const double *b, const uint8_t *mask, double *out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -602,14 +607,15 @@ template <typename T> int bsr_apply(const Level &L, const T *B, const T *x, T *y
 // FP64 coarse solve d = A^-1 r from the FP32 inverse A32 and the FP64 operator B64 of the coarsest
 // level: d = A32 r, then `sweeps` steps of iterative refinement d += A32 (r - A d)
 int coarse_refined(const Level &L, const float *A32, const double *B64, const double *r, double *d, double *t,
-                   int sweeps, cudaStream_t s) {
+                   int sweeps, const int *fidx, int nf, cudaStream_t s) {
   const int n = L.ndof;
-  const unsigned g = (unsigned)((n + 7) / 8);
-  k_dense_gemv_mixed<<<g, 256, 0, s>>>(A32, n, r, L.freemask, d, 0); count_launch();
+  const unsigned g = (unsigned)((nf + 7) / 8);
+  M3_CUDA(cudaMemsetAsync(d, 0, sizeof(double) * n, s));
+  k_dense_gemv_mixed<<<g, 256, 0, s>>>(A32, nf, fidx, r, d, 0); count_launch();
   for (int k = 0; k < sweeps; ++k) {
     M3_TRY(bsr_apply<double>(L, B64, d, t, s));
     k_sub_masked<<<(n + 255) / 256, 256, 0, s>>>(r, t, L.freemask, t, n); count_launch();
-    k_dense_gemv_mixed<<<g, 256, 0, s>>>(A32, n, t, L.freemask, d, 1); count_launch();
+    k_dense_gemv_mixed<<<g, 256, 0, s>>>(A32, nf, fidx, t, d, 1); count_launch();
   }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
@@ -620,19 +626,25 @@ __global__ void k_d2f_n(const double *a, float *b, size_t n) {
   if (i < n) b[i] = (float)a[i];
 }
 // FP32 inverse of the FP64 coarsest operator (its blocks rounded to FP32)
-int dense_inverse_from64(const Level &L, const double *B64, float *B32tmp, float *A, float *work, cudaStream_t s) {
+int dense_inverse_from64(const Level &L, const double *B64, float *B32tmp, float *A, float *work, const int *cmap,
+                         int nf, cudaStream_t s) {
   const size_t nb = 9 * (size_t)L.nnzb;
   k_d2f_n<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B64, B32tmp, nb); count_launch();
-  return dense_inverse_blocked<float>(L, B32tmp, A, work, s);
+  return dense_inverse_blocked<float>(L, B32tmp, A, work, cmap, nf, s);
 }
 
+// d = A^-1 r on the free dofs, 0 on the fixed ones
 template <typename T>
-int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s) {
-  k_dense_gemv<T><<<(n + 7) / 8, 256, 0, s>>>(A, n, x, mask, y); count_launch();
+int dense_gemv(const T *A, int n, int nf, const int *fidx, const T *x, T *y, cudaStream_t s) {
+  M3_CUDA(cudaMemsetAsync(y, 0, sizeof(T) * n, s));
+  if (nf > 0) {
+    k_dense_gemv<T><<<(nf + 7) / 8, 256, 0, s>>>(A, nf, fidx, x, y);
+    count_launch();
+  }
   M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
-template int dense_gemv<double>(const double *, int, const double *, const uint8_t *, double *, cudaStream_t);
-template int dense_gemv<float>(const float *, int, const float *, const uint8_t *, float *, cudaStream_t);
+template int dense_gemv<double>(const double *, int, int, const int *, const double *, double *, cudaStream_t);
+template int dense_gemv<float>(const float *, int, int, const int *, const float *, float *, cudaStream_t);
 
 }  // namespace m3sph

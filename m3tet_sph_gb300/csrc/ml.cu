@@ -313,11 +313,11 @@ __device__ __forceinline__ bool tc_bar_wait(uint32_t bar, uint32_t parity) {
   }
 }
 
-// features of element e as 32 BF16 pairs from the Jacobi-scaled residual z = (r0 - kd) Dinv
-// (same arithmetic and order as element_features)
-__device__ __forceinline__ float element_features_packed(const FeatLevel &L, int e, const float *__restrict__ z,
-                                                         uint32_t (&xp)[32]) {
-  float rt[30];
+// the 52 FP32 features of element e from the Jacobi-scaled residual z = (r0 - kd) Dinv: the 30
+// local values divided by their norm s, the 10 standardised log-viscosities, the 12 geometry
+// factors; returns s (same arithmetic and order as element_features)
+__device__ __forceinline__ float element_features_f32(const FeatLevel &L, int e, const float *__restrict__ z,
+                                                      float (&x)[IN]) {
   float s2 = 0.f;
 #pragma unroll
   for (int n = 0; n < 10; ++n) {
@@ -325,21 +325,45 @@ __device__ __forceinline__ float element_features_packed(const FeatLevel &L, int
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const float v = z[3 * nod + c];
-      rt[3 * n + c] = v;
+      x[3 * n + c] = v;
       s2 += v * v;
     }
   }
   const float s = sqrtf(s2);
   const float is = s > 0.f ? 1.0f / s : 0.f;
 #pragma unroll
-  for (int q = 0; q < 15; ++q) xp[q] = tc_pack(rt[2 * q] * is, rt[2 * q + 1] * is);
+  for (int q = 0; q < 30; ++q) x[q] *= is;
 #pragma unroll
-  for (int q = 0; q < 5; ++q) xp[15 + q] = tc_pack(L.lvisc[(size_t)(2 * q) * L.nel + e], L.lvisc[(size_t)(2 * q + 1) * L.nel + e]);
+  for (int q = 0; q < 10; ++q) x[30 + q] = L.lvisc[(size_t)q * L.nel + e];
 #pragma unroll
-  for (int q = 0; q < 6; ++q) xp[20 + q] = tc_pack(L.geo[(size_t)(2 * q) * L.nel + e], L.geo[(size_t)(2 * q + 1) * L.nel + e]);
-#pragma unroll
-  for (int q = 26; q < 32; ++q) xp[q] = 0u;
+  for (int q = 0; q < 12; ++q) x[40 + q] = L.geo[(size_t)q * L.nel + e];
   return s;
+}
+
+// the same as 32 BF16 pairs (the sweep's A-operand row)
+__device__ __forceinline__ float element_features_packed(const FeatLevel &L, int e, const float *__restrict__ z,
+                                                         uint32_t (&xp)[32]) {
+  float x[IN];
+  const float s = element_features_f32(L, e, z, x);
+#pragma unroll
+  for (int q = 0; q < IN / 2; ++q) xp[q] = tc_pack(x[2 * q], x[2 * q + 1]);
+#pragma unroll
+  for (int q = IN / 2; q < 32; ++q) xp[q] = 0u;
+  return s;
+}
+
+// features of every element of a level in original element order (rows of IN values) and the
+// residual norms s, for checks against a CPU restatement
+__global__ void k_ml_feature_rows(FeatLevel L, const int *__restrict__ perm, const float *__restrict__ z,
+                                  float *__restrict__ X, float *__restrict__ S) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= L.nel) return;
+  float x[IN];
+  const float s = element_features_f32(L, e, z, x);
+  const int o = perm[e];
+#pragma unroll
+  for (int q = 0; q < IN; ++q) X[(size_t)o * IN + q] = x[q];
+  S[o] = s;
 }
 
 // z = (r0 - kd) Dinv in FP32 (kd may be null), the per-dof input of the features
@@ -1062,6 +1086,17 @@ int ml_add_samples(m3sph_mesh *M, const double *r, const double *err, int stride
   count_launch();
   M3_CUDA(cudaGetLastError());
   S->count = std::min<long>(S->cap, S->count + n);
+  return M3SPH_OK;
+}
+
+// features of level j (z: Jacobi-scaled residual, device, 3 nnod) into X [nel][IN] and S [nel]
+int ml_feature_rows(m3sph_mesh *M, int j, const float *z, float *X, float *Sn) {
+  MlState *S = mls(M);
+  Level &L = M->lev[j];
+  FeatLevel f{L.nel, L.el2nod, S->lev[j].lvisc, S->lev[j].geo};
+  k_ml_feature_rows<<<(L.nel + 127) / 128, 128, 0, M->stream>>>(f, L.perm, z, X, Sn);
+  count_launch();
+  M3_CUDA(cudaGetLastError());
   return M3SPH_OK;
 }
 

@@ -37,6 +37,7 @@ int stream_apply_df(const Level &L, const float *Kh, const float *Kl, const doub
 int stream_apply_f64(const Level &L, const double *K, const double *x, double *y, cudaStream_t s);
 int stream_check(const Level &L, cudaStream_t s);
 int pa_upload_tables();
+int ml_feature_rows(m3sph_mesh *M, int j, const float *z, float *X, float *Sn);
 int pa_row_stride(int nel);
 int pa_build_trig(const double *RR, int nnod, float4 *trig, cudaStream_t s);
 int pa_apply_f32(const Level &L, const float *x, float *y, cudaStream_t s);
@@ -66,11 +67,13 @@ template <typename T> int jac_first(T w, const T *r0, const T *Di, T *d, size_t 
 template <typename T> int jac(T w, const T *r0, const T *Kd, const T *Di, T *d, size_t n, cudaStream_t s);
 template <typename T> int restrict_(const Level &F, const Level &C, const T *a, const T *b, T *out, cudaStream_t s);
 template <typename T> int prolong(const Level &F, const Level &C, const T *xc, const T *add, T *out, cudaStream_t s);
-template <typename T> int dense_inverse_blocked(const Level &L, const T *B, T *A, T *work, cudaStream_t s);
-int dense_inverse_from64(const Level &L, const double *B64, float *B32tmp, float *A, float *work, cudaStream_t s);
+template <typename T>
+int dense_inverse_blocked(const Level &L, const T *B, T *A, T *work, const int *cmap, int nf, cudaStream_t s);
+int dense_inverse_from64(const Level &L, const double *B64, float *B32tmp, float *A, float *work, const int *cmap,
+                         int nf, cudaStream_t s);
 int coarse_refined(const Level &L, const float *A32, const double *B64, const double *r, double *d, double *t,
-                   int sweeps, cudaStream_t s);
-template <typename T> int dense_gemv(const T *A, int n, const T *x, const uint8_t *mask, T *y, cudaStream_t s);
+                   int sweeps, const int *fidx, int nf, cudaStream_t s);
+template <typename T> int dense_gemv(const T *A, int n, int nf, const int *fidx, const T *x, T *y, cudaStream_t s);
 size_t element_setup_smem();
 
 // ---- errors and counters ----
@@ -444,6 +447,10 @@ extern "C" int m3sph_mesh_destroy(m3sph_mesh *M) {
     dfree(p);
   dfree(M->coarse.A64);
   dfree(M->coarse.A32);
+  dfree(M->coarse.cmap);
+  dfree(M->coarse.fidx);
+  dfree(M->coarse.B32tmp);
+  dfree(M->coarse.t64);
   dfree(M->Ufix);
   dfree(M->bc_rhs);
   dfree(M->red);
@@ -785,19 +792,40 @@ static int rebuild_operator(m3sph_mesh *M) {
   }
   M->coarse.n = nc;
   M->coarse.refine64 = false;
+  {
+    // free dofs of the coarsest level: the dense inverse covers only them
+    std::vector<uint8_t> fm(nc);
+    M3_CUDA(cudaMemcpyAsync(fm.data(), Lc.freemask, nc, cudaMemcpyDeviceToHost, s));
+    M3_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> cmap(nc, -1), fidx;
+    fidx.reserve(nc);
+    for (int i = 0; i < nc; ++i)
+      if (fm[i]) {
+        cmap[i] = (int)fidx.size();
+        fidx.push_back(i);
+      }
+    if (!M->coarse.cmap) M3_TRY(dalloc(&M->coarse.cmap, (size_t)nc));
+    if (!M->coarse.fidx) M3_TRY(dalloc(&M->coarse.fidx, (size_t)nc));
+    M->coarse.nf = (int)fidx.size();
+    M3_CUDA(cudaMemcpyAsync(M->coarse.cmap, cmap.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+    if (!fidx.empty())
+      M3_CUDA(cudaMemcpyAsync(M->coarse.fidx, fidx.data(), sizeof(int) * fidx.size(), cudaMemcpyHostToDevice, s));
+    M3_CUDA(cudaStreamSynchronize(s));
+  }
+  const int nf = M->coarse.nf;
   if (M->nmg > 1) {
     if (M->precision == 0 && nc <= g_coarse_f64_direct_max) {
       if (!M->coarse.A64) M3_TRY(dalloc(&M->coarse.A64, (size_t)nc * nc));
-      M3_TRY(dense_inverse_blocked<double>(Lc, Lc.B64, M->coarse.A64, W->cwork64, s));
+      M3_TRY(dense_inverse_blocked<double>(Lc, Lc.B64, M->coarse.A64, W->cwork64, M->coarse.cmap, nf, s));
     } else if (M->precision == 0) {
       M->coarse.refine64 = true;
       if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
       if (!M->coarse.B32tmp) M3_TRY(dalloc(&M->coarse.B32tmp, 9 * (size_t)Lc.nnzb));
       if (!M->coarse.t64) M3_TRY(dalloc(&M->coarse.t64, (size_t)nc));
-      M3_TRY(dense_inverse_from64(Lc, Lc.B64, M->coarse.B32tmp, M->coarse.A32, W->cwork32, s));
+      M3_TRY(dense_inverse_from64(Lc, Lc.B64, M->coarse.B32tmp, M->coarse.A32, W->cwork32, M->coarse.cmap, nf, s));
     } else {
       if (!M->coarse.A32) M3_TRY(dalloc(&M->coarse.A32, (size_t)nc * nc));
-      M3_TRY(dense_inverse_blocked<float>(Lc, Lc.B32, M->coarse.A32, W->cwork32, s));
+      M3_TRY(dense_inverse_blocked<float>(Lc, Lc.B32, M->coarse.A32, W->cwork32, M->coarse.cmap, nf, s));
     }
   }
   return M3SPH_OK;
@@ -956,9 +984,10 @@ static int coarse_solve(m3sph_mesh *M, const T *Ainv, const T *r, T *d) {
   const Level &Lc = M->lev[M->nmg - 1];
   if constexpr (std::is_same<T, double>::value) {
     if (M->coarse.refine64)
-      return coarse_refined(Lc, M->coarse.A32, Lc.B64, r, d, M->coarse.t64, g_coarse_refine_sweeps, M->stream);
+      return coarse_refined(Lc, M->coarse.A32, Lc.B64, r, d, M->coarse.t64, g_coarse_refine_sweeps, M->coarse.fidx,
+                            M->coarse.nf, M->stream);
   }
-  return dense_gemv<T>(Ainv, M->coarse.n, r, Lc.freemask, d, M->stream);
+  return dense_gemv<T>(Ainv, M->coarse.n, M->coarse.nf, M->coarse.fidx, r, d, M->stream);
 }
 
 template <typename T>
@@ -967,7 +996,7 @@ static int vcycle_T(m3sph_mesh *M, std::vector<T *> &r, std::vector<T *> &d, std
   cudaStream_t s = M->stream;
   const int nm = M->nmg;
   if (nm == 1) {
-    M3_TRY(dense_gemv<T>(Ainv, M->coarse.n, r[0], M->lev[0].freemask, d[0], s));
+    M3_TRY(dense_gemv<T>(Ainv, M->coarse.n, M->coarse.nf, M->coarse.fidx, r[0], d[0], s));
     return M3SPH_OK;
   }
   const bool ml = M->smoother_active;
@@ -1794,6 +1823,50 @@ extern "C" int m3sph_ml_sweep32(m3sph_mesh *M, int32_t img, const float *r, cons
   M3_CUDA(cudaMemcpyAsync(d, W->d32[img], sizeof(float) * n, cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
   return ml_check(M);
+}
+
+extern "C" int m3sph_level_inverse_diag32(m3sph_mesh *M, int32_t img, float *dinv) {
+  M3_TRY(need_op(M));
+  if (img < 0 || img >= M->nmg || !dinv || !M->lev[img].Dinv32) {
+    set_error("m3sph_level_inverse_diag32: level out of range or no FP32 operator (set up with precision 1)");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  const Level &L = M->lev[img];
+  M3_CUDA(cudaMemcpyAsync(dinv, L.Dinv32, sizeof(float) * L.ndof, cudaMemcpyDeviceToHost, M->stream));
+  M3_CUDA(cudaStreamSynchronize(M->stream));
+  return M3SPH_OK;
+}
+
+extern "C" int m3sph_ml_features(m3sph_mesh *M, int32_t img, const float *z, float *X, float *s_norm) {
+  M3_TRY(need_op(M));
+  if (!M->ml || img < 0 || img >= std::min(2, M->nmg) || !z || !X || !s_norm) {
+    set_error("m3sph_ml_features: no learned smoother on this level or bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Level &L = M->lev[img];
+  cudaStream_t s = M->stream;
+  float *dz = nullptr, *dX = nullptr, *dS = nullptr;
+  const size_t n = L.ndof;
+  auto release = [&]() {
+    if (dz) cudaFree(dz);
+    if (dX) cudaFree(dX);
+    if (dS) cudaFree(dS);
+  };
+  if (cudaMalloc((void **)&dz, sizeof(float) * n) != cudaSuccess ||
+      cudaMalloc((void **)&dX, sizeof(float) * 52 * (size_t)L.nel) != cudaSuccess ||
+      cudaMalloc((void **)&dS, sizeof(float) * (size_t)L.nel) != cudaSuccess) {
+    release();
+    return cuda_fail(cudaGetLastError(), "m3sph_ml_features allocation");
+  }
+  int st = M3SPH_OK;
+  if (cudaMemcpyAsync(dz, z, sizeof(float) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) st = M3SPH_ERR_CUDA;
+  if (!st) st = ml_feature_rows(M, img, dz, dX, dS);
+  if (!st && (cudaMemcpyAsync(X, dX, sizeof(float) * 52 * (size_t)L.nel, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+              cudaMemcpyAsync(s_norm, dS, sizeof(float) * (size_t)L.nel, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+              cudaStreamSynchronize(s) != cudaSuccess))
+    st = cuda_fail(cudaGetLastError(), "m3sph_ml_features copy");
+  release();
+  return st;
 }
 
 extern "C" int m3sph_transfer_matrix(const m3sph_mesh *M, int32_t img, int64_t *nnz, int32_t *rows, int32_t *cols,

@@ -61,6 +61,17 @@ def sweep32(dm, level, r, d, kd=None):
     return out
 
 
+def features(dm, level, z):
+    """Inputs of the learned smoother on `level` for a Jacobi-scaled residual z (m3sph_ml_features):
+    (X [nel][52] in original element order, residual norms s [nel])."""
+    z = np.ascontiguousarray(z, dtype=np.float32)
+    nel = dm.levels[level]['nel']
+    X = np.zeros((nel, 52), np.float32)
+    s = np.zeros(nel, np.float32)
+    L.check(L.lib().m3sph_ml_features(dm.h, int(level), L.fptr(z), L.fptr(X), L.fptr(s)))
+    return X, s
+
+
 def gradients(dm, X, T):
     X = np.ascontiguousarray(X, dtype=np.float32)
     T = np.ascontiguousarray(T, dtype=np.float32)

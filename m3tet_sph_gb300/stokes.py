@@ -130,6 +130,12 @@ class DeviceMesh:
         L.check(L.lib().m3sph_level_apply32(self.h, img, L.fptr(x), L.fptr(y)))
         return y
 
+    def level_inverse_diag32(self, img):
+        """Inverse diagonal of the FP32 level operator (0 on fixed dofs), rotated dof-interleaved."""
+        d = np.empty(3 * self.levels[img]['GCOORD'].shape[1], np.float32)
+        L.check(L.lib().m3sph_level_inverse_diag32(self.h, img, L.fptr(d)))
+        return d
+
     def transfer_matrix(self, img):
         """intermesh_transfer_matrix of levels img -> img+1 as a scipy CSR matrix (scalar Ic2f)."""
         import scipy.sparse as sp
