@@ -544,10 +544,14 @@ def sl_rates(args):
         t = time.perf_counter()
         _, _, info = A.tsearch2_sph(dm, pts)
         t_loc = time.perf_counter() - t
+        ms_dev, _ = A.locate_timing(dm, pts, 5)
     finally:
         dm.close()
     return {"sl_step": step,
             "location_sweep": {"points": args.sweep_points, "s": t_loc, "points_per_s": args.sweep_points / t_loc,
+                               "device_s": ms_dev / 1e3, "device_points_per_s": args.sweep_points / (ms_dev * 1e-3),
+                               "basis": "s: public API with host arrays (copies and layout changes included); "
+                                        "device_s: device-resident location (CUDA events)",
                                "locate": info}}
 
 

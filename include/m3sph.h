@@ -303,6 +303,11 @@ M3SPH_API int m3sph_apply_timing(m3sph_mesh *mesh, int32_t img, int32_t precisio
  * (theta,phi,r) triplets (npt x 3). els_guess (1-based, may be NULL) seeds the neighbour walk. */
 M3SPH_API int m3sph_tsearch_sph(m3sph_mesh *mesh, const double *thphr, int32_t npt, const int32_t *els_guess,
                                 int32_t *els_out, double *lc_out, m3sph_locate_info *info);
+/* Location benchmark: the points (npt x 3, as for m3sph_tsearch_sph) are uploaded once, then nrep
+ * device-resident locations (walk, ring resolution, brute force, counts) are timed with CUDA events;
+ * *ms = mean time per location, info = counts of the last one. */
+M3SPH_API int m3sph_locate_timing(m3sph_mesh *mesh, const double *thphr, int32_t npt, int32_t nrep, double *ms,
+                                  m3sph_locate_info *info);
 /* Replaces interp3d_tet (interp3d_tet.m:39-69): V is nnod x nvar (nvar <= 3), Vi npt x nvar. */
 M3SPH_API int m3sph_interp3d_tet(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
                                  const double *V, int32_t nvar, int32_t monotonic, double *Vi);

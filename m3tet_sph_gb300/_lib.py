@@ -128,6 +128,7 @@ SIGNATURES = {
     "m3sph_set_pressure": ([P, DP], C.c_int),
     "m3sph_stream": ([P, C.POINTER(P)], C.c_int),
     "m3sph_tsearch_sph": ([P, DP, C.c_int32, IP, IP, DP, C.POINTER(LocateInfo)], C.c_int),
+    "m3sph_locate_timing": ([P, DP, C.c_int32, C.c_int32, DP, C.POINTER(LocateInfo)], C.c_int),
     "m3sph_interp3d_tet": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_interp3d_cubic": ([P, IP, DP, C.c_int32, DP, C.c_int32, C.c_int32, DP], C.c_int),
     "m3sph_interp3d_cubic_noalloc": ([P, P, P, C.c_int32, P, C.c_int32, C.c_int32, P], C.c_int),

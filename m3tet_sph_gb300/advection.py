@@ -36,6 +36,16 @@ def tsearch2_sph(dm, gTH_PT, els_guess=None):
     return els, lc.T.copy(), info.as_dict()
 
 
+def locate_timing(dm, gTH_PT, nrep=5):
+    """Device-resident location of points (3,npt) in (theta,phi,r), timed with CUDA events after one
+    upload (m3sph_locate_timing): (ms per location, info of the last one)."""
+    P = np.ascontiguousarray(np.asarray(gTH_PT, dtype=np.float64).T)
+    ms = C.c_double()
+    info = L.LocateInfo()
+    L.check(L.lib().m3sph_locate_timing(dm.h, L.dptr(P), P.shape[0], int(nrep), C.byref(ms), C.byref(info)))
+    return ms.value, info.as_dict()
+
+
 def interp3d_tet(dm, els, lc, V, monotonic=False):
     V = np.asarray(V, dtype=np.float64)
     V2 = V[:, None] if V.ndim == 1 else V

@@ -253,8 +253,30 @@ struct GapBest {
 
 // one element of a ring or of the brute-force set: a candidate (within the tie band, appended to the
 // warp's shared list; the rule does not depend on the order) or a gap contender
-__device__ __forceinline__ void eval_shared(const SlmMesh &m, int e, const PointFrames &f, int *ids, uint8_t *fl,
-                                            int *n, GapBest &G) {
+// an FP32 pre-filter skips the FP64 evaluation of elements the point is far from: FP32 barycentrics
+// err by ~1e-5 here, so an element whose FP32 need exceeds the largest gap tolerance by PRE_MARGIN
+// can be neither a tie candidate nor a gap contender in FP64
+constexpr float PRE_MARGIN = 1e-3f;
+__device__ __forceinline__ PointFramesT<float> frames_f32(const PointFrames &f) {
+  PointFramesT<float> g;
+  for (int k = 0; k < 3; ++k) {
+    g.p0[k] = (float)f.p0[k];
+    g.pz[k] = (float)f.pz[k];
+    g.px[k] = (float)f.px[k];
+  }
+  return g;
+}
+__device__ __forceinline__ void eval_shared(const SlmMesh &m, int e, const PointFrames &f,
+                                            const PointFramesT<float> &g, int *ids, uint8_t *fl, int *n,
+                                            GapBest &G) {
+  {
+    float l[3];
+    local_coords_t<float>(m, m.S0f, m.SZf, m.SXf, e, g, l);
+    const float l4 = 1.0f - l[0] - l[1] - l[2];
+    const float nf = fmaxf(fmaxf(-fminf(fminf(l[0], l[1]), fminf(l[2], l4)), 0.0f),
+                           fmaxf(fmaxf(l[0], l[1]), fmaxf(l[2], l4)) - 1.0f);
+    if (nf > (float)((GAP_QMAX + 1) * GAP_STEP) + PRE_MARGIN) return;   // NaN falls through to FP64
+  }
   double lc[3], mn, mx;
   int am;
   const double step = local_coords(m, e, f, lc);
@@ -356,6 +378,7 @@ __global__ void __launch_bounds__(RING_WARPS * 32) k_resolve_ring(SlmMesh m, con
   if (lane == 0) s_n[wl] = 0;
   PointFrames f;
   point_frames(P[i], P[npt + i], P[2 * npt + i], f);
+  const PointFramesT<float> g32 = frames_f32(f);
   int v0[4], len[4];
   for (int k = 0; k < 4; ++k) {
     v0[k] = m.el2nod[(size_t)k * m.nel + e0];
@@ -375,7 +398,7 @@ __global__ void __launch_bounds__(RING_WARPS * 32) k_resolve_ring(SlmMesh m, con
         const int v = m.el2nod[(size_t)j * m.nel + e1];
         for (int kk = 0; kk < k; ++kk) dup |= v == v0[kk];
       }
-      if (!dup) eval_shared(m, e1, f, s_id[wl], s_fl[wl], &s_n[wl], G);
+      if (!dup) eval_shared(m, e1, f, g32, s_id[wl], s_fl[wl], &s_n[wl], G);
     }
   } else {
     // vertices of the 1-ring, deduplicated in a shared hash table (-1 = empty)
@@ -417,7 +440,7 @@ __global__ void __launch_bounds__(RING_WARPS * 32) k_resolve_ring(SlmMesh m, con
             h = (h + 1) % RING_VTAB;
           }
         }
-        if (!dup) eval_shared(m, e1, f, s_id[wl], s_fl[wl], &s_n[wl], G);
+        if (!dup) eval_shared(m, e1, f, g32, s_id[wl], s_fl[wl], &s_n[wl], G);
       }
     }
   }
@@ -561,7 +584,8 @@ __global__ void __launch_bounds__(BRUTE_WARPS * 32) k_locate_brute(SlmMesh m, co
   PointFrames f;
   point_frames(P[i], P[npt + i], P[2 * npt + i], f);
   GapBest G;
-  for (int e = lane; e < m.nel; e += 32) eval_shared(m, e, f, s_id[wl], s_fl[wl], &s_n[wl], G);
+  const PointFramesT<float> g32 = frames_f32(f);
+  for (int e = lane; e < m.nel; e += 32) eval_shared(m, e, f, g32, s_id[wl], s_fl[wl], &s_n[wl], G);
   __syncwarp();
   int q;
   const int gap_e = gap_reduce(G, q);
@@ -817,7 +841,8 @@ struct SlmState {
   int *el2nod = nullptr, *nbr = nullptr, *v2e_ptr = nullptr, *v2e = nullptr, *node_guess = nullptr, *grid = nullptr;
   float *S0f = nullptr, *SZf = nullptr, *SXf = nullptr;
   uint8_t *cls = nullptr, *iface = nullptr;
-  int *ring_count = nullptr;          // points listed for k_resolve_ring
+  int *ring_count = nullptr;          // [16]: 0 points listed for k_resolve_ring, 1 for the brute force,
+                                      // 2.. status counts (k_status_counts)
   double *S0 = nullptr, *SZ = nullptr, *SX = nullptr;
   // work
   double *P = nullptr, *lc = nullptr, *V = nullptr, *out = nullptr, *upu = nullptr, *rpu = nullptr, *U = nullptr;
@@ -992,7 +1017,7 @@ int slm_build(m3sph_mesh *M, const m3sph_level &f0) {
       (st = sl_upload(&S->cls, cls.data(), cls.size(), s)) || (st = sl_upload(&S->S0, S0.data(), S0.size(), s)) ||
       (st = sl_upload(&S->SZ, SZ.data(), SZ.size(), s)) || (st = sl_upload(&S->SX, SX.data(), SX.size(), s)) ||
       (st = sl_upload(&S->grid, grid.data(), grid.size(), s)) ||
-      (st = sl_upload(&S->iface, iface.data(), iface.size(), s)) || (st = sl_alloc(&S->ring_count, 1)))
+      (st = sl_upload(&S->iface, iface.data(), iface.size(), s)) || (st = sl_alloc(&S->ring_count, 16)))
     return st;
   const std::vector<float> S0f(S0.begin(), S0.end()), SZf(SZ.begin(), SZ.end()), SXf(SX.begin(), SX.end());
   if ((st = sl_upload(&S->S0f, S0f.data(), S0f.size(), s)) || (st = sl_upload(&S->SZf, SZf.data(), SZf.size(), s)) ||
@@ -1031,12 +1056,60 @@ static int slm_reserve(SlmState *S, size_t npt, int nel, int nnod, int nv) {
   return M3SPH_OK;
 }
 
+__global__ void k_aos3_to_soa(const double *__restrict__ a, int n, double *__restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  b[i] = a[3 * (size_t)i];
+  b[n + (size_t)i] = a[3 * (size_t)i + 1];
+  b[2 * (size_t)n + i] = a[3 * (size_t)i + 2];
+}
+__global__ void k_soa3_to_aos(const double *__restrict__ b, int n, double *__restrict__ a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  a[3 * (size_t)i] = b[i];
+  a[3 * (size_t)i + 1] = b[n + (size_t)i];
+  a[3 * (size_t)i + 2] = b[2 * (size_t)n + i];
+}
+__global__ void k_add_int(int *v, int n, int d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] += d;
+}
+
+// points the walk and the rings left unplaced (status bit 8), listed for the brute force; the
+// order of the list does not matter (each point is resolved on its own)
+__global__ void k_status_compact(const uint8_t *__restrict__ status, int npt, int *__restrict__ todo,
+                                 int *__restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < npt && (status[i] & 8)) todo[atomicAdd(cnt, 1)] = i;
+}
+// status counts: [0] walk / ring placed (1), [1] ties (2), [2] gaps (4), [3] brute force (16),
+// [4] lost (8 without 16), [5] ambiguous for the reference (32), [6] candidate overflow (64)
+__global__ void k_status_counts(const uint8_t *__restrict__ status, int npt, int *__restrict__ cnt) {
+  int c[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npt; i += gridDim.x * blockDim.x) {
+    const int st = status[i];
+    c[0] += st & 1;
+    c[1] += (st >> 1) & 1;
+    c[2] += (st >> 2) & 1;
+    c[3] += (st >> 4) & 1;
+    c[4] += (st & 8) && !(st & 16);
+    c[5] += (st >> 5) & 1;
+    c[6] += (st >> 6) & 1;
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    int v = c[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(cnt + k, v);
+  }
+}
+
 // locate S->P (npt points) with optional guesses (S->guess valid if use_guess), writing S->els,
 // S->lc, S->status; unplaced points get a brute-force pass. Returns counts in info.
 static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool node_guess, bool adjust,
                       m3sph_locate_info *info) {
   cudaStream_t s = M->stream;
-  M3_CUDA(cudaMemsetAsync(S->ring_count, 0, sizeof(int), s));
+  M3_CUDA(cudaMemsetAsync(S->ring_count, 0, 16 * sizeof(int), s));
   k_locate<<<(npt + 127) / 128, 128, 0, s>>>(S->view, S->P, npt, use_guess ? S->guess : nullptr,
                                               node_guess ? S->node_guess : nullptr, S->els, S->lc, S->status,
                                               adjust ? 1 : 0, S->todo, S->ring_count); count_launch();
@@ -1050,37 +1123,23 @@ static int slm_locate(m3sph_mesh *M, SlmState *S, int npt, bool use_guess, bool 
                                                                                      adjust ? 1 : 0); count_launch();
     M3_CUDA(cudaGetLastError());
   }
-  std::vector<uint8_t> hs(npt);
-  M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
+  // unplaced points: listed on the device, brute force over the list
+  k_status_compact<<<(npt + 255) / 256, 256, 0, s>>>(S->status, npt, S->todo, S->ring_count + 1); count_launch();
+  int nt = 0;
+  M3_CUDA(cudaMemcpyAsync(&nt, S->ring_count + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
   M3_CUDA(cudaStreamSynchronize(s));
-  std::vector<int> todo;
-  int nwalk = 0;
-  for (int i = 0; i < npt; ++i) {
-    if (hs[i] & 1) nwalk++;
-    if (hs[i] & 8) todo.push_back(i);
-  }
-  int nbrute = 0, nlost = 0;
-  if (!todo.empty()) {
-    M3_CUDA(cudaMemcpyAsync(S->todo, todo.data(), sizeof(int) * todo.size(), cudaMemcpyHostToDevice, s));
-    const int nt = (int)todo.size();
+  if (nt > 0) {
     k_locate_brute<<<(nt + BRUTE_WARPS - 1) / BRUTE_WARPS, BRUTE_WARPS * 32, 0, s>>>(S->view, S->P, npt, S->todo, nt,
                                                                                     S->els, S->lc, S->status,
                                                                                     adjust ? 1 : 0); count_launch();
     M3_CUDA(cudaGetLastError());
-    M3_CUDA(cudaMemcpyAsync(hs.data(), S->status, npt, cudaMemcpyDeviceToHost, s));
-    M3_CUDA(cudaStreamSynchronize(s));
-    for (int i : todo) {
-      if (hs[i] & 16) nbrute++;
-      else nlost++;
-    }
   }
-  int ntie = 0, ngap = 0, nambig = 0, noverflow = 0;
-  for (int i = 0; i < npt; ++i) {
-    if (hs[i] & 2) ntie++;
-    if (hs[i] & 4) ngap++;
-    if (hs[i] & 32) nambig++;
-    if (hs[i] & 64) noverflow++;
-  }
+  k_status_counts<<<std::min((npt + 255) / 256, 1216), 256, 0, s>>>(S->status, npt, S->ring_count + 2); count_launch();
+  int hc[7];
+  M3_CUDA(cudaMemcpyAsync(hc, S->ring_count + 2, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  M3_CUDA(cudaStreamSynchronize(s));
+  const int nwalk = hc[0], ntie = hc[1], ngap = hc[2], nbrute = hc[3], nlost = hc[4], nambig = hc[5],
+            noverflow = hc[6];
   if (info) {
     info->npt = npt;
     info->nwalk = nwalk;
@@ -1146,27 +1205,54 @@ extern "C" int m3sph_tsearch_sph(m3sph_mesh *M, const double *thphr, int32_t npt
   Level &L0 = M->lev[0];
   if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
   cudaStream_t s = M->stream;
-  std::vector<double> P(3 * (size_t)npt);
-  for (int i = 0; i < npt; ++i)
-    for (int k = 0; k < 3; ++k) P[(size_t)k * npt + i] = thphr[3 * (size_t)i + k];
-  M3_CUDA(cudaMemcpyAsync(S->P, P.data(), sizeof(double) * P.size(), cudaMemcpyHostToDevice, s));
+  // points arrive point-major (th ph r per point); S->lc stages them for the transpose to S->P
+  M3_CUDA(cudaMemcpyAsync(S->lc, thphr, sizeof(double) * 3 * (size_t)npt, cudaMemcpyHostToDevice, s));
+  k_aos3_to_soa<<<(npt + 255) / 256, 256, 0, s>>>(S->lc, npt, S->P); count_launch();
   if (els_guess) {
-    std::vector<int> g(npt);
-    for (int i = 0; i < npt; ++i) g[i] = els_guess[i] - 1;
-    M3_CUDA(cudaMemcpyAsync(S->guess, g.data(), sizeof(int) * npt, cudaMemcpyHostToDevice, s));
+    M3_CUDA(cudaMemcpyAsync(S->guess, els_guess, sizeof(int) * npt, cudaMemcpyHostToDevice, s));
+    k_add_int<<<(npt + 255) / 256, 256, 0, s>>>(S->guess, npt, -1); count_launch();
   }
   st = slm_locate(M, S, npt, els_guess != nullptr, npt == L0.nnod, false, info);
   if (st && st != M3SPH_ERR_POINT_NOT_FOUND) return st;
-  std::vector<int> e(npt);
-  std::vector<double> lc(3 * (size_t)npt);
-  M3_CUDA(cudaMemcpyAsync(e.data(), S->els, sizeof(int) * npt, cudaMemcpyDeviceToHost, s));
-  M3_CUDA(cudaMemcpyAsync(lc.data(), S->lc, sizeof(double) * lc.size(), cudaMemcpyDeviceToHost, s));
-  M3_CUDA(cudaStreamSynchronize(s));
-  for (int i = 0; i < npt; ++i) {
-    els_out[i] = e[i] + 1;
-    if (lc_out)
-      for (int k = 0; k < 3; ++k) lc_out[3 * (size_t)i + k] = lc[(size_t)k * npt + i];
+  // 1-based ids; local coordinates back to point-major order (S->P is free now)
+  k_add_int<<<(npt + 255) / 256, 256, 0, s>>>(S->els, npt, 1); count_launch();
+  M3_CUDA(cudaMemcpyAsync(els_out, S->els, sizeof(int) * npt, cudaMemcpyDeviceToHost, s));
+  if (lc_out) {
+    k_soa3_to_aos<<<(npt + 255) / 256, 256, 0, s>>>(S->lc, npt, S->P); count_launch();
+    M3_CUDA(cudaMemcpyAsync(lc_out, S->P, sizeof(double) * 3 * (size_t)npt, cudaMemcpyDeviceToHost, s));
   }
+  M3_CUDA(cudaStreamSynchronize(s));
+  return st;
+}
+
+extern "C" int m3sph_locate_timing(m3sph_mesh *M, const double *thphr, int32_t npt, int32_t nrep, double *ms,
+                                   m3sph_locate_info *info) {
+  int st = slm_check(M);
+  if (st) return st;
+  if (npt <= 0 || nrep <= 0 || !thphr || !ms) {
+    set_error("m3sph_locate_timing: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  SlmState *S = slm_state(M);
+  Level &L0 = M->lev[0];
+  if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
+  cudaStream_t s = M->stream;
+  M3_CUDA(cudaMemcpyAsync(S->lc, thphr, sizeof(double) * 3 * (size_t)npt, cudaMemcpyHostToDevice, s));
+  k_aos3_to_soa<<<(npt + 255) / 256, 256, 0, s>>>(S->lc, npt, S->P); count_launch();
+  st = slm_locate(M, S, npt, false, false, false, info);       // warm-up
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  M3_CUDA(cudaEventCreate(&e0));
+  M3_CUDA(cudaEventCreate(&e1));
+  M3_CUDA(cudaEventRecord(e0, s));
+  for (int r = 0; r < nrep && !st; ++r) st = slm_locate(M, S, npt, false, false, false, info);
+  M3_CUDA(cudaEventRecord(e1, s));
+  M3_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  M3_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t / nrep;
   return st;
 }
 
