@@ -42,8 +42,10 @@ TARGET = 1e-8
 # Patera / MG-PCG tolerances: the reference's rtol_U (5e-3) and a pressure tolerance that the
 # coupled-residual check tightens (x0.1) until the 1e-8 target is met
 SOLVER_KW = dict(rtol_Pat=1e-7, rtol_U=5e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=TARGET)
-# accuracy checks: each timed solution continued from its pressure to a 1e-11 coupled residual; at a
-# 1e-8 residual two solutions of the high-contrast shells may still differ by a few 1e-8 in U
+# accuracy checks: the plain FP64 solution continued from its pressure to a 1e-11 coupled residual,
+# the learned FP32-MG path solved from zero to 1e-11 (warm-started from an already converged
+# pressure its inner solves can stall); at a 1e-8 residual two solutions of the high-contrast
+# shells may still differ by a few 1e-8 in U
 TIGHT = 1e-11
 TIGHT_KW = dict(rtol_Pat=1e-10, rtol_U=5e-3, itmax_Pat=400, itmax_U=40, target_rel_residual=TIGHT)
 
@@ -204,7 +206,7 @@ def run_gb300(args, rank, ws, td):
         t_plain = allmax(td, (time.perf_counter() - t) / args.plain_steps)
         plain = dict(s_per_solve=t_plain, info=infos64[-1])
         U64, P64 = dm.solution()
-        U64t, P64t, _ = dm.solve(P0=P64, allow_not_converged=True, **TIGHT_KW)
+        U64t, P64t, i64t = dm.solve(P0=P64, allow_not_converged=True, **TIGHT_KW)
         fp64_apply_ms = dm.apply_timing(0, 0, 5)
     # ---- the product: FP32 V-cycle with the learned element smoother (one learned sweep per
     # side on the two finest levels) inside FP64 outer CG / Patera; timed region ----
@@ -229,8 +231,8 @@ def run_gb300(args, rank, ws, td):
     accuracy = None
     if plain is not None:
         Um, Pm = dm.solution()
-        Umt, Pmt, _ = dm.solve(P0=Pm, smoother=sm, allow_not_converged=True, **TIGHT_KW)
-        accuracy = accuracy_block(Um, Pm, U64, P64, Umt, Pmt, U64t, P64t)
+        Umt, Pmt, imt = dm.solve(smoother=sm, allow_not_converged=True, **TIGHT_KW)
+        accuracy = accuracy_block(Um, Pm, U64, P64, Umt, Pmt, U64t, P64t, imt["rel_residual"], i64t["rel_residual"])
     ms = allmax(td, ms)
     clocks = clk.summary(dev)
     last = infos[-1]
@@ -367,10 +369,10 @@ def solution_distance(U, P, Uref, Pref):
     return d
 
 
-def accuracy_block(Ul, Pl, Up, Pp, Ult, Plt, Upt, Ppt):
-    """Distances of the learned (l) and plain FP64 (p) solutions at the 1e-8 target and continued
-    to TIGHT (t): the headline pair (learned at 1e-8 against plain FP64 at 1e-8), the learned 1e-8
-    solution against the tight FP64 solution, and the two tight solutions."""
+def accuracy_block(Ul, Pl, Up, Pp, Ult, Plt, Upt, Ppt, res_lt=None, res_pt=None):
+    """Distances of the learned (l) and plain FP64 (p) solutions at the 1e-8 target and at TIGHT
+    (t): the headline pair (learned at 1e-8 against plain FP64 at 1e-8), the learned 1e-8 solution
+    against the tight FP64 solution, and the two tight solutions."""
     d = solution_distance(Ul, Pl, Up, Pp)
     a = solution_distance(Ul, Pl, Upt, Ppt)
     b = solution_distance(Ult, Plt, Upt, Ppt)
@@ -378,7 +380,8 @@ def accuracy_block(Ul, Pl, Up, Pp, Ult, Plt, Upt, Ppt):
     d["learned_1e-8_vs_plain_1e-11"] = {"dU": a["dU_rel_l2_vs_plain_fp64"], "dP": a["dP_rel_l2_vs_plain_fp64"]}
     d["plain_1e-8_vs_plain_1e-11"] = {"dU": c["dU_rel_l2_vs_plain_fp64"], "dP": c["dP_rel_l2_vs_plain_fp64"]}
     d["learned_1e-11_vs_plain_1e-11"] = {"dU": b["dU_rel_l2_vs_plain_fp64"], "dP": b["dP_rel_l2_vs_plain_fp64"],
-                                         "within_1e-8": b["within_1e-8"]}
+                                         "within_1e-8": b["within_1e-8"],
+                                         "rel_residuals": [res_lt, res_pt]}
     return d
 
 
@@ -398,7 +401,7 @@ def c1_leg(args, wfile):
         dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=0)
         ms, infos, _ = timed(0, 1, 3)
         U64, P64 = dm.solution()
-        U64t, P64t, _ = dm.solve(P0=P64, allow_not_converged=True, **TIGHT_KW)
+        U64t, P64t, i64t = dm.solve(P0=P64, allow_not_converged=True, **TIGHT_KW)
         out["plain_fp64_s"] = ms / 1e3
         dm.setup(w["visc"], w["dens"], w["ifix"], w["vfix"], w["phys"], precision=1)
         ms, infos, _ = timed(0, 1, 3)
@@ -409,8 +412,9 @@ def c1_leg(args, wfile):
         out["learned_rel_residual"] = infos[-1]["rel_residual"]
         out["learned_its"] = infos[-1]["nitU"] + infos[-1]["nitZ"]
         Ul, Pl = dm.solution()
-        Ult, Plt, _ = dm.solve(P0=Pl, smoother=1, allow_not_converged=True, **TIGHT_KW)
-        out["accuracy"] = accuracy_block(Ul, Pl, U64, P64, Ult, Plt, U64t, P64t)
+        Ult, Plt, ilt = dm.solve(smoother=1, allow_not_converged=True, **TIGHT_KW)
+        out["accuracy"] = accuracy_block(Ul, Pl, U64, P64, Ult, Plt, U64t, P64t, ilt["rel_residual"],
+                                         i64t["rel_residual"])
     finally:
         dm.close()
     return out
@@ -445,7 +449,6 @@ def c5_leg(args, wfile):
         setup(1)
         il = dm.step_device(smoother=1, **SOLVER_KW)
         Ul, Pl = dm.solution()
-        Ult, Plt, _ = dm.solve(P0=Pl, smoother=1, allow_not_converged=True, **TIGHT_KW)
         out["learned_fp32"] = {"s": (il["t_setup_ms"] + il["t_iter_ms"]) / 1e3, "its": il["nitU"] + il["nitZ"],
                                "itPat": il["itPat"], "rel_residual": il["rel_residual"],
                                "fallbacks": il["smoother_fallbacks"]}
@@ -453,13 +456,12 @@ def c5_leg(args, wfile):
             setup(0)
             ip = dm.step_device(**SOLVER_KW)
             Up, Pp = dm.solution()
-            Upt, Ppt, _ = dm.solve(P0=Pp, allow_not_converged=True, **TIGHT_KW)
             out["plain_fp64"] = {"s": (ip["t_setup_ms"] + ip["t_iter_ms"]) / 1e3, "its": ip["nitU"] + ip["nitZ"],
                                  "itPat": ip["itPat"], "rel_residual": ip["rel_residual"]}
             out["speedup_learned_vs_plain"] = out["plain_fp64"]["s"] / out["learned_fp32"]["s"]
-            out["accuracy"] = accuracy_block(Ul, Pl, Up, Pp, Ult, Plt, Upt, Ppt)
-            del Upt, Ppt
-        del Ult, Plt
+            # at this size the 1e-11 continuations of both solves would add several minutes; the
+            # 8M-DOF and 130k-DOF blocks carry them
+            out["accuracy"] = solution_distance(Ul, Pl, Up, Pp)
         steps = {}
         for name, prec, n in (("learned_fp32", 1, args.c5_steps), ("plain_fp64", 0, args.c5_plain_steps)):
             if n <= 0:

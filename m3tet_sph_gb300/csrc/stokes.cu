@@ -1177,7 +1177,8 @@ static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs
   M3_TRY(set_first_flag(M, 1.0));
   cudaGraphExec_t exec = nullptr;
   if (M->use_graphs) M3_TRY(iteration_graph(M, x, &exec));
-  for (it = 1; it <= itmax; ++it) {
+  int itlim = itmax;
+  for (it = 1; it <= itlim; ++it) {
     if (exec) {
       M3_CUDA(cudaGraphLaunch(exec, s));
       add_launches(M->graph_kernels);
@@ -1195,14 +1196,20 @@ static int mgpcg(m3sph_mesh *M, const double *b, double *x, double tol, bool abs
     if (rrms < tol) break;
     // learned-smoother fallback: a contraction factor above 0.95 (or growth) switches the rest of
     // the solve to the Jacobi smoother
-    if (M->smoother_active && it > 1 && rrms > 0.95 * rrms_prev) {
+    // the same when the learned smoother runs out of iterations above the tolerance: the solve
+    // goes on with Jacobi smoothing for another itmax iterations (flexible CG accepts the change
+    // of preconditioner) rather than handing a less accurate K^-1 to the Patera iteration
+    const bool stalled = it > 1 && rrms > 0.95 * rrms_prev;
+    const bool exhausted = it == itlim;
+    if (M->smoother_active && (stalled || exhausted)) {
       M->smoother_active = false;
       M->smoother_fallbacks++;
+      if (exhausted) itlim += itmax;
       exec = nullptr;
       if (M->use_graphs) M3_TRY(iteration_graph(M, x, &exec));
     }
   }
-  st.it = std::min(it, itmax);
+  st.it = std::min(it, itlim);
   st.rrms = rrms;
   return M3SPH_OK;
 }

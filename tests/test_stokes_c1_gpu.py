@@ -48,3 +48,4 @@ def test_c1_solution_matches_oracle(c1_oracle, path):
         assert eU < TOL and eP < TOL, (path, eU, eP)
     finally:
         dm.close()
+
