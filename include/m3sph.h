@@ -326,7 +326,9 @@ M3SPH_API int m3sph_interp3d_cubic(m3sph_mesh *mesh, const int32_t *els, const d
  * M3SPH_ERR_BAD_INPUT). The array's device address is looked up, and this entry point's kernels
  * are loaded, when the mesh handle is created (m3sph_mesh_create), so under CUDA's lazy module
  * loading the array is committed at start-up and not inside a call. Calls that overlap on the GPU
- * (two handles on two threads) race on the shared scratch. It calls no cudaMalloc / cudaFree. */
+ * (two handles on two threads) race on the shared scratch. It calls no cudaMalloc / cudaFree. It
+ * synchronises the handle's stream before returning, so it cannot be called while that stream is
+ * being captured into a CUDA graph. */
 M3SPH_API int m3sph_interp3d_cubic_noalloc(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
                                            const double *V, int32_t monotonic, int32_t method_wght, double *Vi);
 /* Replaces advect3d_slm_p_sph (advect3d_slm_p_sph.m:1-139): Ux,Uy,Uz Cartesian nodal velocity,
