@@ -414,37 +414,6 @@ class OmpCSR:
         return y
 
 
-class OmpSymCSR(OmpCSR):
-    """y = A @ x for a symmetric A from its lower triangle on `nthreads` host threads
-    (oracle/csr_omp.c sym_csr_matvec): the storage and product the reference uses for its
-    stiffness matrices (flow3d_patera_mg_sph_p.m:311-318, mgpcg_solver_p.m:728-740). Half the
-    matrix traffic of the full product; the sums differ from scipy's in rounding only."""
-
-    @classmethod
-    def lib(cls):
-        L = OmpCSR.lib()
-        if not getattr(L, "_sym_ready", False):
-            import ctypes as C
-            L.sym_csr_matvec.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                         C.c_void_p, C.c_int]
-            L.sym_csr_matvec.restype = None
-            L._sym_ready = True
-        return L
-
-    def __init__(self, A, nthreads):
-        super().__init__(sp.tril(A.tocsr()).tocsr(), nthreads)
-        self.shape = A.shape
-        self.work = np.empty(self.nthreads * self.shape[0])
-        self.lib()
-
-    def __matmul__(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        y = np.empty(self.shape[0])
-        self.lib().sym_csr_matvec(self.shape[0], self.ptr.ctypes.data, self.col.ctypes.data, self.val.ctypes.data,
-                                  x.ctypes.data, y.ctypes.data, self.work.ctypes.data, self.nthreads)
-        return y
-
-
 class MGPCG:
     """mgpcg_solver_p (flexible Polak-Ribiere PCG, V-cycle v2, Jacobi weights 'Setup 3')."""
 
@@ -465,8 +434,8 @@ class MGPCG:
         if not hasattr(self, "_serial"):
             self._serial = (self.K1, list(self.KK), list(self.P), list(self.PT))
         K1, KK, P = self._serial[0], self._serial[1], self._serial[2]
-        self.K1 = OmpSymCSR(K1, nthreads)
-        self.KK = [KK[0]] + [OmpSymCSR(K, nthreads) for K in KK[1:]]
+        self.K1 = OmpCSR(K1, nthreads)
+        self.KK = [KK[0]] + [OmpCSR(K, nthreads) for K in KK[1:]]
         self.PT = [OmpCSR(p.T, nthreads) for p in P]
         self.P = [OmpCSR(p, nthreads) for p in P]
 

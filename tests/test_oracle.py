@@ -66,18 +66,14 @@ def test_transfer_matches_host_setup(tiny):
 
 
 def test_threaded_sparse_products_match_serial(tiny):
-    """The CPU baseline's threaded mode: the stiffness products from the lower triangle agree with
-    the serial CSR product to rounding, the transfer products bit for bit, and MG-PCG iterates agree
-    with the serial solver to rounding."""
+    """The CPU baseline's threaded mode: row-block products equal the serial CSR product bit for
+    bit, and MG-PCG iterates agree with the serial solver to rounding."""
     w = tiny
     s1 = O.StokesSystem(w['levels'], w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'])
     s4 = O.StokesSystem(w['levels'], w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'])
     s4.mg.use_threads(4)
     x = np.random.default_rng(3).standard_normal(s1.mg.K1.shape[0])
-    y1 = s1.mg.K1 @ x
-    assert np.max(np.abs(s4.mg.K1 @ x - y1)) <= 1e-13 * np.max(np.abs(y1))
-    xc = np.random.default_rng(5).standard_normal(s1.mg.P[0].shape[1])
-    assert np.array_equal(s4.mg.P[0] @ xc, s1.mg.P[0] @ xc)
+    assert np.array_equal(s4.mg.K1 @ x, s1.mg.K1 @ x)
     b = np.random.default_rng(4).standard_normal(len(s1.ifree))
     x1, it1, _ = s1.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
     x4, it4, _ = s4.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
@@ -167,22 +163,3 @@ def test_gelu_erf_approximation_bound():
     gelu_as = np.where(x >= 0, x - q, q)
     gelu = 0.5 * x * (1.0 + erf(x / np.sqrt(2.0)))
     assert np.all(np.abs(gelu_as - gelu) <= 0.5 * 1.5e-7 * np.abs(x) + 1e-15)
-
-
-def test_threaded_products_of_the_cpu_baseline():
-    """The timed CPU solve's sparse products: the full CSR product on host threads is bit-identical
-    to scipy's; the symmetric lower-triangle product (the reference's storage of its stiffness
-    matrices) agrees with it to rounding, for 1 and 4 threads."""
-    import scipy.sparse as sp
-    from oracle import stokes_oracle as O
-    rng = np.random.default_rng(3)
-    n = 3000
-    B = sp.random(n, n, density=2e-3, random_state=rng, format='csr')
-    A = (B + B.T + sp.diags(rng.uniform(1, 2, n))).tocsr()
-    A.sort_indices()
-    x = rng.standard_normal(n)
-    y = A @ x
-    for t in (1, 4):
-        assert np.array_equal(O.OmpCSR(A, t) @ x, y)
-        ys = O.OmpSymCSR(A, t) @ x
-        assert np.max(np.abs(ys - y)) <= 1e-13 * np.max(np.abs(y))
