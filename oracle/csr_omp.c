@@ -4,7 +4,8 @@
  * The CPU baseline times the oracle's MG-PCG / Patera solve with its sparse products here; the
  * reference's own product (mgpcg_solver_p.m:728-733 -> MUTILS spmv) is multi-threaded the same way.
  * Each row is summed in index order with separate multiply and add (built with
- * -ffp-contract=off), so the result is bit-identical to scipy's serial CSR product.
+ * -ffp-contract=off): the same sums as scipy's serial CSR product, bit-identical to it where the
+ * host compiler does not fuse scipy's multiply-adds (x86-64) and equal to rounding elsewhere.
  */
 #include <stdint.h>
 

@@ -380,8 +380,8 @@ class CoarseChol:
 class OmpCSR:
     """y = A @ x on `nthreads` host threads through the oracle's OpenMP product (oracle/csr_omp.c).
     The reference's own product (mgpcg_solver_p.m:728-733, MUTILS spmv) is multi-threaded too. Each
-    row is summed in the same order with separate multiply and add, so the result is bit-identical
-    to scipy's ``A @ x``."""
+    row is summed in the same order with separate multiply and add, so the result equals scipy's
+    ``A @ x`` to rounding (bit for bit where scipy's multiply-adds are not fused)."""
 
     _lib = None
 

@@ -66,14 +66,16 @@ def test_transfer_matches_host_setup(tiny):
 
 
 def test_threaded_sparse_products_match_serial(tiny):
-    """The CPU baseline's threaded mode: row-block products equal the serial CSR product bit for
-    bit, and MG-PCG iterates agree with the serial solver to rounding."""
+    """The CPU baseline's threaded mode: row-block products equal the serial CSR product to rounding
+    (bit for bit where the host compiler does not fuse scipy's multiply-adds), and MG-PCG iterates
+    agree with the serial solver to rounding."""
     w = tiny
     s1 = O.StokesSystem(w['levels'], w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'])
     s4 = O.StokesSystem(w['levels'], w['visc'], w['dens'], w['ifix'], w['vfix'], w['phys'])
     s4.mg.use_threads(4)
     x = np.random.default_rng(3).standard_normal(s1.mg.K1.shape[0])
-    assert np.array_equal(s4.mg.K1 @ x, s1.mg.K1 @ x)
+    y1 = s1.mg.K1 @ x
+    assert np.max(np.abs(s4.mg.K1 @ x - y1)) <= 1e-14 * np.max(np.abs(y1))
     b = np.random.default_rng(4).standard_normal(len(s1.ifree))
     x1, it1, _ = s1.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
     x4, it4, _ = s4.mg.solve(b, np.zeros_like(b), rtol=1e-30, itmax=4)
