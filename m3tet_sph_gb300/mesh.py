@@ -304,8 +304,8 @@ def cubic_geometry(Xc, Sc, T4iso, theta_cone_deg):
             xr = RR_X_90_CW @ sph2cart(sr)
             P[:, :, 4 + 2 * k + m] = np.where(both_out[None, :], xo, xr).T
     # face nodes
-    Srot = np.stack([cart2sph(RR_X_90_CCW @ P[e]) for e in range(nel)]) if nel else np.zeros((0, 3, 20))
-    Sorig = np.stack([cart2sph(P[e]) for e in range(nel)]) if nel else np.zeros((0, 3, 20))
+    Srot = _cart2sph_nodes(P, RR_X_90_CCW)
+    Sorig = _cart2sph_nodes(P, None)
     for f in range(4):
         nodes = FACES20[f]
         verts = nodes[:3]
@@ -327,7 +327,20 @@ def cubic_geometry(Xc, Sc, T4iso, theta_cone_deg):
         xf = np.where((all_out & cross)[:, None], x180, np.where(all_out[:, None], x_orig, x_rot))
         P[:, :, 16 + f] = xf
         del m_orig
-    return np.stack([cart2sph(RR_X_90_CCW @ P[e]) for e in range(nel)]) if nel else np.zeros((0, 3, 20))
+    return _cart2sph_nodes(P, RR_X_90_CCW)
+
+
+def _cart2sph_nodes(P, R):
+    """(theta,phi,r) of the nodes P (nel,3,k), rotated by R first if given: (nel,3,k). The rotations
+    used here are signed permutations, so applying them to all nodes at once gives the values of
+    the per-element products exactly."""
+    nel, _, k = P.shape
+    if nel == 0:
+        return np.zeros((0, 3, k))
+    X = P.transpose(1, 0, 2).reshape(3, nel * k)
+    if R is not None:
+        X = R @ X
+    return cart2sph(X).reshape(3, nel, k).transpose(1, 0, 2)
 
 
 def _unwrap_face_mean(Sn):
@@ -383,7 +396,8 @@ def transfer_rows(EL2NOD_f, isplit_c, EL2NOD_c):
     nel_f = len(EL2NOD_f)
     nnod_f = int(EL2NOD_f.max()) + 1
     flat = EL2NOD_f.ravel()                  # element-major: first occurrence = lowest element
-    _, first = np.unique(flat, return_index=True)
+    first = np.full(nnod_f, flat.size, dtype=np.int64)
+    np.minimum.at(first, flat, np.arange(flat.size, dtype=np.int64))
     el = first // 10
     loc = first % 10
     par = el // 8
@@ -392,7 +406,7 @@ def transfer_rows(EL2NOD_f, isplit_c, EL2NOD_c):
     W = CHILD_PROLONG[s, k, loc]             # (nnod_f,10)
     cols = EL2NOD_c[par]                     # (nnod_f,10)
     W = np.where(np.abs(W) < 1e-14, 0.0, W)
-    assert nnod_f == len(first)
+    assert np.all(first < flat.size), "fine nodes without an element"
     return cols, W
 
 
