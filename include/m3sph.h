@@ -131,6 +131,12 @@ M3SPH_API int m3sph_mesh_ncolors(const m3sph_mesh *mesh, int32_t img, int32_t *n
  * (restrict_stiffmat.m) and the coarse factorisation (cholesky_factorization.m). */
 M3SPH_API int m3sph_stokes_setup(m3sph_mesh *mesh, const double *Visc, const double *Dens, const int32_t *ifix,
                        const double *vfix, int32_t nfix, const m3sph_physics *phys, int32_t precision);
+/* Replaces the UBC that update_vel_bc (update_vel_bc.m:84-150) hands to the next flow3d_patera_sph
+ * call in a GPlates-driven loop: new prescribed values vfix on the fixed dofs ifix (1-based, any
+ * order) of the last m3sph_stokes_setup. The dof set must equal the set-up's (M3SPH_ERR_BAD_INPUT
+ * otherwise: a new set needs m3sph_stokes_setup). The next operator rebuild (m3sph_time_step,
+ * m3sph_stokes_step_device, or m3sph_stokes_solve, which rebuilds when values changed) uses them. */
+M3SPH_API int m3sph_stokes_set_vel_bc(m3sph_mesh *mesh, const int32_t *ifix, const double *vfix, int32_t nfix);
 
 /* Replaces flow3d_patera_mg_sph_p (flow3d_patera_mg_sph_p.m:1-780): Patera pressure CG around
  * MG-PCG. P (nvnod) is the initial pressure on input and the solution on output; U_xyz (3*nnod,

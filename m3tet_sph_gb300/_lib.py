@@ -103,6 +103,7 @@ SIGNATURES = {
     "m3sph_mesh_ncolors": ([P, C.c_int32, IP], C.c_int),
     "m3sph_stokes_setup": ([P, DP, DP, IP, DP, C.c_int32, C.POINTER(Physics), C.c_int32], C.c_int),
     "m3sph_stokes_solve": ([P, DP, DP, C.POINTER(Opts), C.POINTER(Info)], C.c_int),
+    "m3sph_stokes_set_vel_bc": ([P, IP, DP, C.c_int32], C.c_int),
     "m3sph_mgpcg": ([P, DP, DP, C.c_double, C.c_int32, C.c_int32, IP, DP], C.c_int),
     "m3sph_stokes_apply": ([P, DP, DP], C.c_int),
     "m3sph_grad_apply": ([P, DP, DP], C.c_int),

@@ -236,6 +236,7 @@ struct m3sph_mesh {
   double *Ufix = nullptr;             // [ndof0] prescribed values (rotated frame)
   double *bc_rhs = nullptr;           // K1_full * Ufix
   bool has_nonzero_fix = false;
+  bool bc_stale = false;              // prescribed values changed since the last operator rebuild
   // scratch
   std::vector<void *> work;           // device buffers owned by the workspace
   void *wk = nullptr;                 // host-side workspace descriptor

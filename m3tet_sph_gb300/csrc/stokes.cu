@@ -704,6 +704,7 @@ static int rebuild_operator(m3sph_mesh *M) {
   cudaStream_t s = M->stream;
   Level &L0 = M->lev[0];
   Work *W = get_work(M);
+  M->bc_stale = false;
   M3_CUDA(cudaMemsetAsync(M->fin.err, 0, sizeof(int) * 4, s));
   SetupArgs a{};
   a.nel = L0.nel; a.nnod = L0.nnod; a.el2nod = L0.el2nod; a.cls = M->fin.cls; a.iso_slot = M->fin.iso_slot;
@@ -900,6 +901,58 @@ extern "C" int m3sph_stokes_setup(m3sph_mesh *M, const double *Visc, const doubl
   cudaEventDestroy(e1);
   M->have_operator = true;
   (void)t0;
+  return M3SPH_OK;
+}
+
+// update_vel_bc between time steps (update_vel_bc.m:84-150): new prescribed values on the fixed
+// dofs of the last set-up. The dof set is unchanged (same masks, colours and coarse free-dof maps),
+// so only the resident Ufix is rewritten; the next operator rebuild (every time step, or the next
+// m3sph_stokes_solve) folds it into the boundary-condition right-hand side.
+extern "C" int m3sph_stokes_set_vel_bc(m3sph_mesh *M, const int32_t *ifix, const double *vfix, int32_t nfix) {
+  if (!M || nfix < 0 || (nfix > 0 && (!ifix || !vfix))) {
+    set_error("m3sph_stokes_set_vel_bc: bad arguments");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  if (!M->have_operator) {
+    set_error("m3sph_stokes_set_vel_bc: call m3sph_stokes_setup first");
+    return M3SPH_ERR_BAD_INPUT;
+  }
+  Level &L0 = M->lev[0];
+  std::vector<int> fx(nfix);
+  for (int i = 0; i < nfix; ++i) {
+    if (ifix[i] < 1 || ifix[i] > L0.ndof) {
+      set_error("m3sph_stokes_set_vel_bc: ifix entry out of range");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+    fx[i] = ifix[i] - 1;
+  }
+  {
+    std::vector<int> a(fx), b(M->h_ifix);
+    std::sort(a.begin(), a.end());
+    std::sort(b.begin(), b.end());
+    if (a != b) {
+      set_error("m3sph_stokes_set_vel_bc: the fixed dofs differ from the set-up's (a new dof set needs "
+                "m3sph_stokes_setup)");
+      return M3SPH_ERR_BAD_INPUT;
+    }
+  }
+  M3_CUDA(cudaSetDevice(M->device));
+  cudaStream_t s = M->stream;
+  M->h_ifix = fx;
+  M->h_vfix.assign(vfix, vfix + nfix);
+  M->has_nonzero_fix = false;
+  for (int i = 0; i < nfix; ++i) M->has_nonzero_fix |= vfix[i] != 0.0;
+  int *d_fix = nullptr;
+  double *d_vals = nullptr;
+  M3_TRY(upload(&d_fix, fx.data(), std::max<size_t>(1, fx.size()), s));
+  M3_TRY(upload(&d_vals, M->h_vfix.data(), std::max<size_t>(1, fx.size()), s));
+  M3_CUDA(cudaMemsetAsync(M->Ufix, 0, sizeof(double) * L0.ndof, s));
+  if (nfix) k_scatter_vals<<<(nfix + 255) / 256, 256, 0, s>>>(M->Ufix, d_fix, d_vals, nfix); count_launch();
+  M3_CUDA(cudaGetLastError());
+  M3_CUDA(cudaStreamSynchronize(s));
+  dfree(d_fix);
+  dfree(d_vals);
+  M->bc_stale = true;
   return M3SPH_OK;
 }
 
@@ -1513,6 +1566,8 @@ extern "C" int m3sph_stokes_solve(m3sph_mesh *M, double *U_xyz, double *P, const
   Work *W = get_work(M);
   cudaStream_t s = M->stream;
   Level &L0 = M->lev[0];
+  // prescribed values replaced by m3sph_stokes_set_vel_bc since the last rebuild
+  if (M->bc_stale) M3_TRY(rebuild_operator(M));
   M3_CUDA(cudaMemcpyAsync(W->pP, P, sizeof(double) * L0.nvnod, cudaMemcpyHostToDevice, s));
   cudaEvent_t e0, e1;
   M3_CUDA(cudaEventCreate(&e0));

@@ -88,6 +88,15 @@ class DeviceMesh:
                                            len(fx), C.byref(ph), int(precision)))
         self.precision = precision
 
+    def set_vel_bc(self, ifix, vfix):
+        """New prescribed values on the set-up's fixed dofs (0-based, any order): update_vel_bc's
+        UBC between time steps. The next operator rebuild uses them."""
+        fx = np.ascontiguousarray(np.asarray(ifix, dtype=np.int32) + 1)
+        vf = np.ascontiguousarray(vfix, dtype=np.float64)
+        if fx.size != vf.size:
+            raise ValueError('ifix and vfix differ in length')
+        L.check(L.lib().m3sph_stokes_set_vel_bc(self.h, L.iptr(fx), L.dptr(vf), len(fx)))
+
     # ---- operators ----
     def apply(self, x):
         y = np.empty(self.ndof)
@@ -236,6 +245,7 @@ class DeviceMesh:
 
     def set_temperature(self, T, time=0.0):
         L.check(L.lib().m3sph_set_temperature(self.h, L.dptr(np.ascontiguousarray(T, dtype=np.float64)), float(time)))
+        self.model_time = float(time)
 
     def get_temperature(self):
         T = np.empty(self.nnod)
@@ -258,9 +268,16 @@ class DeviceMesh:
         return T, nit.value
 
     def time_step(self, stokes_kw=None, slm=None, rock=None, dt_adv_limit=0.005, dtmax=0.1, smoother=0,
-                  r_cmb=3480.0, r_surf=6371.0, diffusion=False, allow_not_converged=False):
+                  r_cmb=3480.0, r_surf=6371.0, diffusion=False, allow_not_converged=False, vel_bcs=None):
         """One device-resident time step (rock_prop if `rock` is given -> Stokes -> calculate_dt ->
-        semi-Lagrangian advection of the resident T). Returns the step info as a dict."""
+        semi-Lagrangian advection of the resident T). Returns the step info as a dict.
+
+        ``vel_bcs`` (a ``gplates.VelBCSeries``): the surface velocities at the model time of the
+        step's start are pushed first (update_vel_bc before flow3d_patera_sph,
+        M3TET_SPH_SOUTH_ATLANTIC_PLUME.m:236-241); the step info then holds 'Plate' (VAR.Plate)."""
+        plate = None
+        if vel_bcs is not None:
+            _, plate = vel_bcs.apply(self, getattr(self, 'model_time', 0.0))
         kw = dict(rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20, target_rel_residual=0.0)
         kw.update(stokes_kw or {})
         slm = dict(slm or {})
@@ -278,7 +295,12 @@ class DeviceMesh:
         o.diffusion = 1 if diffusion else 0
         info = L.StepInfo()
         code = L.lib().m3sph_time_step(self.h, C.byref(o), C.byref(info))
-        return self._finish(code, info.as_dict(), allow_not_converged)
+        d = info.as_dict()
+        if code in (L.OK, L.ERR_NOT_CONVERGED):
+            self.model_time = d['time']
+        if plate is not None:
+            d['Plate'] = plate
+        return self._finish(code, d, allow_not_converged)
 
     def set_option(self, name, value):
         L.check(L.lib().m3sph_set_option(self.h, name.encode(), int(value)))
