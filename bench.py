@@ -14,8 +14,8 @@ Arms:
       same GPU: the plain-FP64 path and the Jacobi-smoothed FP32 solve of the same shell; the same
       three solves on the 130k-DOF shell next to the FP64 oracle's full solve of it on the host
       (`c1`); on the 64M-DOF shell (`c5`) one learned and one plain-FP64 solve to 1e-8 and
-      device-resident time steps (rock_prop -> Stokes -> calculate_dt -> semi-Lagrangian
-      advection); semi-Lagrangian rates on the 130k-DOF shell.
+      device-resident time steps (GPlates surface velocities -> rock_prop -> Stokes -> calculate_dt
+      -> semi-Lagrangian advection); semi-Lagrangian rates on the 130k-DOF shell.
   --impl reference: the FP64 CPU oracle (numpy/scipy restatement of the reference algorithm with
       OpenMP sparse products on all host threads): one step = one full solve of the 130k-DOF shell
       (set-up + Patera / MG-PCG to a 1e-8 coupled residual), timed, not extrapolated.
@@ -29,6 +29,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -427,11 +428,12 @@ def c5_leg(args, wfile):
     """The 64M-DOF shell (level 6 x 64 layers, 15,728,640 curved P2 tets, 63,406,854 velocity DOF,
     1e6 viscosity contrast x30 below 660 km, 12 plate caps): one learned + FP32-MG solve and one
     plain-FP64 solve to the 1e-8 coupled residual, their distance, then device-resident time steps
-    (rock_prop -> Stokes at the reference's default tolerances -> calculate_dt -> diffusion half step
-    -> PC2 + cubic semi-Lagrangian advection of T -> diffusion half step) with each path."""
-    from m3tet_sph_gb300 import learned as LS, stokes, workloads
+    (GPlates surface velocities at the step's model time -> rock_prop -> Stokes at the reference's
+    default tolerances -> calculate_dt -> diffusion half step -> PC2 + cubic semi-Lagrangian
+    advection of T -> diffusion half step) with each path."""
+    from m3tet_sph_gb300 import gplates, learned as LS, stokes, workloads
     t0 = time.time()
-    w = workloads.make_workload("c5", seed=args.seed)
+    w = workloads.make_workload(args.c5_workload, seed=args.seed)
     f = w["levels"][0]
     dm = stokes.DeviceMesh(w["levels"])
     dm.set_option("fp32_operator", args.fp32_operator)
@@ -465,6 +467,17 @@ def c5_leg(args, wfile):
             # at this size the 1e-11 continuations of both solves would add several minutes; the
             # 8M-DOF and 130k-DOF blocks carry them
             out["accuracy"] = solution_distance(Ul, Pl, Up, Pp)
+        # the time steps take their surface velocities from a GPlates series, updated before every
+        # step as the reference's loop does (update_vel_bc); the series is seeded (four 1-Myr exports
+        # in GPlates' format, written and read back), the reference's own exports not being shipped
+        t_rd = time.time()
+        with tempfile.TemporaryDirectory() as tmp:
+            folder = gplates.write_synthetic_folder(tmp, gplates.synthetic_vel_bcs(f, seed=args.seed))
+            V_BCs, t_files = gplates.read_vel_gplates_folder(folder)
+        series = gplates.VelBCSeries(V_BCs, t_files, f["PointID"], workloads.R_SURF)
+        out["gplates"] = {"files": len(V_BCs), "surface_nodes": int(V_BCs[0]["Uth_Uph"].shape[1]),
+                          "write_and_read_s": time.time() - t_rd,
+                          "source": "seeded exports in GPlates' five-column format (Euler-pole plates)"}
         steps = {}
         for name, prec, n in (("learned_fp32", 1, args.c5_steps), ("plain_fp64", 0, args.c5_plain_steps)):
             if n <= 0:
@@ -475,7 +488,8 @@ def c5_leg(args, wfile):
             dm.diffusion_setup(workloads.KAPPA, fix, T0[fix])
             dm.set_temperature(T0)
             infos = [dm.time_step(step_kw, slm=dict(method_BT="PC2", method_interp="cubic"), rock=rock,
-                                  smoother=prec, dt_adv_limit=0.005, dtmax=0.1, diffusion=True) for _ in range(n)]
+                                  smoother=prec, dt_adv_limit=0.005, dtmax=0.1, diffusion=True, vel_bcs=series)
+                     for _ in range(n)]
             t_st = sum(i["t_stokes_ms"] for i in infos) / 1e3
             t_ad = sum(i["t_advect_ms"] for i in infos) / 1e3
             steps[name] = {"steps": n, "s_per_step": sum(i["t_total_ms"] for i in infos) / 1e3 / n,
@@ -485,7 +499,8 @@ def c5_leg(args, wfile):
                            "its_per_step": [i["stokes"]["nitU"] + i["stokes"]["nitZ"] for i in infos],
                            "dt": [i["dt"] for i in infos], "locate_nties": sum(i["locate"]["nties"] for i in infos),
                            "locate_ngap": sum(i["locate"]["ngap"] for i in infos),
-                           "locate_nlost": sum(i["locate"]["nlost"] for i in infos)}
+                           "locate_nlost": sum(i["locate"]["nlost"] for i in infos),
+                           "vel_bc_update_ms_per_step": sum(i["t_vel_bc_ms"] for i in infos) / n}
         if steps:
             out["time_steps"] = steps
             if "learned_fp32" in steps and "plain_fp64" in steps:
@@ -702,6 +717,7 @@ def main():
     ap.add_argument("--c5-skip-plain", action="store_true", help="64M-DOF shell: no plain-FP64 1e-8 solve")
     ap.add_argument("--c5-steps", type=int, default=3, help="64M-DOF time steps with the learned + FP32-MG solve")
     ap.add_argument("--c5-plain-steps", type=int, default=1, help="64M-DOF time steps with the plain FP64 solve")
+    ap.add_argument("--c5-workload", default="c5", help="mesh of the time-step leg (a plate workload)")
     ap.add_argument("--jacobi-steps", type=int, default=3, help="timed Jacobi-smoothed comparison solves")
     ap.add_argument("--skip-learned", action="store_true", help="time the Jacobi-smoothed FP32 solve instead")
     ap.add_argument("--skip-jacobi", action="store_true", help="skip the Jacobi-smoothed comparison solve")

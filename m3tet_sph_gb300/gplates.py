@@ -238,12 +238,43 @@ def update_vel_bc(PointID, V_BCs, time_VBCs_files, model_time, r_surf, RR1=None,
     return dict(nfix=int(ifix.size), ifix=ifix, vfix=vfix, PlateInfo=plate_info, PLUME=plume), Plate
 
 
+def rotation_operator(latlon, r_surf, RR1=None, RR2=None):
+    """(n,2,2) per-point matrices A with A @ (theta, phi) = rotate_to_mesh_frame's result: the
+    frame change of update_vel_bc.m:66-81 is linear in the velocity and depends only on the
+    GPlates points, so a time loop forms it once (it agrees with the step-by-step form to rounding)."""
+    sph = np.array(latlon, dtype=np.float64)
+    sph[0] = 90.0 - sph[0]
+    sph = (np.pi / 180.0) * sph
+    sph = np.vstack([sph, r_surf * np.ones((1, sph.shape[1]))])
+    cart = meshmod.sph2cart(sph)
+    RR = (np.eye(3) if RR2 is None else np.asarray(RR2)) @ (np.eye(3) if RR1 is None else np.asarray(RR1))
+    F, Fr = _frames(cart), _frames(RR.T @ cart)
+    return np.einsum('nji,jk,nkl->nil', Fr, RR.T, F)[:, :2, :2]
+
+
 class VelBCSeries:
-    """A loaded GPlates series driving the surface velocities of a device-resident time loop."""
+    """A loaded GPlates series driving the surface velocities of a device-resident time loop. The
+    fixed-dof layout and the frame change are formed once; each step interpolates and applies them."""
 
     def __init__(self, V_BCs, time_VBCs_files, PointID, r_surf, RR1=None, RR2=None, UBC=None):
         self.V_BCs, self.times = V_BCs, np.asarray(time_VBCs_files, dtype=np.float64).ravel()
         self.PointID, self.r_surf, self.RR1, self.RR2, self.UBC = PointID, r_surf, RR1, RR2, UBC
+        # layout and plate lists from one full update_vel_bc at the first file's time
+        UBC0, _ = update_vel_bc(PointID, V_BCs, self.times, 0.0, r_surf, RR1, RR2, UBC)
+        self._ifix, self._plume = UBC0['ifix'], UBC0['PLUME']
+        ifix0 = self._ifix - 1
+        pid = np.asarray(PointID).ravel()
+        node, comp = ifix0 // 3, ifix0 % 3
+        surf_dof = (pid[node] == PID_SURF) & (comp < 2)
+        nplume = 0 if not self._plume else len(np.ravel(self._plume['iUfix_plume']))
+        surf_dof[self._ifix.size - nplume:] = False
+        self._th = np.nonzero(surf_dof & (comp == 0))[0]       # ascending node order = record order
+        self._ph = np.nonzero(surf_dof & (comp == 1))[0]
+        self._vfix0 = np.zeros(self._ifix.size)
+        if nplume:
+            self._vfix0[self._ifix.size - nplume:] = np.ravel(self._plume['vUfix_plume'])
+        self._A = rotation_operator(V_BCs[0]['latlon'], r_surf, RR1, RR2)
+        self._surf = pid == PID_SURF
 
     @classmethod
     def from_mat(cls, path, PointID, r_surf, **kw):
@@ -252,8 +283,16 @@ class VelBCSeries:
 
     def at(self, model_time):
         """(UBC, Plate) of update_vel_bc at the model time."""
-        return update_vel_bc(self.PointID, self.V_BCs, self.times, model_time, self.r_surf, self.RR1, self.RR2,
-                             self.UBC)
+        U, i0 = interpolate_velocities(self.V_BCs, self.times, model_time)
+        Ur = np.einsum('nij,jn->in', self._A, U)
+        vfix = self._vfix0.copy()
+        vfix[self._th] = Ur[0]
+        vfix[self._ph] = Ur[1]
+        plate_info = np.asarray(self.V_BCs[i0]['PlateID'], dtype=np.float64).ravel()
+        Plate = np.zeros(self._surf.size)
+        Plate[self._surf] = plate_info
+        return dict(nfix=int(self._ifix.size), ifix=self._ifix.copy(), vfix=vfix, PlateInfo=plate_info,
+                    PLUME=self._plume), Plate
 
     def apply(self, dm, model_time):
         """Push the prescribed velocities at ``model_time`` to the device (same fixed dofs as the

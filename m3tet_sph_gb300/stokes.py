@@ -274,10 +274,13 @@ class DeviceMesh:
 
         ``vel_bcs`` (a ``gplates.VelBCSeries``): the surface velocities at the model time of the
         step's start are pushed first (update_vel_bc before flow3d_patera_sph,
-        M3TET_SPH_SOUTH_ATLANTIC_PLUME.m:236-241); the step info then holds 'Plate' (VAR.Plate)."""
-        plate = None
+        M3TET_SPH_SOUTH_ATLANTIC_PLUME.m:236-241); the step info then holds 'Plate' (VAR.Plate) and
+        't_vel_bc_ms' (that host update)."""
+        plate, t_bc = None, 0.0
         if vel_bcs is not None:
+            t0 = time.perf_counter()
             _, plate = vel_bcs.apply(self, getattr(self, 'model_time', 0.0))
+            t_bc = (time.perf_counter() - t0) * 1e3
         kw = dict(rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20, target_rel_residual=0.0)
         kw.update(stokes_kw or {})
         slm = dict(slm or {})
@@ -300,6 +303,7 @@ class DeviceMesh:
             self.model_time = d['time']
         if plate is not None:
             d['Plate'] = plate
+            d['t_vel_bc_ms'] = t_bc       # host update_vel_bc + upload, before the device step
         return self._finish(code, d, allow_not_converged)
 
     def set_option(self, name, value):

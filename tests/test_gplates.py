@@ -180,3 +180,18 @@ def test_update_vel_bc_appends_plume_and_checks_boundaries(series, shell):
     pid[np.nonzero(pid == 0)[0][:3]] = 999
     with pytest.warns(UserWarning, match='999'):
         G.boundary_nodes(pid)
+
+
+@pytest.mark.parametrize('model_time', [0.0, 0.6, 2.0, 3.2])
+def test_series_equals_update_vel_bc(series, shell, model_time):
+    """The time-loop form (layout and frame change formed once) gives update_vel_bc's lists."""
+    from m3tet_sph_gb300 import gplates as G
+    plume = dict(iUbc_plume=2, iUfix_plume=[4, 5], vUfix_plume=[1.5, -2.5])
+    S = G.VelBCSeries(series['V'], series['t'], shell['PointID'], 6371.0, series['RR1'], series['RR2'],
+                      UBC=dict(PLUME=plume))
+    UBC, Plate = S.at(model_time)
+    ref, Plate_r = G.update_vel_bc(shell['PointID'], series['V'], series['t'], model_time, 6371.0,
+                                   series['RR1'], series['RR2'], UBC=dict(PLUME=plume))
+    assert np.array_equal(UBC['ifix'], ref['ifix']) and UBC['nfix'] == ref['nfix']
+    assert np.max(np.abs(UBC['vfix'] - ref['vfix'])) <= 1e-13 * np.max(np.abs(ref['vfix']))
+    assert np.array_equal(Plate, Plate_r) and np.array_equal(UBC['PlateInfo'], ref['PlateInfo'])
