@@ -166,16 +166,32 @@ def _frames(X):
     return meshmod.rotation_blocks(X)
 
 
-def rotate_to_mesh_frame(latlon, Uth_Uph, r_surf, RR1=None, RR2=None):
-    """update_vel_bc.m:66-81: (theta, phi) velocities of the GPlates points in the mesh frame."""
+def _earth_points(latlon, r_surf):
+    """update_vel_bc.m:66-70: GPlates (lat, lon) in degrees -> Cartesian points at the surface."""
     sph = np.array(latlon, dtype=np.float64)
     sph[0] = 90.0 - sph[0]
     sph = (np.pi / 180.0) * sph
     sph = np.vstack([sph, r_surf * np.ones((1, sph.shape[1]))])
-    cart = meshmod.sph2cart(sph)
+    return meshmod.sph2cart(sph)
+
+
+def _mesh_rotation(RR1=None, RR2=None):
+    """RR2 RR1: mesh frame -> GPlates (Earth) frame; its transpose brings GPlates data onto the mesh
+    (MESH.RR1/RR2 of an embedded mesh, load_mesh_sph.m:57-60; identity for a global mesh)."""
+    return (np.eye(3) if RR2 is None else np.asarray(RR2)) @ (np.eye(3) if RR1 is None else np.asarray(RR1))
+
+
+def earth_to_mesh_points(latlon, r_surf, RR1=None, RR2=None):
+    """update_vel_bc.m:77: the GPlates points in the mesh frame (3, n)."""
+    return _mesh_rotation(RR1, RR2).T @ _earth_points(latlon, r_surf)
+
+
+def rotate_to_mesh_frame(latlon, Uth_Uph, r_surf, RR1=None, RR2=None):
+    """update_vel_bc.m:66-81: (theta, phi) velocities of the GPlates points in the mesh frame."""
+    cart = _earth_points(latlon, r_surf)
     u_sph = np.vstack([Uth_Uph, np.zeros((1, Uth_Uph.shape[1]))])
     u_cart = np.einsum('nij,jn->in', _frames(cart), u_sph)
-    RR = (np.eye(3) if RR2 is None else np.asarray(RR2)) @ (np.eye(3) if RR1 is None else np.asarray(RR1))
+    RR = _mesh_rotation(RR1, RR2)
     u_cart_rot = RR.T @ u_cart
     cart_rot = RR.T @ cart
     u_sph_rot = np.einsum('nji,jn->in', _frames(cart_rot), u_cart_rot)
@@ -242,12 +258,8 @@ def rotation_operator(latlon, r_surf, RR1=None, RR2=None):
     """(n,2,2) per-point matrices A with A @ (theta, phi) = rotate_to_mesh_frame's result: the
     frame change of update_vel_bc.m:66-81 is linear in the velocity and depends only on the
     GPlates points, so a time loop forms it once (it agrees with the step-by-step form to rounding)."""
-    sph = np.array(latlon, dtype=np.float64)
-    sph[0] = 90.0 - sph[0]
-    sph = (np.pi / 180.0) * sph
-    sph = np.vstack([sph, r_surf * np.ones((1, sph.shape[1]))])
-    cart = meshmod.sph2cart(sph)
-    RR = (np.eye(3) if RR2 is None else np.asarray(RR2)) @ (np.eye(3) if RR1 is None else np.asarray(RR1))
+    cart = _earth_points(latlon, r_surf)
+    RR = _mesh_rotation(RR1, RR2)
     F, Fr = _frames(cart), _frames(RR.T @ cart)
     return np.einsum('nji,jk,nkl->nil', Fr, RR.T, F)[:, :2, :2]
 
@@ -312,8 +324,7 @@ def synthetic_vel_bcs(f, times=(103.0, 102.0, 101.0, 100.0), nplates=12, vmax_cm
     rng = np.random.default_rng(seed + 11)
     X = f['GCOORD']
     surf = np.nonzero(np.asarray(f['PointID']) == PID_SURF)[0]
-    RR = (np.eye(3) if RR2 is None else np.asarray(RR2)) @ (np.eye(3) if RR1 is None else np.asarray(RR1))
-    xe = RR @ X[:, surf]                                   # Earth-frame positions
+    xe = _mesh_rotation(RR1, RR2) @ X[:, surf]              # Earth-frame positions
     S = meshmod.cart2sph(xe)
     lat = 90.0 - np.rad2deg(S[0])
     lon = np.rad2deg(S[1])

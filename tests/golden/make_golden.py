@@ -3,6 +3,9 @@
 * earthshell_n37k.npz: the reference's shipped curved P2 mesh
   (SETUP_TEST/MESHES/EarthShell_n37k.mat, produced by tetmesh_p1_to_p2_sph): vertex
   coordinates, 10-node connectivity (0-based), all node coordinates and PointIDs.
+* earthshell_n37k_frame.json: the same file's frame data: RR1_center, RR2_center (the rotations
+  between the GPlates (Earth) frame and the mesh frame that update_vel_bc.m:76-77 applies) and the
+  refined region's centre in both frames (theta_center, phi_center; theta0, phi0; degrees).
 * quadrature_14.json: the numeric values of the 14-point rule documented in
   mfiles_M3TET/ip_tetrahedron.m:109-117 (read from the comments as text).
 
@@ -25,6 +28,10 @@ def main(ref):
     el = m.EL2NOD.astype(np.int64).T - 1
     np.savez_compressed(HERE / 'earthshell_n37k.npz', EL2NOD=el.astype(np.int32), GCOORD=m.GCOORD.T.copy(),
                         PointID=m.PointID.astype(np.int32), r_cmb=float(m.r_cmb), r_surf=float(m.r_surf))
+    frame = dict(RR1_center=m.RR1_center.tolist(), RR2_center=m.RR2_center.tolist(),
+                 theta_center=float(m.theta_center), phi_center=float(m.phi_center),
+                 theta0=float(m.theta0), phi0=float(m.phi0))
+    (HERE / 'earthshell_n37k_frame.json').write_text(json.dumps(frame, indent=1, sort_keys=True) + '\n')
     txt = (ref / 'mfiles_M3TET/ip_tetrahedron.m').read_text(errors='replace').splitlines()
     vals = {}
     for ln in txt[108:118]:

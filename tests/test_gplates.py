@@ -195,3 +195,54 @@ def test_series_equals_update_vel_bc(series, shell, model_time):
     assert np.array_equal(UBC['ifix'], ref['ifix']) and UBC['nfix'] == ref['nfix']
     assert np.max(np.abs(UBC['vfix'] - ref['vfix'])) <= 1e-13 * np.max(np.abs(ref['vfix']))
     assert np.array_equal(Plate, Plate_r) and np.array_equal(UBC['PlateInfo'], ref['PlateInfo'])
+
+
+# ---- the reference's shipped embedded mesh (SETUP_TEST/MESHES/EarthShell_n37k.mat) and its frame ----
+
+@pytest.fixture(scope='module')
+def ref_mesh():
+    import json
+    from pathlib import Path
+    g = Path(__file__).resolve().parent / 'golden'
+    d = np.load(g / 'earthshell_n37k.npz')
+    fr = json.loads((g / 'earthshell_n37k_frame.json').read_text())
+    f = dict(GCOORD=d['GCOORD'].T.copy(), PointID=d['PointID'].astype(np.int64))
+    return f, fr, float(d['r_surf'])
+
+
+def test_reference_frame_puts_the_refined_region_at_the_mesh_centre(ref_mesh):
+    """Pinned against the reference's mesh file: (RR2 RR1)^T takes the refined region's centre given
+    in the GPlates frame (theta_center, phi_center = 128, 353 degrees: the South Atlantic) onto the
+    mesh frame's (theta0, phi0) = (90, 90), the convention update_vel_bc.m:71-77 states."""
+    from m3tet_sph_gb300 import gplates as G, mesh as M
+    f, fr, r_surf = ref_mesh
+    lat, lon = 90.0 - fr['theta_center'], fr['phi_center']
+    p = G.earth_to_mesh_points(np.array([[lat], [lon]]), r_surf, fr['RR1_center'], fr['RR2_center'])
+    th, ph, r = M.cart2sph(p)[:, 0]
+    assert abs(np.rad2deg(th) - fr['theta0']) < 1e-12 and abs(np.rad2deg(ph) - fr['phi0']) < 1e-12
+    assert abs(r - r_surf) < 1e-9
+
+
+def test_update_vel_bc_on_the_reference_mesh(ref_mesh, tmp_path):
+    """A seeded series on the reference mesh's 3,954 surface nodes, written in the Earth frame of its
+    own RR1/RR2: update_vel_bc matches the oracle, brings every record back onto its surface node,
+    and leaves free slip on its 162 core-mantle-boundary nodes."""
+    from m3tet_sph_gb300 import gplates as G
+    f, fr, r_surf = ref_mesh
+    RR1, RR2 = np.array(fr['RR1_center']), np.array(fr['RR2_center'])
+    folder = G.write_synthetic_folder(tmp_path, G.synthetic_vel_bcs(f, seed=7, RR1=RR1, RR2=RR2))
+    V, t = G.read_vel_gplates_folder(folder)
+    surf = np.nonzero(f['PointID'] == G.PID_SURF)[0]
+    assert V[0]['Uth_Uph'].shape == (2, surf.size) == (2, 3954)
+    # the records sit on the mesh's surface nodes once rotated (10 decimals of a degree in the files)
+    p = G.earth_to_mesh_points(V[0]['latlon'], r_surf, RR1, RR2)
+    assert np.max(np.linalg.norm(p - f['GCOORD'][:, surf], axis=0)) < 1e-5
+    for mt in (0.0, 1.4):
+        UBC, Plate = G.update_vel_bc(f['PointID'], V, t, mt, r_surf, RR1, RR2)
+        ifix, vfix, Plate_r = BO.update_vel_bc(f['PointID'], V, t, mt, r_surf, RR1, RR2)
+        assert np.array_equal(UBC['ifix'], ifix) and np.array_equal(Plate, Plate_r)
+        assert np.max(np.abs(UBC['vfix'] - vfix)) <= 1e-13 * np.max(np.abs(vfix))
+        S = G.VelBCSeries(V, t, f['PointID'], r_surf, RR1, RR2)
+        U2, _ = S.at(mt)
+        assert np.max(np.abs(U2['vfix'] - vfix)) <= 1e-13 * np.max(np.abs(vfix))
+    assert UBC['nfix'] == 162 + 3 * 3954
