@@ -1,6 +1,6 @@
 """ORACLE (test infrastructure only): CPU FP64 restatement of the reference's Stokes hot path.
 
-This module is the checker for the CUDA library, and the timed CPU baseline. Only tests,
+This module checks the CUDA library's results and is the timed CPU baseline. Only tests,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it. It shares no code
 with the product kernels: the element operator, assembly, rotation, boundary conditions,
 Galerkin restriction, coarse Cholesky, MG-PCG and Patera pressure CG are restated here in
@@ -323,8 +323,7 @@ def local_coords_3d(Xc, EL4, els, pts):
     x4 = Xc[:, EL4[els, 3]]
     A = np.stack([Xc[:, EL4[els, 0]] - x4, Xc[:, EL4[els, 1]] - x4, Xc[:, EL4[els, 2]] - x4], axis=2)
     b = (pts - x4).T[:, :, None]
-    return np.linalg.solve(A.transpose(1, 0, 2).transpose(0, 1, 2).reshape(-1, 3, 3) if False else
-                           np.moveaxis(A, 1, 0), b)[:, :, 0].T
+    return np.linalg.solve(np.moveaxis(A, 1, 0), b)[:, :, 0].T
 
 
 def intermesh_transfer_matrix(Xs_f, EL_f, Xs_c, EL_c):
