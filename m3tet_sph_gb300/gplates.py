@@ -85,16 +85,21 @@ def write_vel_gplates(path, LatLon, PlateID, Ucolat_Ulon_cm_yr):
 
 
 def read_vel_gplates_folder(folder):
-    """SAVE_GPLATES_VEL_BCS_TO_MAT_FILE.m:51-81: every ``<t>Ma.txt`` of a folder, 1-Myr apart,
-    starting from the time in the last file name (three digits) and going down. Returns
-    (V_BCs list of dicts, time_VBCs_files)."""
+    """SAVE_GPLATES_VEL_BCS_TO_MAT_FILE.m:51-81: every ``<t>Ma.txt`` of a folder (or ``<t>Ma.xy``, the
+    extension GPlates writes, which the reference renames to .txt first), 1-Myr apart, starting from
+    the time in the last file name (three digits) and going down. Returns (V_BCs list of dicts,
+    time_VBCs_files)."""
+    ext = '.txt'
     files = sorted(Path(folder).glob('*.txt'), key=lambda p: p.name)
     if not files:
-        raise ValueError('no GPlates velocity files (.txt) in the folder')
+        ext = '.xy'
+        files = sorted(Path(folder).glob('*.xy'), key=lambda p: p.name)
+    if not files:
+        raise ValueError('no GPlates velocity files (.txt or .xy) in the folder')
     t = float(files[-1].name[:3])
     V_BCs, times = [], []
     for _ in files:
-        U, ll, pid, names = read_vel_gplates(Path(folder) / f'{int(t)}Ma.txt')
+        U, ll, pid, names = read_vel_gplates(Path(folder) / f'{int(t)}Ma{ext}')
         V_BCs.append(dict(time=t, Uth_Uph=U, latlon=ll, PlateID=pid, plateid2name=names))
         times.append(t)
         t -= 1.0

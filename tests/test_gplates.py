@@ -65,6 +65,18 @@ def test_reader_matches_oracle(series):
     assert np.array_equal(series['t'], [103.0, 102.0, 101.0, 100.0])
 
 
+def test_folder_of_xy_exports(series, tmp_path):
+    """GPlates writes .xy files; the folder reader takes them as the reference does after renaming."""
+    from m3tet_sph_gb300 import gplates as G
+    for p in series['folder'].glob('*.txt'):
+        (tmp_path / (p.stem + '.xy')).write_text(p.read_text())
+    V, t = G.read_vel_gplates_folder(tmp_path)
+    assert np.array_equal(t, series['t'])
+    assert all(np.array_equal(a['Uth_Uph'], b['Uth_Uph']) for a, b in zip(V, series['V']))
+    with pytest.raises(ValueError, match='no GPlates'):
+        G.read_vel_gplates_folder(tmp_path / 'missing')
+
+
 def test_mat_round_trip(series, tmp_path):
     from m3tet_sph_gb300 import gplates as G
     p = tmp_path / 'Vel_BCs_test.mat'
