@@ -314,7 +314,9 @@ M3SPH_API int m3sph_tsearch_sph(m3sph_mesh *mesh, const double *thphr, int32_t n
  * *ms = mean time per location, info = counts of the last one. */
 M3SPH_API int m3sph_locate_timing(m3sph_mesh *mesh, const double *thphr, int32_t npt, int32_t nrep, double *ms,
                                   m3sph_locate_info *info);
-/* Replaces interp3d_tet (interp3d_tet.m:39-69): V is nnod x nvar (nvar <= 3), Vi npt x nvar. */
+/* Replaces interp3d_tet (interp3d_tet.m:39-69): V is nnod x nvar (nvar <= 3), Vi npt x nvar.
+ * els are 1-based ids of finest-level elements; an id outside 1..nel is M3SPH_ERR_BAD_INPUT (the
+ * reference's indexing error). npt = 0 does nothing. The same holds for m3sph_interp3d_cubic. */
 M3SPH_API int m3sph_interp3d_tet(m3sph_mesh *mesh, const int32_t *els, const double *lc, int32_t npt,
                                  const double *V, int32_t nvar, int32_t monotonic, double *Vi);
 /* Replaces interp3d_cubic_p (interp3d_cubic_p.m:80-382) for one nodal field V (nnod). */
@@ -326,7 +328,8 @@ M3SPH_API int m3sph_interp3d_cubic(m3sph_mesh *mesh, const int32_t *els, const d
  * streams that a cudaMalloc / cudaFree (which may synchronise the device) would stall.
  * els (npt, 1-based), lc (npt x 3), V (nnod) and Vi (npt) must be memory the device can access
  * (device, managed or mapped pinned host memory), with the inputs complete before the call; the
- * work runs on the handle's stream (m3sph_stream), which is synchronised before returning.
+ * work runs on the handle's stream (m3sph_stream), which is synchronised before returning. The ids
+ * are not read on the host: a point whose id is outside 1..nel gets NaN.
  * Scratch lives in one fixed 8 MiB array per device that every call shares (7 values per element
  * + 4 per vertex, about 120k elements of a spherical-shell mesh; larger meshes are rejected with
  * M3SPH_ERR_BAD_INPUT). The array's device address is looked up, and this entry point's kernels

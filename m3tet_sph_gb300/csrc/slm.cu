@@ -599,7 +599,7 @@ __global__ void k_interp_p2(SlmMesh m, const int *__restrict__ els, const double
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npt) return;
   const int e = els[i];
-  if (e < 0) {
+  if (e < 0 || e >= m.nel) {
     for (int k = 0; k < nvar; ++k) out[(size_t)k * npt + i] = nan("");
     return;
   }
@@ -677,7 +677,7 @@ __global__ void k_cubic_interp(SlmMesh m, const double *__restrict__ X, const in
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npt) return;
   const int e = els[i];
-  if (e < 0) {
+  if (e < 0 || e >= m.nel) {
     out[i] = nan("");
     return;
   }
@@ -1183,6 +1183,18 @@ static SlmState *slm_state(m3sph_mesh *M) { return reinterpret_cast<SlmState *>(
 
 using namespace m3sph;
 
+// element ids of interp3d_tet / interp3d_cubic_p callers: 1-based, within the mesh (the reference
+// indexes EL2NOD with them, so any other value is an error there too)
+static int check_element_ids(const int32_t *els, int npt, int nel, const char *fn) {
+  for (int i = 0; i < npt; ++i)
+    if (els[i] < 1 || els[i] > nel) {
+      set_error(std::string(fn) + ": element id " + std::to_string(els[i]) + " at point " + std::to_string(i + 1) +
+                " is outside 1.." + std::to_string(nel));
+      return M3SPH_ERR_BAD_INPUT;
+    }
+  return M3SPH_OK;
+}
+
 static int slm_check(m3sph_mesh *M) {
   if (!M || !M->slm) {
     set_error("mesh handle without advection data");
@@ -1260,12 +1272,14 @@ extern "C" int m3sph_interp3d_tet(m3sph_mesh *M, const int32_t *els, const doubl
                                   int32_t nvar, int32_t monotonic, double *Vi) {
   int st = slm_check(M);
   if (st) return st;
-  if (npt <= 0 || nvar < 1 || nvar > 3 || !els || !lc || !V || !Vi) {
+  if (npt < 0 || nvar < 1 || nvar > 3 || (npt > 0 && (!els || !lc || !V || !Vi))) {
     set_error("m3sph_interp3d_tet: bad arguments");
     return M3SPH_ERR_BAD_INPUT;
   }
+  if (npt == 0) return M3SPH_OK;
   SlmState *S = slm_state(M);
   Level &L0 = M->lev[0];
+  if ((st = check_element_ids(els, npt, L0.nel, "m3sph_interp3d_tet"))) return st;
   if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
   cudaStream_t s = M->stream;
   std::vector<int> e(npt);
@@ -1293,12 +1307,14 @@ extern "C" int m3sph_interp3d_cubic(m3sph_mesh *M, const int32_t *els, const dou
                                     int32_t monotonic, int32_t method_wght, double *Vi) {
   int st = slm_check(M);
   if (st) return st;
-  if (npt <= 0 || !els || !lc || !V || !Vi) {
+  if (npt < 0 || (npt > 0 && (!els || !lc || !V || !Vi))) {
     set_error("m3sph_interp3d_cubic: bad arguments");
     return M3SPH_ERR_BAD_INPUT;
   }
+  if (npt == 0) return M3SPH_OK;
   SlmState *S = slm_state(M);
   Level &L0 = M->lev[0];
+  if ((st = check_element_ids(els, npt, L0.nel, "m3sph_interp3d_cubic"))) return st;
   if ((st = slm_reserve(S, npt, L0.nel, L0.nnod, L0.nvnod))) return st;
   cudaStream_t s = M->stream;
   std::vector<int> e(npt);
@@ -1627,10 +1643,11 @@ extern "C" int m3sph_interp3d_cubic_noalloc(m3sph_mesh *M, const int32_t *els, c
                                             const double *V, int32_t monotonic, int32_t method_wght, double *Vi) {
   int st = slm_check(M);
   if (st) return st;
-  if (npt <= 0 || !els || !lc || !V || !Vi) {
+  if (npt < 0 || (npt > 0 && (!els || !lc || !V || !Vi))) {
     set_error("m3sph_interp3d_cubic_noalloc: bad arguments");
     return M3SPH_ERR_BAD_INPUT;
   }
+  if (npt == 0) return M3SPH_OK;
   SlmState *S = slm_state(M);
   Level &L0 = M->lev[0];
   const size_t nel = L0.nel, nv = L0.nvnod;

@@ -188,3 +188,28 @@ def test_advection_with_zero_velocity_regions(mesh_case):
     assert np.array_equal(WS['els_INTERP'] - 1, e2)
     assert WS['locate_info']['nties'] > 0
     assert np.abs(Tg - Tr).max() < 1e-10
+
+
+def test_empty_inputs_and_element_id_range(tiny):
+    """No points is a no-op for location and both interpolations; interpolation ids outside 1..nel
+    are rejected on the host (the reference's own indexing error) before anything runs."""
+    from m3tet_sph_gb300 import _lib as L, advection as A, stokes
+    f = tiny['levels'][0]
+    dm = stokes.DeviceMesh(tiny['levels'])
+    try:
+        els, lc, info = A.tsearch2_sph(dm, np.zeros((3, 0)))
+        assert els.shape == (0,) and lc.shape == (3, 0) and info['npt'] == 0
+        T = np.linspace(0.0, 1.0, f['nnod'])
+        assert A.interp3d_tet(dm, np.zeros(0, np.int32), np.zeros((3, 0)), T).shape == (0,)
+        assert A.interp3d_cubic_p(dm, np.zeros(0, np.int32), np.zeros((3, 0)), T).shape == (0,)
+        lc1 = np.full((3, 2), 0.25)
+        for bad in ([1, f['nel'] + 1], [0, 1], [-3, 1]):
+            with pytest.raises(L.M3SphError, match='outside 1'):
+                A.interp3d_tet(dm, np.array(bad, np.int32), lc1, T)
+            with pytest.raises(L.M3SphError, match='outside 1'):
+                A.interp3d_cubic_p(dm, np.array(bad, np.int32), lc1, T)
+        # the first and the last element are valid ids; P2 weights at the centroid sum to one
+        v = A.interp3d_tet(dm, np.array([1, f['nel']], np.int32), lc1, np.ones(f['nnod']))
+        assert np.allclose(v, 1.0, rtol=0, atol=1e-14)
+    finally:
+        dm.close()
