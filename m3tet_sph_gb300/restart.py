@@ -8,8 +8,9 @@ The reference writes with MATLAB's ``save`` (default format: MAT v7, zlib-compre
 * ``load_restart_file`` (mfiles_M3TET/load_restart_data.m:296-311) reads either: ``time`` (or
   ``time_yr``), ``istep``, ``VAR`` and ``iplot`` if present.
 ``<prefix>`` is COMM.prefix, ``Lab<nsd,2 digits>x<myid,2 digits>`` (init_COMM.m:26): ``Lab01x01`` for
-the serial curved-mesh code. VAR holds nodal column vectors (Ux Uy Uz Uth Uph Ur T Dens Visc) and the
-vertex pressure P. scipy.io writes the same v5 elements with compression, which MATLAB's ``load`` reads.
+the serial curved-mesh code. VAR holds nodal column vectors (Ux Uy Uz Uth Uph Ur T Dens Visc), the
+vertex pressure P, and in GPlates runs the surface plate indices Plate. scipy.io writes the same v5
+elements with compression, which MATLAB's ``load`` reads.
 """
 from __future__ import annotations
 
@@ -20,7 +21,9 @@ import scipy.io as sio
 
 from . import mesh as meshmod
 
-VAR_FIELDS = ('Ux', 'Uy', 'Uz', 'Uth', 'Uph', 'Ur', 'P', 'T', 'Dens', 'Visc')
+# Plate: the plate index of each surface node that update_vel_bc sets in GPlates runs
+# (update_vel_bc.m:151-152), written when the caller's VAR holds it
+VAR_FIELDS = ('Ux', 'Uy', 'Uz', 'Uth', 'Uph', 'Ur', 'P', 'T', 'Dens', 'Visc', 'Plate')
 
 
 def prefix(COMM=None):

@@ -43,3 +43,15 @@ def test_round_trip(tmp_path):
     sio.savemat(q, d)
     V3, time, istep, iplot = R.load_restart_file(q)
     assert time == 12.0 and iplot is None and np.array_equal(V3['P'], VAR['P'])
+
+
+def test_plate_field_of_gplates_runs(tmp_path):
+    """VAR.Plate (update_vel_bc.m:151-152) is written and read back with the other nodal fields."""
+    from m3tet_sph_gb300 import restart as R
+    VAR = _var(9, 4, 2)
+    VAR['Plate'] = np.array([0, 0, 3, 3, 12, 0, 1, 1, 0], dtype=np.float64)
+    p = R.write_output_file({'outdir': str(tmp_path)}, VAR, None, 0.5, 1, 0.1, 1)
+    v = sio.loadmat(p)['VAR'][0, 0]
+    assert v['Plate'].shape == (9, 1)
+    V2, *_ = R.load_restart_file(p)
+    assert np.array_equal(V2['Plate'], VAR['Plate'])
