@@ -240,12 +240,11 @@ def update_vel_bc(PointID, V_BCs, time_VBCs_files, model_time, r_surf, RR1=None,
     vfix = np.zeros(int(cnt.sum()))
     c = DBindx == PID_CMB
     ifix[start[c]] = 3 * (DBnods[c] + 1)
-    s = DBindx == PID_SURF
-    k = np.arange(surf.size)
+    s = DBindx == PID_SURF                     # the k-th surface node takes the k-th record
     ifix[start[s]] = 3 * (DBnods[s] + 1) - 2
-    vfix[start[s]] = Uth_Uph[0, k]
+    vfix[start[s]] = Uth_Uph[0]
     ifix[start[s] + 1] = 3 * (DBnods[s] + 1) - 1
-    vfix[start[s] + 1] = Uth_Uph[1, k]
+    vfix[start[s] + 1] = Uth_Uph[1]
     ifix[start[s] + 2] = 3 * (DBnods[s] + 1)
     plume = (UBC or {}).get('PLUME') or None
     if plume:
