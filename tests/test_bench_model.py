@@ -1,0 +1,44 @@
+"""The bench's size and byte models against the shell counts and the per-unit figures they restate:
+closed-form node / element counts of the three shells, and the algorithmic bytes of one operator
+apply (x and y in the vector precision, 10 int32 connectivity entries and a class byte per element,
+vertex (theta, phi, r) and viscosity)."""
+import pytest
+
+
+@pytest.mark.parametrize('level,nlayer,nel,nnod,nP', [
+    (3, 8, 30_720, 43_554, 5_778),            # 130,662 velocity DOF
+    (5, 32, 1_966_080, 2_662_530, 337_986),   # 7,987,590 velocity DOF
+    (6, 64, 15_728_640, 21_135_618, 2_662_530),  # 63,406,854 velocity DOF
+])
+def test_shell_counts(level, nlayer, nel, nnod, nP):
+    from m3tet_sph_gb300 import mesh as M
+    c = M.mesh_counts(level, nlayer)
+    assert (c['nel'], c['nnod'], c['nP']) == (nel, nnod, nP)
+
+
+def test_built_shell_matches_the_counts():
+    from m3tet_sph_gb300 import mesh as M
+    lv = M.build_hierarchy(3, 8, 3)
+    for j, (L, n) in enumerate([(3, 8), (2, 4), (1, 2)]):
+        c = M.mesh_counts(L, n)
+        assert lv[j]['nel'] == c['nel'] and lv[j]['nnod'] == c['nnod']
+        assert int(lv[j]['EL2NOD'][:, :4].max()) + 1 == c['nP']
+
+
+def test_algorithmic_apply_bytes():
+    import bench
+    from m3tet_sph_gb300 import mesh as M
+    c5, c2 = M.mesh_counts(6, 64), M.mesh_counts(5, 32)
+    # 64M-DOF shell, FP64: 0.507 + 0.507 + 0.629 + 0.016 + 0.064 + 0.021 GB
+    b5 = bench.algorithmic_apply_bytes(c5['nel'], 3 * c5['nnod'], c5['nP'], 8)
+    assert b5 == 2 * 8 * 63_406_854 + 41 * 15_728_640 + 32 * 2_662_530
+    assert abs(b5 / 1e9 - 1.74) < 0.01
+    # 8M-DOF shell: 219 MB in FP64 (the double-float outer apply's roofline), 155 MB in FP32
+    b2 = bench.algorithmic_apply_bytes(c2['nel'], 3 * c2['nnod'], c2['nP'], 8)
+    assert abs(b2 / 1e6 - 219.2) < 0.1
+    b2f = bench.algorithmic_apply_bytes(c2['nel'], 3 * c2['nnod'], c2['nP'], 4)
+    assert abs(b2f / 1e6 - 155.3) < 0.1
+    # streamed bytes of the partially assembled FP32 apply on the 491,520-element profiling shell
+    cp = M.mesh_counts(5, 8)
+    assert abs(bench.apply_bytes_pa(cp['nel'], 3 * cp['nnod'], cp['nnod']) / 1e9 - 0.297) < 0.001
+    assert abs(bench.apply_bytes(cp['nel'], 3 * cp['nnod'], 4) / 1e9 - 0.951) < 0.001
