@@ -194,6 +194,16 @@ def unique_bars(T4):
     return bars, el2bar
 
 
+def _marked(ids, n, drop=None):
+    """Sorted distinct values of non-negative ids below n (np.unique's result), minus ``drop``
+    (np.setdiff1d's), by marking instead of sorting."""
+    m = np.zeros(n, bool)
+    m[ids] = True
+    if drop is not None:
+        m[drop] = False
+    return np.nonzero(m)[0]
+
+
 def _mid_in_frame(Xc, bars, R):
     """Spherical midpoints of bars computed in the frame rotated by R (no phi unwrap)."""
     Sr = cart2sph(R @ Xc)
@@ -233,17 +243,18 @@ def promote_p2_sph(Xc, Sc, T4, pid_c, r_cmb, r_surf, theta_cone_deg=45.0):
     tc = np.deg2rad(theta_cone_deg)
     in_cone = cls >= CLS_IN_NO_ISO
     if in_cone.any():
-        cone_bars = np.unique(el2bar[in_cone].ravel())
         iso = cls == CLS_IN_ISO
+        drop = None
         if iso.any():
-            iso_bars = np.unique(el2bar[iso].ravel())
+            iso_bars = _marked(el2bar[iso].ravel(), nbar)
             thb = Sc[0][bars[iso_bars]]
             out2 = np.sum((thb > tc) & (thb < np.pi - tc), axis=1) == 2
-            cone_bars = np.setdiff1d(cone_bars, iso_bars[out2])
+            drop = iso_bars[out2]
+        cone_bars = _marked(el2bar[in_cone].ravel(), nbar, drop)
         mid[:, cone_bars] = _mid_in_frame(Xc, bars[cone_bars], RR_X_90_CCW)
     cross = cls == CLS_OUT_CROSS
     if cross.any():
-        cb = np.unique(el2bar[cross].ravel())
+        cb = _marked(el2bar[cross].ravel(), nbar)
         mid[:, cb] = _mid_in_frame(Xc, bars[cb], RR_Z_180)
     EL2NOD = np.concatenate([T4, nV + el2bar], axis=1).astype(np.int64)
     S = np.concatenate([Sc, mid], axis=1)
