@@ -185,12 +185,19 @@ def unique_bars(T4):
     e = T4[:, EDGES].reshape(-1, 2)
     n = int(T4.max()) + 1
     key = np.minimum(e[:, 0], e[:, 1]) * n + np.maximum(e[:, 0], e[:, 1])
-    _, first, inv = np.unique(key, return_index=True, return_inverse=True)
-    order = np.argsort(first, kind='stable')
-    rank = np.empty_like(order)
-    rank[order] = np.arange(len(order))
-    bars = e[first[order]]
-    el2bar = rank[inv].reshape(-1, 6)
+    perm = np.argsort(key, kind='stable')
+    ks = key[perm]
+    new = np.empty(ks.size, bool)
+    new[0] = True
+    np.not_equal(ks[1:], ks[:-1], out=new[1:])
+    first = perm[new]                            # first occurrence of each edge (stable sort)
+    is_first = np.zeros(key.size, bool)
+    is_first[first] = True
+    bar_at = np.cumsum(is_first) - 1             # bar id of a first occurrence, in occurrence order
+    grp = np.empty(key.size, np.int64)
+    grp[perm] = np.cumsum(new) - 1               # edge group of every occurrence
+    el2bar = bar_at[first][grp].reshape(-1, 6)
+    bars = e[is_first]
     return bars, el2bar
 
 
