@@ -42,3 +42,10 @@ def test_algorithmic_apply_bytes():
     cp = M.mesh_counts(5, 8)
     assert abs(bench.apply_bytes_pa(cp['nel'], 3 * cp['nnod'], cp['nnod']) / 1e9 - 0.297) < 0.001
     assert abs(bench.apply_bytes(cp['nel'], 3 * cp['nnod'], 4) / 1e9 - 0.951) < 0.001
+
+
+def test_extra_leg_reports_failures():
+    import bench
+    assert bench.extra_leg(lambda a, b: {"x": a + b}, 1, 2) == {"x": 3}
+    r = bench.extra_leg(lambda: 1 / 0)
+    assert r["error"].startswith("ZeroDivisionError")
