@@ -1,7 +1,8 @@
-"""The bench's size and byte models against the shell counts and the per-unit figures they restate:
-closed-form node / element counts of the three shells, and the algorithmic bytes of one operator
-apply (x and y in the vector precision, 10 int32 connectivity entries and a class byte per element,
-vertex (theta, phi, r) and viscosity)."""
+"""The bench's host side: its size and byte models against the shell counts and the per-unit figures
+they restate (closed-form node / element counts of the three shells; the algorithmic bytes of one
+operator apply: x and y in the vector precision, 10 int32 connectivity entries and a class byte per
+element, vertex (theta, phi, r) and viscosity), the reporting of failed side legs, and the CPU
+reference arm's JSON line."""
 import pytest
 
 
@@ -49,3 +50,26 @@ def test_extra_leg_reports_failures():
     assert bench.extra_leg(lambda a, b: {"x": a + b}, 1, 2) == {"x": 3}
     r = bench.extra_leg(lambda: 1 / 0)
     assert r["error"].startswith("ZeroDivisionError")
+
+
+def test_reference_arm_line():
+    """`bench.py --impl reference` (one timed FP64 oracle solve of the 130,662-DOF shell on the host
+    threads) prints one JSON line with the contract's keys and a converged solve."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
+                       cwd=root, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "s" and d["higher_is_better"] is False
+    assert d["value"] > 0 and d["steps"] == 1 and d["n_gpus"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "coupled residual" in d["cpu_baseline"]["sample"]
+    res = float(d["cpu_baseline"]["sample"].split("to a ")[1].split(" coupled")[0])
+    assert res < 1e-8
