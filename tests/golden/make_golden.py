@@ -8,6 +8,8 @@
   refined region's centre in both frames (theta_center, phi_center; theta0, phi0; degrees).
 * quadrature_14.json: the numeric values of the 14-point rule documented in
   mfiles_M3TET/ip_tetrahedron.m:109-117 (read from the comments as text).
+* quadrature_4.json: the two coordinates of the 4-point rule documented in
+  mfiles_M3TET/ip_tetrahedron.m:41-42 (the comments' eight decimals).
 
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
@@ -39,7 +41,13 @@ def main(ref):
         if mm:
             vals[mm.group(1)] = float(mm.group(2))
     (HERE / 'quadrature_14.json').write_text(json.dumps(vals, indent=1, sort_keys=True) + '\n')
-    print(sorted(vals.items()))
+    vals4 = {}
+    for ln in txt[38:48]:
+        mm = re.match(r'\s*([ab])\s*=.*%\s*([0-9.]+)', ln)
+        if mm:
+            vals4[mm.group(1)] = float(mm.group(2))
+    (HERE / 'quadrature_4.json').write_text(json.dumps(vals4, indent=1, sort_keys=True) + '\n')
+    print(sorted(vals.items()), sorted(vals4.items()))
 
 
 if __name__ == '__main__':

@@ -22,6 +22,19 @@ def test_quadrature_matches_documented_values():
     assert abs((ipw * r ** 2 * s * t).sum() - 2.0 / 5040.0) < 1e-17
 
 
+def test_four_point_rule_matches_documented_values():
+    """The diffusion operator's 4-point rule against the values ip_tetrahedron.m:41-42 documents
+    (eight decimals): point k has coordinate a in direction k and b in the others, weights 1/4."""
+    from oracle import thermal_oracle as TO
+    vals = json.loads((GOLD / 'quadrature_4.json').read_text())
+    assert abs(TO.IPX[0, 0] - vals['a']) < 5e-9 and abs(TO.IPX[1, 0] - vals['b']) < 5e-9
+    assert np.array_equal(TO.IPX, [[TO._A, TO._B, TO._B, TO._B], [TO._B, TO._A, TO._B, TO._B],
+                                   [TO._B, TO._B, TO._A, TO._B]])
+    assert np.array_equal(TO.IPW, [0.25] * 4)
+    # degree-2 exactness: the mean of r^2 over the unit tet is 2!/(2+3)! * 6 = 1/10
+    assert abs((TO.IPW * TO.IPX[0] ** 2).sum() - 0.1) < 1e-15
+
+
 def test_shape_function_derivatives_fd():
     rng = np.random.default_rng(0)
     for fn, n in ((O.sf10, 10), (O.sf20, 20)):
