@@ -10,6 +10,8 @@
   mfiles_M3TET/ip_tetrahedron.m:109-117 (read from the comments as text).
 * quadrature_4.json: the two coordinates of the 4-point rule documented in
   mfiles_M3TET/ip_tetrahedron.m:41-42 (the comments' eight decimals).
+* scaling_mantle.json: the 'mantle' units of mfiles_M3TET/numerical_eq_scaling.m:20-27 (L0, t0 = Myr,
+  Visc0, Dens0), which the seeded workloads use.
 
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
@@ -47,7 +49,18 @@ def main(ref):
         if mm:
             vals4[mm.group(1)] = float(mm.group(2))
     (HERE / 'quadrature_4.json').write_text(json.dumps(vals4, indent=1, sort_keys=True) + '\n')
-    print(sorted(vals.items()), sorted(vals4.items()))
+    sc = {}
+    src = (ref / 'mfiles_M3TET/numerical_eq_scaling.m').read_text(errors='replace').splitlines()
+    blk = src[src.index(next(ln for ln in src if "case 'mantle'" in ln)):]
+    blk = blk[:next(i for i, ln in enumerate(blk[1:], 1) if ln.strip().startswith('case'))]
+    for ln in blk:
+        mm = re.match(r'\s*(Myr|NUMSCALE\.(L0|t0|Visc0|Dens0))\s*=\s*([^;]+);', ln)
+        if mm:
+            expr = mm.group(3).strip()
+            v = sc['Myr'] if expr == 'Myr' else float(np.prod([float(f) for f in expr.split('*')]))
+            sc[mm.group(2) or 'Myr'] = v
+    (HERE / 'scaling_mantle.json').write_text(json.dumps(sc, indent=1, sort_keys=True) + '\n')
+    print(sorted(vals.items()), sorted(vals4.items()), sorted(sc.items()))
 
 
 if __name__ == '__main__':

@@ -35,6 +35,19 @@ def test_four_point_rule_matches_documented_values():
     assert abs((TO.IPW * TO.IPX[0] ** 2).sum() - 0.1) < 1e-15
 
 
+def test_workload_units_are_the_reference_mantle_scaling():
+    """The seeded workloads' units are numerical_eq_scaling('mantle') (values read from the
+    reference source): L0 = 1 km, t0 = 1 Myr, Visc0 = 2e18 Pa s, Dens0 = 3300, and the derived
+    U0 = L0/t0 and Bscale = L0^2/(Visc0 U0) of numerical_eq_scaling.m:51-64."""
+    from m3tet_sph_gb300 import workloads as W
+    sc = json.loads((GOLD / 'scaling_mantle.json').read_text())
+    for k in ('L0', 't0', 'Visc0', 'Dens0'):
+        assert W.SCALE[k] == sc[k], k
+    U0 = sc['L0'] / sc['t0']
+    assert W.SCALE['U0'] == U0 and W.SCALE['Bscale'] == sc['L0'] ** 2 / (sc['Visc0'] * U0)
+    assert W.physics()['Bscale'] == W.SCALE['Bscale'] and W.physics()['Dens0'] == sc['Dens0']
+
+
 def test_shape_function_derivatives_fd():
     rng = np.random.default_rng(0)
     for fn, n in ((O.sf10, 10), (O.sf20, 20)):
