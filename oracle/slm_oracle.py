@@ -106,6 +106,9 @@ def sf10(r, s, t):
     return N, dN
 
 
+NEWTON_STEPS, NEWTON_TOL = 6, 1e-8      # local_coords_curved_3d_sph.m: nimprove, delTH_tol
+
+
 def local_coords_curved(SX, EL, els, pX):
     """local_coords_curved_3d_sph: linear guess + up to 6 Newton steps on the 10-node map in the
     X-90 frame; a point stops once its own error is below 1e-8. Returns lc and the sum of |delS| of
@@ -115,12 +118,12 @@ def local_coords_curved(SX, EL, els, pX):
     G = SX[:, EL[els]]                      # (3,n,10)
     step = np.zeros(lc.shape[1])
     active = np.ones(lc.shape[1], bool)
-    for _ in range(6):
+    for _ in range(NEWTON_STEPS):
         N, dN = sf10(*lc)                   # N (10,n), dN (10,3,n)
         TH0 = np.einsum('kni,in->kn', G, N)
         dTH = pX - TH0
         err = np.sqrt((dTH * dTH).sum(0))
-        active &= ~(err < 1e-8)
+        active &= ~(err < NEWTON_TOL)
         if not active.any():
             break
         a = np.nonzero(active)[0]

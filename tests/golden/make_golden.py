@@ -12,6 +12,11 @@
   mfiles_M3TET/ip_tetrahedron.m:41-42 (the comments' eight decimals).
 * scaling_mantle.json: the 'mantle' units of mfiles_M3TET/numerical_eq_scaling.m:20-27 (L0, t0 = Myr,
   Visc0, Dens0), which the seeded workloads use.
+* reference_constants.json: solver and location constants read from the source: the V-cycle's
+  Jacobi weights ('Setup 3', mgpcg_solver_p.m:674-682), the Patera defaults
+  (flow3d_patera_mg_sph_p.m:70-93), the gap tolerance growth
+  (locate_points_in_neighboring_element.m:3,24) and the curved Newton iteration
+  (local_coords_curved_3d_sph.m:62-64).
 
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
@@ -60,7 +65,40 @@ def main(ref):
             v = sc['Myr'] if expr == 'Myr' else float(np.prod([float(f) for f in expr.split('*')]))
             sc[mm.group(2) or 'Myr'] = v
     (HERE / 'scaling_mantle.json').write_text(json.dumps(sc, indent=1, sort_keys=True) + '\n')
+    (HERE / 'reference_constants.json').write_text(json.dumps(reference_constants(ref), indent=1,
+                                                              sort_keys=True) + '\n')
     print(sorted(vals.items()), sorted(vals4.items()), sorted(sc.items()))
+
+
+def _assign(path, name):
+    """The right-hand side of the first ``name = value;`` line of a reference file, as text."""
+    for ln in path.read_text(errors='replace').splitlines():
+        mm = re.match(r'\s*' + re.escape(name) + r'\s*=\s*([^;%]+);', ln)
+        if mm:
+            return mm.group(1).strip()
+    raise KeyError(f'{name} not found in {path}')
+
+
+def _vec(txt):
+    return [float(v) for v in txt.strip('[] ').split()]
+
+
+def reference_constants(ref):
+    mg = ref / 'mfiles_M3TET/mgpcg_solver_p.m'
+    pat = ref / 'mfiles_M3TET/flow3d_patera_mg_sph_p.m'
+    nb = ref / 'mfiles_M3TET/locate_points_in_neighboring_element.m'
+    lcc = ref / 'mfiles_SPH/local_coords_curved_3d_sph.m'
+    gap_max = re.search(r'while isempty\(iel_ok_nb\) && tol <= ([0-9.e-]+)', nb.read_text()).group(1)
+    return {
+        'mgpcg_weights': {'finest_down': _vec(_assign(mg, 'Jwght_down{1}')),
+                          'finest_up': _vec(_assign(mg, 'Jwght_up{1}')),
+                          'other_down': _vec(_assign(mg, 'Jwght_down{jmg}'))},
+        'patera': {'rtol_Pat': float(_assign(pat, 'rtol_Pat')), 'itmin_Pat': int(_assign(pat, 'itmin_Pat')),
+                   'itmax_Pat': int(_assign(pat, 'itmax_Pat')), 'rtol_U': float(_assign(pat, 'rtol_U')),
+                   'itmax_U': int(_assign(pat, 'itmax_U')), 'rtol_restart': _assign(pat, 'rtol_restart')},
+        'location': {'gap_step': float(_assign(nb, 'tol_step')), 'gap_max': float(gap_max),
+                     'newton_tol': float(_assign(lcc, 'delTH_tol')), 'newton_steps': int(_assign(lcc, 'nimprove'))},
+    }
 
 
 if __name__ == '__main__':

@@ -48,6 +48,31 @@ def test_workload_units_are_the_reference_mantle_scaling():
     assert W.physics()['Bscale'] == W.SCALE['Bscale'] and W.physics()['Dens0'] == sc['Dens0']
 
 
+def test_solver_and_location_constants_are_the_reference_values():
+    """Constants read from the reference source (tests/golden/reference_constants.json): the V-cycle's
+    Jacobi weights, the Patera defaults of the oracle and of the library's Python mirror, and the
+    location's gap tolerance growth and curved Newton iteration."""
+    import inspect
+    import scipy.sparse as sp
+    from oracle import slm_oracle as SO
+    from m3tet_sph_gb300 import stokes
+    c = json.loads((GOLD / 'reference_constants.json').read_text())
+    w = c['mgpcg_weights']
+    eye = sp.identity(3, format='csr')
+    mg = O.MGPCG(eye, [np.ones(3), eye, eye], [eye, eye], 3)
+    assert mg.wd == [w['finest_down'], w['other_down']]
+    assert mg.wu == [w['finest_up'], w['other_down'][::-1]]
+    pat = c['patera']
+    assert pat['rtol_restart'] == '0.8*rtol_Pat'
+    for fn in (O.patera, stokes.DeviceMesh.solve, stokes.DeviceMesh.step_device):
+        par = inspect.signature(fn).parameters
+        for k in ('rtol_Pat', 'rtol_U', 'itmax_Pat', 'itmin_Pat', 'itmax_U'):
+            assert par[k].default == pat[k], (fn.__name__, k)
+    loc = c['location']
+    assert SO.GAP_STEP == loc['gap_step'] and abs(SO.GAP_QMAX * SO.GAP_STEP - loc['gap_max']) < 1e-15
+    assert (SO.NEWTON_STEPS, SO.NEWTON_TOL) == (loc['newton_steps'], loc['newton_tol'])
+
+
 def test_shape_function_derivatives_fd():
     rng = np.random.default_rng(0)
     for fn, n in ((O.sf10, 10), (O.sf20, 20)):
