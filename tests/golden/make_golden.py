@@ -15,8 +15,9 @@
 * reference_constants.json: solver and location constants read from the source: the V-cycle's
   Jacobi weights ('Setup 3', mgpcg_solver_p.m:674-682), the Patera defaults
   (flow3d_patera_mg_sph_p.m:70-93), the gap tolerance growth
-  (locate_points_in_neighboring_element.m:3,24) and the curved Newton iteration
-  (local_coords_curved_3d_sph.m:62-64).
+  (locate_points_in_neighboring_element.m:3,24), the curved Newton iteration
+  (local_coords_curved_3d_sph.m:62-64), rock_prop's gas constant (rock_prop.m:67) and the plume
+  model's conductivity, heat capacity and density (model_parameters_sph_south_atlantic_plume.m:453,483-484).
 
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
@@ -88,6 +89,8 @@ def reference_constants(ref):
     pat = ref / 'mfiles_M3TET/flow3d_patera_mg_sph_p.m'
     nb = ref / 'mfiles_M3TET/locate_points_in_neighboring_element.m'
     lcc = ref / 'mfiles_SPH/local_coords_curved_3d_sph.m'
+    rock = ref / 'mfiles_M3TET/rock_prop.m'
+    mp = ref / 'SETUP_TEST/model_parameters_sph_south_atlantic_plume.m'
     gap_max = re.search(r'while isempty\(iel_ok_nb\) && tol <= ([0-9.e-]+)', nb.read_text()).group(1)
     return {
         'mgpcg_weights': {'finest_down': _vec(_assign(mg, 'Jwght_down{1}')),
@@ -98,6 +101,9 @@ def reference_constants(ref):
                    'itmax_U': int(_assign(pat, 'itmax_U')), 'rtol_restart': _assign(pat, 'rtol_restart')},
         'location': {'gap_step': float(_assign(nb, 'tol_step')), 'gap_max': float(gap_max),
                      'newton_tol': float(_assign(lcc, 'delTH_tol')), 'newton_steps': int(_assign(lcc, 'nimprove'))},
+        'rock_prop': {'R': float(_assign(rock, 'R'))},
+        'plume_model': {'K': float(_assign(mp, 'PHYSICS.K')), 'Cp': float(_assign(mp, 'PHYSICS.Cp')),
+                        'Dens': float(_assign(mp, 'PHYSICS.Dens'))},
     }
 
 

@@ -71,6 +71,12 @@ def test_solver_and_location_constants_are_the_reference_values():
     loc = c['location']
     assert SO.GAP_STEP == loc['gap_step'] and abs(SO.GAP_QMAX * SO.GAP_STEP - loc['gap_max']) < 1e-15
     assert (SO.NEWTON_STEPS, SO.NEWTON_TOL) == (loc['newton_steps'], loc['newton_tol'])
+    # rock_prop's gas constant; the time steps' diffusivity K / (rho Cp) of the plume model in model units
+    from m3tet_sph_gb300 import workloads as W
+    assert O.ROCK_R == c['rock_prop']['R']
+    pm = c['plume_model']
+    kappa_si = pm['K'] / (pm['Dens'] * pm['Cp'])
+    assert abs(W.KAPPA - kappa_si / (W.SCALE['L0'] ** 2 / W.SCALE['t0'])) < 1e-12 * W.KAPPA
 
 
 def test_shape_function_derivatives_fd():
