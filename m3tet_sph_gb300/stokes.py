@@ -57,6 +57,7 @@ class DeviceMesh:
         self.ndof = 3 * self.nnod
         self.nvnod = int(f['EL2NOD'][:, :4].max()) + 1
         self.precision = None
+        self.model_time = 0.0          # model time of the resident time series (set_temperature, time_step)
 
     def close(self):
         if getattr(self, 'h', None):
@@ -279,7 +280,7 @@ class DeviceMesh:
         plate, t_bc = None, 0.0
         if vel_bcs is not None:
             t0 = time.perf_counter()
-            _, plate = vel_bcs.apply(self, getattr(self, 'model_time', 0.0))
+            _, plate = vel_bcs.apply(self, self.model_time)
             t_bc = (time.perf_counter() - t0) * 1e3
         kw = dict(rtol_Pat=1e-4, rtol_U=5e-3, itmax_Pat=120, itmin_Pat=3, itmax_U=20, target_rel_residual=0.0)
         kw.update(stokes_kw or {})
